@@ -1,0 +1,379 @@
+/*
+ * am_ref_shim.h -- host stand-ins that let the reference's own CUDA sources
+ * compile as plain C++ with OpenMP, so the reference marching loop can run on
+ * the CPU.  TEST INFRASTRUCTURE ONLY: used by oracle/build_ref.py to build
+ * oracle/_ref/libamref.so, the parity pin for the oracle and the timed CPU
+ * baseline.  Nothing in the product links it.
+ *
+ * Mapping (all kernels in the reference are one-thread-per-item with no
+ * shared memory, no barriers and no warp intrinsics, so a parallel loop over
+ * the flattened thread index runs them faithfully):
+ *   kernel<<<g, b>>>(args)  -> amref_launch(g, b, lambda) : omp parallel for
+ *   threadIdx/blockIdx/...  -> thread_local variables set per iteration
+ *   atomic*                 -> GCC __atomic builtins
+ *   cublas{S,D}gemm[...]    -> plain loop GEMM with cuBLAS column-major semantics
+ *   cudaMalloc/Memcpy/...   -> host memory
+ *   torch::Tensor           -> a view over (pointer, sizes, dtype)
+ */
+#ifndef AM_REF_SHIM_H
+#define AM_REF_SHIM_H
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <functional>
+#include <iostream>
+#include <numeric>
+#include <string>
+#include <sys/types.h>
+#include <type_traits>
+#include <vector>
+
+/* ------------------------------------------------------------------ CUDA */
+#define __global__
+#define __device__
+#define __host__
+#define __forceinline__ inline
+
+struct amref_dim3 {
+    unsigned int x, y, z;
+};
+static thread_local amref_dim3 threadIdx = {0, 0, 0};
+static thread_local amref_dim3 blockIdx = {0, 0, 0};
+static thread_local amref_dim3 blockDim = {1, 1, 1};
+static thread_local amref_dim3 gridDim = {1, 1, 1};
+
+template <class F>
+inline void amref_launch(long grid, long block, F &&f)
+{
+    if (grid <= 0 || block <= 0) return; /* an empty launch does nothing on the GPU either */
+    const long total = grid * block;
+#pragma omp parallel for schedule(static)
+    for (long t = 0; t < total; ++t) {
+        blockIdx.x = (unsigned)(t / block);
+        threadIdx.x = (unsigned)(t % block);
+        blockDim.x = (unsigned)block;
+        gridDim.x = (unsigned)grid;
+        f();
+    }
+}
+
+typedef int cudaError_t;
+typedef void *cudaStream_t;
+typedef void *cudaEvent_t;
+#define cudaSuccess 0
+enum { cudaMemcpyHostToHost = 0, cudaMemcpyHostToDevice = 1, cudaMemcpyDeviceToHost = 2, cudaMemcpyDeviceToDevice = 3 };
+inline const char *cudaGetErrorString(cudaError_t) { return "host shim error"; }
+
+template <class T>
+inline cudaError_t cudaMalloc(T **p, size_t bytes)
+{
+    *p = (T *)calloc(bytes ? bytes : 1, 1);
+    return *p ? 0 : 2;
+}
+inline cudaError_t cudaFree(void *p)
+{
+    free(p);
+    return 0;
+}
+inline cudaError_t cudaMemcpy(void *d, const void *s, size_t n, int)
+{
+    if (n) memmove(d, s, n);
+    return 0;
+}
+inline cudaError_t cudaMemcpyAsync(void *d, const void *s, size_t n, int, cudaStream_t = 0)
+{
+    if (n) memmove(d, s, n);
+    return 0;
+}
+inline cudaError_t cudaMemset(void *d, int v, size_t n)
+{
+    memset(d, v, n);
+    return 0;
+}
+inline cudaError_t cudaDeviceSynchronize() { return 0; }
+inline cudaError_t cudaSetDevice(int) { return 0; }
+
+inline float rsqrtf(float x) { return 1.0f / sqrtf(x); }
+inline double rsqrt(double x) { return 1.0 / sqrt(x); }
+inline long long __double_as_longlong(double d)
+{
+    long long r;
+    memcpy(&r, &d, 8);
+    return r;
+}
+inline double __longlong_as_double(long long v)
+{
+    double r;
+    memcpy(&r, &v, 8);
+    return r;
+}
+inline unsigned int __float_as_uint(float f)
+{
+    unsigned int r;
+    memcpy(&r, &f, 4);
+    return r;
+}
+inline float __uint_as_float(unsigned int v)
+{
+    float r;
+    memcpy(&r, &v, 4);
+    return r;
+}
+
+inline int atomicAdd(int *a, int v) { return __atomic_fetch_add(a, v, __ATOMIC_SEQ_CST); }
+inline int atomicMax(int *a, int v)
+{
+    int old = __atomic_load_n(a, __ATOMIC_SEQ_CST);
+    while (old < v && !__atomic_compare_exchange_n(a, &old, v, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST)) {
+    }
+    return old;
+}
+inline int atomicOr(int *a, int v) { return __atomic_fetch_or(a, v, __ATOMIC_SEQ_CST); }
+template <class T>
+inline T amref_cas(T *a, T cmp, T val)
+{
+    T expected = cmp;
+    __atomic_compare_exchange_n(a, &expected, val, false, __ATOMIC_SEQ_CST, __ATOMIC_SEQ_CST);
+    return expected; /* old value, as CUDA's atomicCAS returns */
+}
+inline int atomicCAS(int *a, int c, int v) { return amref_cas(a, c, v); }
+inline unsigned int atomicCAS(unsigned int *a, unsigned int c, unsigned int v) { return amref_cas(a, c, v); }
+inline unsigned long long atomicCAS(unsigned long long *a, unsigned long long c, unsigned long long v)
+{
+    return amref_cas(a, c, v);
+}
+
+/* ------------------------------------------------------------------ cuBLAS */
+typedef int *cublasHandle_t;
+typedef enum {
+    CUBLAS_STATUS_SUCCESS = 0,
+    CUBLAS_STATUS_NOT_INITIALIZED = 1,
+    CUBLAS_STATUS_ALLOC_FAILED = 3,
+    CUBLAS_STATUS_INVALID_VALUE = 7,
+    CUBLAS_STATUS_ARCH_MISMATCH = 8,
+    CUBLAS_STATUS_MAPPING_ERROR = 11,
+    CUBLAS_STATUS_EXECUTION_FAILED = 13,
+    CUBLAS_STATUS_INTERNAL_ERROR = 14,
+    CUBLAS_STATUS_NOT_SUPPORTED = 15,
+    CUBLAS_STATUS_LICENSE_ERROR = 16
+} cublasStatus_t;
+typedef enum { CUBLAS_OP_N = 0, CUBLAS_OP_T = 1 } cublasOperation_t;
+
+inline cublasStatus_t cublasCreate(cublasHandle_t *h)
+{
+    static int dummy;
+    *h = &dummy;
+    return CUBLAS_STATUS_SUCCESS;
+}
+inline cublasStatus_t cublasDestroy(cublasHandle_t) { return CUBLAS_STATUS_SUCCESS; }
+
+/* column-major C(m x n) = alpha op(A) op(B) + beta C, summing k in order */
+template <class T>
+inline void amref_gemm_one(cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, T alpha, const T *A, int lda,
+                           const T *B, int ldb, T beta, T *C, int ldc)
+{
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < m; ++i) {
+            T acc = 0;
+            for (int l = 0; l < k; ++l) {
+                T a = (ta == CUBLAS_OP_N) ? A[i + (long)l * lda] : A[l + (long)i * lda];
+                T b = (tb == CUBLAS_OP_N) ? B[l + (long)j * ldb] : B[j + (long)l * ldb];
+                acc += a * b;
+            }
+            T *c = C + i + (long)j * ldc;
+            *c = (beta == T(0)) ? alpha * acc : alpha * acc + beta * *c;
+        }
+}
+
+template <class T>
+inline cublasStatus_t amref_gemm(cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, const T *alpha, const T *A,
+                                 int lda, const T *B, int ldb, const T *beta, T *C, int ldc)
+{
+#pragma omp parallel for schedule(static)
+    for (int j = 0; j < n; ++j) {
+        const T *Bj = (tb == CUBLAS_OP_N) ? B + (long)j * ldb : B + j;
+        amref_gemm_one<T>(ta, tb, m, 1, k, *alpha, A, lda, (tb == CUBLAS_OP_N) ? Bj : Bj, ldb, *beta, C + (long)j * ldc, ldc);
+    }
+    return CUBLAS_STATUS_SUCCESS;
+}
+
+template <class T>
+inline cublasStatus_t amref_gemm_sb(cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k, const T *alpha,
+                                    const T *A, int lda, long long sA, const T *B, int ldb, long long sB, const T *beta,
+                                    T *C, int ldc, long long sC, int batch)
+{
+#pragma omp parallel for schedule(static)
+    for (int p = 0; p < batch; ++p)
+        amref_gemm_one<T>(ta, tb, m, n, k, *alpha, A + p * sA, lda, B + p * sB, ldb, *beta, C + p * sC, ldc);
+    return CUBLAS_STATUS_SUCCESS;
+}
+
+inline cublasStatus_t cublasSgemm(cublasHandle_t, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
+                                  const float *al, const float *A, int lda, const float *B, int ldb, const float *be,
+                                  float *C, int ldc)
+{
+    return amref_gemm<float>(ta, tb, m, n, k, al, A, lda, B, ldb, be, C, ldc);
+}
+inline cublasStatus_t cublasDgemm(cublasHandle_t, cublasOperation_t ta, cublasOperation_t tb, int m, int n, int k,
+                                  const double *al, const double *A, int lda, const double *B, int ldb, const double *be,
+                                  double *C, int ldc)
+{
+    return amref_gemm<double>(ta, tb, m, n, k, al, A, lda, B, ldb, be, C, ldc);
+}
+inline cublasStatus_t cublasSgemmStridedBatched(cublasHandle_t, cublasOperation_t ta, cublasOperation_t tb, int m, int n,
+                                                int k, const float *al, const float *A, int lda, long long sA,
+                                                const float *B, int ldb, long long sB, const float *be, float *C, int ldc,
+                                                long long sC, int batch)
+{
+    return amref_gemm_sb<float>(ta, tb, m, n, k, al, A, lda, sA, B, ldb, sB, be, C, ldc, sC, batch);
+}
+inline cublasStatus_t cublasDgemmStridedBatched(cublasHandle_t, cublasOperation_t ta, cublasOperation_t tb, int m, int n,
+                                                int k, const double *al, const double *A, int lda, long long sA,
+                                                const double *B, int ldb, long long sB, const double *be, double *C,
+                                                int ldc, long long sC, int batch)
+{
+    return amref_gemm_sb<double>(ta, tb, m, n, k, al, A, lda, sA, B, ldb, sB, be, C, ldc, sC, batch);
+}
+template <class T>
+inline cublasStatus_t amref_geam(cublasOperation_t ta, cublasOperation_t tb, int m, int n, const T *al, const T *A, int lda,
+                                 const T *be, const T *B, int ldb, T *C, int ldc)
+{
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < m; ++i) {
+            T a = (ta == CUBLAS_OP_N) ? A[i + (long)j * lda] : A[j + (long)i * lda];
+            T b = (tb == CUBLAS_OP_N) ? B[i + (long)j * ldb] : B[j + (long)i * ldb];
+            C[i + (long)j * ldc] = *al * a + *be * b;
+        }
+    return CUBLAS_STATUS_SUCCESS;
+}
+inline cublasStatus_t cublasSgeam(cublasHandle_t, cublasOperation_t ta, cublasOperation_t tb, int m, int n, const float *al,
+                                  const float *A, int lda, const float *be, const float *B, int ldb, float *C, int ldc)
+{
+    return amref_geam<float>(ta, tb, m, n, al, A, lda, be, B, ldb, C, ldc);
+}
+inline cublasStatus_t cublasDgeam(cublasHandle_t, cublasOperation_t ta, cublasOperation_t tb, int m, int n,
+                                  const double *al, const double *A, int lda, const double *be, const double *B, int ldb,
+                                  double *C, int ldc)
+{
+    return amref_geam<double>(ta, tb, m, n, al, A, lda, be, B, ldb, C, ldc);
+}
+inline cublasStatus_t cublasSaxpy(cublasHandle_t, int n, const float *al, const float *x, int incx, float *y, int incy)
+{
+    for (int i = 0; i < n; ++i) y[(long)i * incy] += *al * x[(long)i * incx];
+    return CUBLAS_STATUS_SUCCESS;
+}
+inline cublasStatus_t cublasDaxpy(cublasHandle_t, int n, const double *al, const double *x, int incx, double *y, int incy)
+{
+    for (int i = 0; i < n; ++i) y[(long)i * incy] += *al * x[(long)i * incx];
+    return CUBLAS_STATUS_SUCCESS;
+}
+
+/* ------------------------------------------------------------------ torch */
+namespace at {
+enum class ScalarType { Float, Double, Int, Bool };
+}
+namespace torch {
+using at::ScalarType;
+struct Tensor {
+    void *ptr = nullptr;
+    int64_t sizes[2] = {0, 0};
+    int ndim = 0;
+    at::ScalarType st = at::ScalarType::Float;
+    template <class T>
+    T *data_ptr() const
+    {
+        return (T *)ptr;
+    }
+    int64_t size(int i) const { return sizes[i]; }
+    at::ScalarType scalar_type() const { return st; }
+};
+} // namespace torch
+
+#define AT_DISPATCH_FLOATING_TYPES(TYPE, NAME, ...)           \
+    do {                                                      \
+        if ((TYPE) == at::ScalarType::Double) {               \
+            using scalar_t = double;                          \
+            (__VA_ARGS__)();                                  \
+        } else {                                              \
+            using scalar_t = float;                           \
+            (__VA_ARGS__)();                                  \
+        }                                                     \
+    } while (0)
+
+/* ------------------------------------------------------------------ sort */
+/* sortDistance (process.h:244-264) does a stable global sort of the
+ * distances (descending) carrying (segment, index) through a zip iterator,
+ * then a stable sort by segment.  The net effect is a per-segment stable
+ * descending sort.  Host thrust's zip-iterator stable_sort_by_key corrupts
+ * its payload in this toolkit, so this computes the same permutation with
+ * std::stable_sort per segment (NaN ordered last). */
+template <class T, class V>
+inline void amref_sort_segments(T *value, V &segments, V &key_vec, int one_batch_len, int batch_num)
+{
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int s = 0; s < batch_num; ++s) {
+        std::vector<int> perm(one_batch_len);
+        std::iota(perm.begin(), perm.end(), 0);
+        const T *v = value + (long)s * one_batch_len;
+        std::stable_sort(perm.begin(), perm.end(), [v](int a, int b) {
+            T va = v[a], vb = v[b];
+            if (va != va) return false;
+            if (vb != vb) return true;
+            return va > vb;
+        });
+        std::vector<T> tmp(one_batch_len);
+        for (int q = 0; q < one_batch_len; ++q) tmp[q] = v[perm[q]];
+        for (int q = 0; q < one_batch_len; ++q) {
+            value[(long)s * one_batch_len + q] = tmp[q];
+            segments[(long)s * one_batch_len + q] = s;
+            key_vec[(long)s * one_batch_len + q] = perm[q];
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ records */
+/* One record per popped region, captured after corrNormDir and before
+ * inferAndAppend (cuam_kernel.cu:90-93), whose push_back reuses the popped
+ * FACEDATA slots. */
+struct amref_records {
+    int N = 0, words = 0, vm = 0;
+    std::vector<uint32_t> bits;
+    std::vector<int> nverts, ntab, tab, start;
+    std::vector<double> verts, mid;
+    void clear()
+    {
+        bits.clear(); nverts.clear(); ntab.clear(); tab.clear(); start.clear(); verts.clear(); mid.clear();
+    }
+};
+static amref_records g_amref_rec;
+
+template <class V, class T, class FD>
+inline void amref_record(V &var, const T *states_buffer, const FD *faces, int batch)
+{
+    amref_records &r = g_amref_rec;
+    const int N = var.states.state_len;
+    const int VM = var.VERT_MAX;
+    r.N = N;
+    r.vm = VM;
+    r.words = (N + 31) / 32;
+    for (int b = 0; b < batch; ++b) {
+        std::vector<uint32_t> w(r.words, 0u);
+        for (int k = 0; k < N; ++k)
+            if (states_buffer[(long)b * N + k] != T(0)) w[k >> 5] |= 1u << (k & 31);
+        r.bits.insert(r.bits.end(), w.begin(), w.end());
+        const T *vt = var.vertices_buffer + (long)b * (1 + 3 * VM);
+        const int *tb = var.tabij + (long)b * (2 + VM);
+        r.nverts.push_back((int)vt[0]);
+        for (int q = 0; q < 3 * VM; ++q) r.verts.push_back((double)vt[1 + q]);
+        r.ntab.push_back(tb[0]);
+        for (int q = 0; q < VM + 1; ++q) r.tab.push_back(tb[1 + q]);
+        for (int q = 0; q < 3; ++q) r.mid.push_back((double)faces[b].midpoint[q]);
+        r.start.push_back(faces[b].start_idx);
+    }
+}
+
+#endif
