@@ -1,0 +1,74 @@
+"""ctypes binding of include/analyticmesh_gb300.h (libamgb300.so).
+
+The library is built in-tree by ``analyticmesh_gb300.build``.  There is no
+fallback: if the library is missing or fails to load, every entry point
+raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+_LIB = None
+
+
+class AmStats(C.Structure):
+    _fields_ = [
+        ("num_regions", C.c_int64), ("num_faces", C.c_int64), ("num_seeds", C.c_int64),
+        ("num_nostart", C.c_int64), ("num_open", C.c_int64), ("num_truncated", C.c_int64),
+        ("num_singular", C.c_int64), ("mesh_num_verts", C.c_int64), ("mesh_num_faces", C.c_int64),
+        ("mesh_num_indices", C.c_int64), ("chunks", C.c_int32), ("max_polygon_verts", C.c_int32),
+        ("am_time_ms", C.c_double), ("compose_ms", C.c_double), ("polygon_ms", C.c_double),
+        ("frontier_ms", C.c_double), ("kernel_launches", C.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+AM_OPT_CHUNK = 1
+AM_OPT_PHASE_TIMING = 2
+
+
+class AmError(RuntimeError):
+    pass
+
+
+def lib():
+    """Load libamgb300.so (building it when the sources are newer)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path) or os.environ.get("AM_REBUILD"):
+        path = _build.build()
+    L = C.CDLL(path)
+    vp, i32p = C.c_void_p, C.POINTER(C.c_int32)
+    L.am_init.argtypes = [C.POINTER(vp), C.c_char_p, i32p, C.c_int, i32p, C.c_int, C.c_int, C.c_int]
+    L.am_analytic_marching.argtypes = [vp, vp, vp, vp, vp, C.c_int, vp, i32p, C.c_int, vp, vp, C.c_double, C.c_int, vp]
+    L.am_combine_mesh.argtypes = [vp, C.c_double, C.POINTER(C.c_double)]
+    L.am_export_mesh.argtypes = [vp, C.c_char_p, C.c_int, C.c_int]
+    L.am_destroy.argtypes = [vp]
+    L.am_strerror.restype = C.c_char_p
+    L.am_strerror.argtypes = [C.c_int]
+    L.am_last_error.restype = C.c_char_p
+    L.am_last_error.argtypes = [vp]
+    L.am_get_stats.argtypes = [vp, C.POINTER(AmStats)]
+    L.am_get_mesh.argtypes = [vp, vp, vp, vp]
+    L.am_get_regions.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
+    L.am_set_option.argtypes = [vp, C.c_int, C.c_int64]
+    _LIB = L
+    return L
+
+
+def check(rc: int, handle=None):
+    if rc != 0:
+        L = lib()
+        detail = L.am_last_error(handle).decode() if handle else ""
+        raise AmError("%s%s" % (L.am_strerror(rc).decode(), (": " + detail) if detail else ""))
+
+
+def vert_capacity() -> int:
+    return lib().am_vert_capacity()

@@ -1,0 +1,790 @@
+// am_engine.cpp -- host driver of the GB300 Analytic Marching engine and the
+// C ABI declared in include/analyticmesh_gb300.h.
+//
+// The marching loop processes the append-only region store FIFO in chunks:
+// compose every region of the chunk, build its face polygon and insert its
+// neighbours, append the new regions at the tail.  One stream, no host work
+// inside a chunk; the host reads the new tail once per chunk.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/analyticmesh_gb300.h"
+#include "am_internal.h"
+#include "am_mesh.h"
+
+using namespace am;
+
+namespace {
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { reset(); }
+    void reset()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    cudaError_t alloc(size_t n)
+    {
+        reset();
+        if (n == 0) n = 16;
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e == cudaSuccess) bytes = n;
+        else p = nullptr;
+        return e;
+    }
+    // grow keeping the first `keep` bytes
+    cudaError_t grow(size_t n, size_t keep, cudaStream_t st)
+    {
+        if (n <= bytes) return cudaSuccess;
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, n);
+        if (e != cudaSuccess) return e;
+        if (p && keep) {
+            e = cudaMemcpyAsync(q, p, std::min(keep, bytes), cudaMemcpyDeviceToDevice, st);
+            if (e != cudaSuccess) {
+                cudaFree(q);
+                return e;
+            }
+            cudaStreamSynchronize(st);
+        }
+        if (p) cudaFree(p);
+        p = q;
+        bytes = n;
+        return cudaSuccess;
+    }
+    template <class T>
+    T *as() const
+    {
+        return (T *)p;
+    }
+};
+
+struct Failure {
+    int code;
+    std::string msg;
+};
+
+#define AM_CUDA(x)                                                                                \
+    do {                                                                                          \
+        cudaError_t e_ = (x);                                                                     \
+        if (e_ != cudaSuccess) {                                                                  \
+            throw Failure{e_ == cudaErrorMemoryAllocation ? AM_ERR_OUT_OF_MEMORY : AM_ERR_CUDA,   \
+                          std::string(#x) + ": " + cudaGetErrorString(e_)};                       \
+        }                                                                                         \
+    } while (0)
+
+#define AM_CHECK(cond, msg)                                                     \
+    do {                                                                        \
+        if (!(cond)) throw Failure{AM_ERR_INVALID_ARGUMENT, std::string(msg)}; \
+    } while (0)
+
+bool is_device_ptr(const void *p)
+{
+    if (!p) return false;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// copy n bytes from a host or device pointer to a device buffer
+void upload(DevBuf &dst, const void *src, size_t n, cudaStream_t st)
+{
+    AM_CUDA(dst.alloc(n));
+    if (n) AM_CUDA(cudaMemcpyAsync(dst.p, src, n, is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
+}
+
+void to_host(void *dst, const void *src, size_t n, cudaStream_t st)
+{
+    if (!n) return;
+    AM_CUDA(cudaMemcpyAsync(dst, src, n, is_device_ptr(src) ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost, st));
+}
+
+} // namespace
+
+struct am_engine {
+    int prec = kFloat32;
+    std::vector<int> nodes;
+    std::vector<int32_t> arc;
+    int arc_cols = 1;
+    int n_lin = 0, N = 0, E = 0, ALL = 0, ALLP = 0, W = 0;
+    size_t tc = 4, ts = 4; // constraint / solve element sizes
+    cudaStream_t own = nullptr, st = nullptr;
+    std::string last_error;
+    int64_t chunk_opt = 0;
+    bool phase_timing = false;
+
+    // network
+    DevBuf wt[kMaxLayers], bias[kMaxLayers], w0, tmt[64], wext, bext, scratch;
+    NetDev net{};
+    // regions
+    DevBuf keys, hash, mid, start, nv, status, verts, edges;
+    long long cap = 0;
+    DevBuf table;
+    unsigned long long hcap = 0;
+    // chunk
+    DevBuf cons, eq, rec, blocksum;
+    int chunk_cap = 0;
+    // seeds
+    DevBuf s_states, s_keys, s_hash, s_pts, s_rec;
+    // counters
+    DevBuf d_tail, d_err;
+    // results
+    bool has_am = false, has_mesh = false;
+    long long num_regions = 0;
+    am_stats stats{};
+    int flip = 0;
+    // mesh
+    DevBuf w_table, w_rep, w_flag, w_vidx, w_bsum, w_fflag, w_fsize, w_fid, w_foff, w_verts, w_fs, w_fi, w_counts;
+    std::vector<double> mesh_verts;
+    std::vector<int32_t> mesh_fs, mesh_fi;
+
+    ~am_engine()
+    {
+        if (own) cudaStreamDestroy(own);
+    }
+
+    RegionsDev regions() const
+    {
+        RegionsDev r;
+        r.keys = keys.as<uint32_t>();
+        r.hash = hash.as<uint64_t>();
+        r.mid = mid.p;
+        r.start = start.as<int32_t>();
+        r.nv = nv.as<int32_t>();
+        r.status = status.as<int8_t>();
+        r.verts = verts.p;
+        r.edges = edges.as<int32_t>();
+        r.cap = cap;
+        return r;
+    }
+    HashDev hashdev() const { return HashDev{table.as<unsigned long long>(), hcap - 1}; }
+
+    void ensure_regions(long long need)
+    {
+        if (need <= cap) return;
+        long long nc = std::max<long long>(need, cap ? cap * 2 : (long long)1 << 16);
+        const long long keep = num_regions;
+        AM_CUDA(keys.grow(sizeof(uint32_t) * (size_t)W * nc, sizeof(uint32_t) * (size_t)W * keep, st));
+        AM_CUDA(hash.grow(sizeof(uint64_t) * nc, sizeof(uint64_t) * keep, st));
+        AM_CUDA(mid.grow(ts * 4 * nc, ts * 4 * keep, st));
+        AM_CUDA(start.grow(sizeof(int32_t) * nc, sizeof(int32_t) * keep, st));
+        AM_CUDA(nv.grow(sizeof(int32_t) * nc, sizeof(int32_t) * keep, st));
+        AM_CUDA(status.grow(sizeof(int8_t) * nc, sizeof(int8_t) * keep, st));
+        AM_CUDA(verts.grow(ts * 3 * kVMax * nc, ts * 3 * kVMax * keep, st));
+        AM_CUDA(edges.grow(sizeof(int32_t) * kVMax * nc, sizeof(int32_t) * kVMax * keep, st));
+        cap = nc;
+    }
+
+    // keep the load factor of the region table <= 1/2
+    void ensure_table(long long entries, bool rehash)
+    {
+        unsigned long long need = 1;
+        while (need < (unsigned long long)std::max<long long>(entries, 1) * 2ull) need <<= 1;
+        need = std::max<unsigned long long>(need, 1ull << 16);
+        if (need <= hcap) return;
+        AM_CUDA(table.alloc(sizeof(unsigned long long) * need));
+        hcap = need;
+        AM_CUDA(cudaMemsetAsync(table.p, 0xff, sizeof(unsigned long long) * need, st));
+        if (rehash && num_regions > 0) {
+            launch_rehash(regions(), num_regions, hashdev(), d_err.as<int>(), st);
+            AM_CUDA(cudaGetLastError());
+        }
+    }
+
+    void ensure_chunk(int count)
+    {
+        if (count <= chunk_cap) return;
+        AM_CUDA(cons.alloc(tc * 4 * (size_t)ALLP * count));
+        AM_CUDA(eq.alloc(tc * 4 * (size_t)count));
+        AM_CUDA(rec.alloc(sizeof(int32_t) * (size_t)kVMax * count));
+        AM_CUDA(blocksum.alloc(sizeof(int) * ((size_t)count * kVMax / 1024 + 2)));
+        chunk_cap = count;
+    }
+
+    int default_chunk() const
+    {
+        if (chunk_opt > 0) return (int)std::min<int64_t>(chunk_opt, (int64_t)(0x7fffffff / std::max(ALL, 1)));
+        const size_t per = tc * 4 * (size_t)ALLP;
+        long long c = (long long)((1ull << 30) / std::max<size_t>(per, 1));
+        c = std::max<long long>(1024, std::min<long long>(c, 1 << 18));
+        c = std::min<long long>(c, 0x7fffffff / std::max(ALL, 1));
+        return (int)c;
+    }
+
+    long long read_tail()
+    {
+        long long t = 0;
+        AM_CUDA(cudaMemcpyAsync(&t, d_tail.p, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        return t;
+    }
+
+    void check_err()
+    {
+        int e = 0;
+        AM_CUDA(cudaMemcpyAsync(&e, d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        if (e & kErrTableFull) throw Failure{AM_ERR_TABLE_FULL, "hash probe bound reached"};
+        if (e & kErrCapacity) throw Failure{AM_ERR_CAPACITY, "region store capacity exceeded"};
+    }
+};
+
+namespace {
+
+template <class F>
+int guarded(am_engine *e, F &&f)
+{
+    try {
+        f();
+        return AM_OK;
+    } catch (const Failure &x) {
+        if (e) e->last_error = x.msg;
+        return x.code;
+    } catch (const std::bad_alloc &) {
+        if (e) e->last_error = "host allocation failed";
+        return AM_ERR_OUT_OF_MEMORY;
+    }
+}
+
+int size_of_prec(int prec) { return prec == kFloat64 ? 8 : 4; }
+
+} // namespace
+
+extern "C" {
+
+const char *am_strerror(int s)
+{
+    switch (s) {
+    case AM_OK: return "ok";
+    case AM_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case AM_ERR_NOT_INITIALIZED: return "engine not initialised";
+    case AM_ERR_CUDA: return "CUDA error";
+    case AM_ERR_OUT_OF_MEMORY: return "out of memory";
+    case AM_ERR_TABLE_FULL: return "region hash table full";
+    case AM_ERR_NO_RESULT: return "no result: run AnalyticMarching (and CombineMesh) first";
+    case AM_ERR_IO: return "I/O error";
+    case AM_ERR_CAPACITY: return "region store capacity exceeded";
+    default: return "unknown status";
+    }
+}
+
+const char *am_last_error(const am_engine *e) { return e ? e->last_error.c_str() : "null engine"; }
+
+int am_vert_capacity(void) { return kVMax; }
+
+int am_init(am_engine **out, const char *float_type, const int32_t *nodesnum, int num_nodes, const int32_t *arc_table,
+            int arc_rows, int arc_cols, int num_extra_constraints)
+{
+    if (!out) return AM_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    std::unique_ptr<am_engine> e(new am_engine());
+    int rc = guarded(e.get(), [&] {
+        AM_CHECK(float_type, "float_type is NULL");
+        const std::string ft(float_type);
+        AM_CHECK(ft == "float32" || ft == "float64" || ft == "mixed", "float_type is either float32, float64 or mixed");
+        e->prec = ft == "float64" ? kFloat64 : (ft == "mixed" ? kMixed : kFloat32);
+        e->tc = size_of_prec(e->prec == kMixed ? kFloat32 : e->prec);
+        e->ts = e->prec == kFloat32 ? 4 : 8;
+        // cuam.cpp:69-86
+        AM_CHECK(nodesnum && num_nodes >= 3, "nodesnum needs at least 3 entries");
+        AM_CHECK(nodesnum[0] == 3, "nodesnum[0] must be 3");
+        AM_CHECK(nodesnum[num_nodes - 1] == 1, "nodesnum[-1] must be 1");
+        AM_CHECK(num_nodes - 1 <= kMaxLayers, "too many layers");
+        AM_CHECK(arc_rows == num_nodes - 2, "arc_table must have len(nodesnum) - 2 rows");
+        AM_CHECK(arc_cols >= 1 && (arc_cols + 1) % 2 == 0, "arc_table width must be odd");
+        AM_CHECK(num_extra_constraints >= 0, "num_extra_constraints must be >= 0");
+        AM_CHECK(arc_table || arc_rows == 0, "arc_table is NULL");
+        for (int i = 0; i < arc_rows; ++i) {
+            const int cnt = arc_table[(size_t)i * arc_cols];
+            AM_CHECK(cnt >= 0 && 1 + 2 * cnt <= arc_cols, "arc_table row has more connections than columns");
+            AM_CHECK(cnt <= kMaxSkips, "too many connections into one layer");
+            for (int c = 0; c < cnt; ++c) {
+                const int from = arc_table[(size_t)i * arc_cols + 1 + 2 * c];
+                AM_CHECK(from >= 0 && from <= i + 1, "arc_table source must precede the target layer");
+            }
+        }
+        for (int i = 0; i < num_nodes; ++i) AM_CHECK(nodesnum[i] > 0, "layer widths must be positive");
+        e->nodes.assign(nodesnum, nodesnum + num_nodes);
+        e->arc.assign(arc_table, arc_table + (size_t)arc_rows * arc_cols);
+        e->arc_cols = arc_cols;
+        e->n_lin = num_nodes - 1;
+        e->N = 0;
+        for (int i = 1; i < num_nodes - 1; ++i) e->N += nodesnum[i];
+        e->E = num_extra_constraints;
+        e->ALL = e->N + e->E;
+        e->ALLP = (e->ALL + 7) / 8 * 8;
+        e->W = (e->N + 31) / 32;
+        AM_CUDA(cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking));
+        e->st = e->own;
+        AM_CUDA(e->d_tail.alloc(sizeof(long long)));
+        AM_CUDA(e->d_err.alloc(sizeof(int)));
+    });
+    if (rc == AM_OK) *out = e.release();
+    return rc;
+}
+
+int am_set_option(am_engine *e, int option, int64_t value)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (option == AM_OPT_CHUNK) {
+        if (value < 0) return AM_ERR_INVALID_ARGUMENT;
+        e->chunk_opt = value;
+        return AM_OK;
+    }
+    if (option == AM_OPT_PHASE_TIMING) {
+        e->phase_timing = value != 0;
+        return AM_OK;
+    }
+    return AM_ERR_INVALID_ARGUMENT;
+}
+
+int am_analytic_marching(am_engine *e, const void *const *weights, const void *const *biases, const uint8_t *states,
+                         const void *points, int num_points, const void *const *arc_tm, const int32_t *arc_tm_shapes,
+                         int num_arc_tm, const void *w_extra, const void *b_extra, double iso, int flip_insideout,
+                         void *stream)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    e->has_am = false;
+    e->has_mesh = false;
+    return guarded(e, [&] {
+        e->st = stream ? (cudaStream_t)stream : e->own;
+        cudaStream_t st = e->st;
+        const int prec = e->prec;
+        const size_t tc = e->tc, ts = e->ts;
+        AM_CHECK(weights && biases, "weights / biases are NULL");
+        AM_CHECK(states && points && num_points >= 1, "states / points are empty"); // cuam.cpp:142
+        AM_CHECK(e->E == 0 || (w_extra && b_extra), "extra constraints are NULL");
+        // arc_tm shapes, cuam.cpp:160-173
+        for (int i = 0; i + 1 < e->n_lin; ++i) {
+            const int *row = e->arc.data() + (size_t)i * e->arc_cols;
+            for (int c = 0; c < row[0]; ++c) {
+                const int from = row[1 + 2 * c], t = row[2 + 2 * c];
+                AM_CHECK(t >= 0 && t < num_arc_tm && arc_tm_shapes, "arc_table refers to a missing transform");
+                const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
+                if (h || w) {
+                    AM_CHECK(h == e->nodes[i + 2], "transform rows must match the target width");
+                    AM_CHECK(w == e->nodes[from], "transform columns must match the source width");
+                } else {
+                    AM_CHECK(e->nodes[from] == e->nodes[i + 2], "identity connection between different widths");
+                }
+            }
+        }
+
+        cudaEvent_t ev0, ev1, pa, pb;
+        AM_CUDA(cudaEventCreate(&ev0));
+        AM_CUDA(cudaEventCreate(&ev1));
+        AM_CUDA(cudaEventCreate(&pa));
+        AM_CUDA(cudaEventCreate(&pb));
+        struct EvGuard {
+            cudaEvent_t a, b, c, d;
+            ~EvGuard()
+            {
+                cudaEventDestroy(a);
+                cudaEventDestroy(b);
+                cudaEventDestroy(c);
+                cudaEventDestroy(d);
+            }
+        } evg{ev0, ev1, pa, pb};
+
+        // ---------------------------------------------------------- network
+        NetDev &net = e->net;
+        memset(&net, 0, sizeof(net));
+        net.n_lin = e->n_lin;
+        net.N = e->N;
+        net.E = e->E;
+        net.ALL = e->ALL;
+        net.ALLP = e->ALLP;
+        net.W = e->W;
+        for (int i = 0; i <= e->n_lin; ++i) net.nodes[i] = e->nodes[i];
+        net.hoff[1] = 0;
+        for (int h = 1; h < e->n_lin; ++h) net.hoff[h + 1] = net.hoff[h] + e->nodes[h];
+        for (int i = 0; i < e->n_lin; ++i) {
+            const int M = e->nodes[i + 1], K = e->nodes[i];
+            AM_CHECK(weights[i] && biases[i], "a weight / bias pointer is NULL");
+            upload(e->bias[i], biases[i], tc * M, st);
+            net.bias[i] = e->bias[i].p;
+            if (i == 0) {
+                upload(e->w0, weights[0], tc * (size_t)M * 3, st);
+                net.W0 = e->w0.p;
+            } else {
+                const int Mp = (M + 3) / 4 * 4;
+                upload(e->scratch, weights[i], tc * (size_t)M * K, st);
+                AM_CUDA(e->wt[i].alloc(tc * (size_t)K * Mp));
+                launch_prepare_weights(prec == kFloat64 ? kFloat64 : kFloat32, e->scratch.p, M, K, Mp, e->wt[i].p, st);
+                net.Wt[i] = e->wt[i].p;
+                net.Mp[i] = Mp;
+            }
+        }
+        int ntm = 0;
+        for (int i = 1; i < e->n_lin; ++i) {
+            const int *row = e->arc.data() + (size_t)(i - 1) * e->arc_cols;
+            net.nskip[i] = row[0];
+            for (int c = 0; c < row[0]; ++c) {
+                const int from = row[1 + 2 * c], t = row[2 + 2 * c];
+                SkipDev &sk = net.skip[i][c];
+                sk.from = from;
+                const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
+                if (h == 0 && w == 0) {
+                    sk.kind = 0;
+                    sk.tmt = nullptr;
+                    sk.Mp = 0;
+                } else {
+                    AM_CHECK(ntm < 64, "too many transform matrices");
+                    const int Mp = (h + 3) / 4 * 4;
+                    upload(e->scratch, arc_tm[t], tc * (size_t)h * w, st);
+                    AM_CUDA(e->tmt[ntm].alloc(tc * (size_t)w * Mp));
+                    launch_prepare_weights(prec == kFloat64 ? kFloat64 : kFloat32, e->scratch.p, h, w, Mp,
+                                           e->tmt[ntm].p, st);
+                    sk.kind = 1;
+                    sk.tmt = e->tmt[ntm].p;
+                    sk.Mp = Mp;
+                    ntm++;
+                }
+            }
+        }
+        if (e->E) {
+            upload(e->wext, w_extra, tc * 3 * (size_t)e->E, st);
+            upload(e->bext, b_extra, tc * (size_t)e->E, st);
+        }
+        net.w_extra = e->wext.p;
+        net.b_extra = e->bext.p;
+        AM_CUDA(cudaGetLastError());
+
+        // ---------------------------------------------------------- seeds
+        const int S = num_points;
+        upload(e->s_states, states, (size_t)S * e->N, st);
+        {
+            // seed points in the solve precision
+            std::vector<double> pd(3 * (size_t)S);
+            std::vector<unsigned char> raw(tc * 3 * (size_t)S);
+            to_host(raw.data(), points, raw.size(), st);
+            AM_CUDA(cudaStreamSynchronize(st));
+            for (size_t q = 0; q < 3 * (size_t)S; ++q)
+                pd[q] = tc == 8 ? ((const double *)raw.data())[q] : (double)((const float *)raw.data())[q];
+            if (ts == 8) {
+                upload(e->s_pts, pd.data(), sizeof(double) * pd.size(), st);
+            } else {
+                std::vector<float> pf(pd.begin(), pd.end());
+                upload(e->s_pts, pf.data(), sizeof(float) * pf.size(), st);
+            }
+            AM_CUDA(cudaStreamSynchronize(st));
+        }
+        AM_CUDA(e->s_keys.alloc(sizeof(uint32_t) * (size_t)S * e->W));
+        AM_CUDA(e->s_hash.alloc(sizeof(uint64_t) * (size_t)S));
+        AM_CUDA(e->s_rec.alloc(sizeof(int32_t) * (size_t)S));
+
+        e->num_regions = 0;
+        e->hcap = 0;
+        e->stats = am_stats{};
+        AM_CUDA(cudaMemsetAsync(e->d_tail.p, 0, sizeof(long long), st));
+        AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
+        const int chunk = e->default_chunk();
+        e->ensure_chunk(std::min(chunk, std::max(S, 1024)));
+        e->ensure_regions(std::max<long long>(S, 1) + (long long)chunk * kVMax);
+        e->ensure_table((long long)S + (long long)chunk * kVMax, false);
+        AM_CUDA(e->blocksum.grow(sizeof(int) * ((size_t)S / 1024 + 2), 0, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+
+        long long launches = 0;
+        AM_CUDA(cudaEventRecord(ev0, st));
+        launch_seed_pack(e->s_states.as<uint8_t>(), S, e->N, e->W, e->s_keys.as<uint32_t>(), e->s_hash.as<uint64_t>(), st);
+        launch_seed_insert(e->s_keys.as<uint32_t>(), e->s_hash.as<uint64_t>(), S, e->W, e->hashdev(),
+                           e->s_rec.as<int32_t>(), e->d_err.as<int>(), st);
+        {
+            ChunkDev sc{};
+            sc.rec = e->s_rec.as<int32_t>();
+            launch_append(1, prec, net, e->regions(), sc, e->hashdev(), e->s_keys.as<uint32_t>(),
+                          e->s_hash.as<uint64_t>(), e->s_pts.p, S, e->d_tail.as<long long>(), e->blocksum.as<int>(),
+                          (int)(e->blocksum.bytes / sizeof(int)), e->d_err.as<int>(), st);
+        }
+        launches += 5;
+        AM_CUDA(cudaGetLastError());
+        long long tail = e->read_tail();
+        e->check_err();
+        e->num_regions = tail;
+        e->stats.num_seeds = tail;
+
+        const Tolerances tol = prec == kFloat64 ? Tolerances{1e-20, 3e-14, 1e-12} : Tolerances{1e-12, 3e-7, 1e-6};
+        long long head = 0;
+        int chunks = 0;
+        double t_comp = 0, t_poly = 0, t_front = 0;
+        while (head < tail) {
+            const int count = (int)std::min<long long>(tail - head, chunk);
+            e->ensure_chunk(count);
+            e->ensure_regions(tail + (long long)count * kVMax);
+            e->ensure_table(tail + (long long)count * kVMax, true);
+            ChunkDev ch;
+            ch.head = head;
+            ch.count = count;
+            ch.cons = e->cons.p;
+            ch.eq = e->eq.p;
+            ch.rec = e->rec.as<int32_t>();
+            const RegionsDev reg = e->regions();
+            const HashDev hs = e->hashdev();
+            float ms = 0;
+            if (e->phase_timing) AM_CUDA(cudaEventRecord(pa, st));
+            launch_compose(prec == kMixed ? kFloat32 : prec, net, reg, ch, iso, st);
+            if (e->phase_timing) {
+                AM_CUDA(cudaEventRecord(pb, st));
+                AM_CUDA(cudaEventSynchronize(pb));
+                AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
+                t_comp += ms;
+                AM_CUDA(cudaEventRecord(pa, st));
+            }
+            launch_polygon(prec, net, reg, ch, hs, tol, e->d_err.as<int>(), st);
+            if (e->phase_timing) {
+                AM_CUDA(cudaEventRecord(pb, st));
+                AM_CUDA(cudaEventSynchronize(pb));
+                AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
+                t_poly += ms;
+                AM_CUDA(cudaEventRecord(pa, st));
+            }
+            launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, count * kVMax, e->d_tail.as<long long>(),
+                          e->blocksum.as<int>(), (int)(e->blocksum.bytes / sizeof(int)), e->d_err.as<int>(), st);
+            if (e->phase_timing) {
+                AM_CUDA(cudaEventRecord(pb, st));
+                AM_CUDA(cudaEventSynchronize(pb));
+                AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
+                t_front += ms;
+            }
+            launches += 5;
+            AM_CUDA(cudaGetLastError());
+            head += count;
+            tail = e->read_tail();
+            e->num_regions = tail;
+            chunks++;
+            e->check_err();
+        }
+        AM_CUDA(cudaEventRecord(ev1, st));
+        AM_CUDA(cudaEventSynchronize(ev1));
+        float total = 0;
+        AM_CUDA(cudaEventElapsedTime(&total, ev0, ev1));
+        e->check_err();
+
+        // statistics
+        am_stats &sx = e->stats;
+        sx.num_regions = tail;
+        sx.chunks = chunks;
+        sx.am_time_ms = total;
+        sx.compose_ms = t_comp;
+        sx.polygon_ms = t_poly;
+        sx.frontier_ms = t_front;
+        sx.kernel_launches = launches;
+        {
+            std::vector<int32_t> hn((size_t)tail);
+            std::vector<int8_t> hsx((size_t)tail);
+            AM_CUDA(cudaMemcpyAsync(hn.data(), e->nv.p, sizeof(int32_t) * tail, cudaMemcpyDeviceToHost, st));
+            AM_CUDA(cudaMemcpyAsync(hsx.data(), e->status.p, sizeof(int8_t) * tail, cudaMemcpyDeviceToHost, st));
+            AM_CUDA(cudaStreamSynchronize(st));
+            for (long long r = 0; r < tail; ++r) {
+                if (hn[r] >= 3) sx.num_faces++;
+                sx.max_polygon_verts = std::max(sx.max_polygon_verts, hn[r]);
+                switch (hsx[r]) {
+                case kNoStart: sx.num_nostart++; break;
+                case kOpen: sx.num_open++; break;
+                case kTruncated: sx.num_truncated++; break;
+                case kSingular: sx.num_singular++; break;
+                default: break;
+                }
+            }
+        }
+        e->flip = flip_insideout ? 1 : 0;
+        e->has_am = true;
+    });
+}
+
+int am_get_stats(const am_engine *e, am_stats *out)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (!out) return AM_ERR_INVALID_ARGUMENT;
+    *out = e->stats;
+    return AM_OK;
+}
+
+int am_combine_mesh(am_engine *e, double scale, const double *center3)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (!e->has_am) return AM_ERR_NO_RESULT;
+    return guarded(e, [&] {
+        cudaStream_t st = e->st;
+        const long long R = e->num_regions;
+        const long long ns = std::max<long long>(R * kVMax, 1);
+        unsigned long long tcap = 1;
+        while (tcap < (unsigned long long)ns * 2ull) tcap <<= 1;
+        AM_CUDA(e->w_table.alloc(sizeof(unsigned long long) * tcap));
+        AM_CUDA(e->w_rep.alloc(sizeof(long long) * ns));
+        AM_CUDA(e->w_flag.alloc(sizeof(int) * ns));
+        AM_CUDA(e->w_vidx.alloc(sizeof(int) * ns));
+        AM_CUDA(e->w_bsum.alloc(sizeof(int) * (ns / 1024 + 2)));
+        AM_CUDA(e->w_fflag.alloc(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_fsize.alloc(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_fid.alloc(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_foff.alloc(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_verts.alloc(e->ts * 3 * ns));
+        AM_CUDA(e->w_fs.alloc(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_fi.alloc(sizeof(int) * ns));
+        AM_CUDA(e->w_counts.alloc(sizeof(long long) * 3));
+        WeldBuffers wb;
+        wb.table = e->w_table.as<unsigned long long>();
+        wb.mask = tcap - 1;
+        wb.rep = e->w_rep.as<long long>();
+        wb.flag = e->w_flag.as<int>();
+        wb.vidx = e->w_vidx.as<int>();
+        wb.bsum = e->w_bsum.as<int>();
+        wb.fflag = e->w_fflag.as<int>();
+        wb.fsize = e->w_fsize.as<int>();
+        wb.fid = e->w_fid.as<int>();
+        wb.foff = e->w_foff.as<int>();
+        wb.out_verts = e->w_verts.p;
+        wb.face_sizes = e->w_fs.as<int>();
+        wb.face_idx = e->w_fi.as<int>();
+        wb.counts = e->w_counts.as<long long>();
+        const double c0[3] = {0, 0, 0};
+        AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
+        launch_weld(e->prec, e->regions(), R, wb, scale, center3 ? center3 : c0, e->flip, e->d_err.as<int>(), st);
+        AM_CUDA(cudaGetLastError());
+        long long cnt[3] = {0, 0, 0};
+        AM_CUDA(cudaMemcpyAsync(cnt, wb.counts, sizeof(cnt), cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        e->check_err();
+        const long long V = cnt[0], F = cnt[1], I = cnt[2];
+        e->mesh_verts.assign((size_t)V * 3, 0.0);
+        e->mesh_fs.assign((size_t)F, 0);
+        e->mesh_fi.assign((size_t)I, 0);
+        if (e->ts == 8) {
+            AM_CUDA(cudaMemcpyAsync(e->mesh_verts.data(), e->w_verts.p, sizeof(double) * 3 * V, cudaMemcpyDeviceToHost, st));
+        } else {
+            std::vector<float> tmp((size_t)V * 3);
+            AM_CUDA(cudaMemcpyAsync(tmp.data(), e->w_verts.p, sizeof(float) * 3 * V, cudaMemcpyDeviceToHost, st));
+            AM_CUDA(cudaStreamSynchronize(st));
+            for (size_t q = 0; q < tmp.size(); ++q) e->mesh_verts[q] = tmp[q];
+        }
+        AM_CUDA(cudaMemcpyAsync(e->mesh_fs.data(), e->w_fs.p, sizeof(int) * F, cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaMemcpyAsync(e->mesh_fi.data(), e->w_fi.p, sizeof(int) * I, cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        e->stats.mesh_num_verts = V;
+        e->stats.mesh_num_faces = F;
+        e->stats.mesh_num_indices = I;
+        e->has_mesh = true;
+    });
+}
+
+int am_get_mesh(am_engine *e, double *verts, int32_t *face_sizes, int32_t *face_indices)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (!e->has_mesh) return AM_ERR_NO_RESULT;
+    if (verts) std::copy(e->mesh_verts.begin(), e->mesh_verts.end(), verts);
+    if (face_sizes) std::copy(e->mesh_fs.begin(), e->mesh_fs.end(), face_sizes);
+    if (face_indices) std::copy(e->mesh_fi.begin(), e->mesh_fi.end(), face_indices);
+    return AM_OK;
+}
+
+int am_export_mesh(am_engine *e, const char *file_path, int is_polymesh, int is_float32)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (!e->has_mesh) return AM_ERR_NO_RESULT;
+    if (!file_path) return AM_ERR_INVALID_ARGUMENT;
+    FILE *f = fopen(file_path, "wb");
+    if (!f) {
+        e->last_error = std::string("cannot open ") + file_path;
+        return AM_ERR_IO;
+    }
+    const long long V = e->stats.mesh_num_verts, F = e->stats.mesh_num_faces;
+    long long tri = 0;
+    if (!is_polymesh)
+        for (long long i = 0; i < F; ++i) tri += e->mesh_fs[i] - 2;
+    // header as polymesh.h:368-377
+    fprintf(f, "ply\nformat binary_little_endian 1.0\nelement vertex %lld\n", V);
+    const char *ty = is_float32 ? "float" : "double";
+    fprintf(f, "property %s x\nproperty %s y\nproperty %s z\n", ty, ty, ty);
+    fprintf(f, "element face %lld\nproperty list uchar int vertex_index\nend_header\n", is_polymesh ? F : tri);
+    bool ok = true;
+    for (long long i = 0; i < V && ok; ++i) {
+        if (is_float32) {
+            const float v[3] = {(float)e->mesh_verts[3 * i], (float)e->mesh_verts[3 * i + 1], (float)e->mesh_verts[3 * i + 2]};
+            ok = fwrite(v, sizeof(float), 3, f) == 3;
+        } else {
+            ok = fwrite(&e->mesh_verts[3 * i], sizeof(double), 3, f) == 3;
+        }
+    }
+    size_t off = 0;
+    for (long long i = 0; i < F && ok; ++i) {
+        const int n = e->mesh_fs[i];
+        const int32_t *idx = e->mesh_fi.data() + off;
+        if (is_polymesh) {
+            const unsigned char c = (unsigned char)n;
+            ok = fwrite(&c, 1, 1, f) == 1 && fwrite(idx, sizeof(int32_t), n, f) == (size_t)n;
+        } else {
+            const unsigned char c = 3;
+            for (int j = 0; j + 2 < n && ok; ++j) {
+                const int32_t t[3] = {idx[0], idx[j + 1], idx[j + 2]};
+                ok = fwrite(&c, 1, 1, f) == 1 && fwrite(t, sizeof(int32_t), 3, f) == 3;
+            }
+        }
+        off += n;
+    }
+    if (fclose(f) != 0) ok = false;
+    if (!ok) {
+        e->last_error = std::string("write failed: ") + file_path;
+        return AM_ERR_IO;
+    }
+    return AM_OK;
+}
+
+int am_get_regions(am_engine *e, uint32_t *bits, int32_t *nverts, double *verts, int32_t *edges, int8_t *status,
+                   double *seeds, int32_t *start)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (!e->has_am) return AM_ERR_NO_RESULT;
+    return guarded(e, [&] {
+        cudaStream_t st = e->st;
+        const long long R = e->num_regions;
+        if (bits) AM_CUDA(cudaMemcpyAsync(bits, e->keys.p, sizeof(uint32_t) * e->W * R, cudaMemcpyDeviceToHost, st));
+        if (nverts) AM_CUDA(cudaMemcpyAsync(nverts, e->nv.p, sizeof(int32_t) * R, cudaMemcpyDeviceToHost, st));
+        if (edges) AM_CUDA(cudaMemcpyAsync(edges, e->edges.p, sizeof(int32_t) * kVMax * R, cudaMemcpyDeviceToHost, st));
+        if (status) AM_CUDA(cudaMemcpyAsync(status, e->status.p, R, cudaMemcpyDeviceToHost, st));
+        if (start) AM_CUDA(cudaMemcpyAsync(start, e->start.p, sizeof(int32_t) * R, cudaMemcpyDeviceToHost, st));
+        if (verts || seeds) {
+            std::vector<unsigned char> vb(verts ? e->ts * 3 * kVMax * R : 0), mb(seeds ? e->ts * 4 * R : 0);
+            if (verts) AM_CUDA(cudaMemcpyAsync(vb.data(), e->verts.p, vb.size(), cudaMemcpyDeviceToHost, st));
+            if (seeds) AM_CUDA(cudaMemcpyAsync(mb.data(), e->mid.p, mb.size(), cudaMemcpyDeviceToHost, st));
+            AM_CUDA(cudaStreamSynchronize(st));
+            const size_t nvv = (size_t)3 * kVMax * R;
+            if (verts)
+                for (size_t q = 0; q < nvv; ++q)
+                    verts[q] = e->ts == 8 ? ((const double *)vb.data())[q] : (double)((const float *)vb.data())[q];
+            if (seeds)
+                for (long long r = 0; r < R; ++r)
+                    for (int c = 0; c < 3; ++c)
+                        seeds[3 * r + c] = e->ts == 8 ? ((const double *)mb.data())[4 * r + c]
+                                                      : (double)((const float *)mb.data())[4 * r + c];
+        }
+        AM_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int am_destroy(am_engine *e)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (e->st) cudaStreamSynchronize(e->st);
+    delete e;
+    return AM_OK;
+}
+
+} // extern "C"

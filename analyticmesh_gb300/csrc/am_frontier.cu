@@ -1,0 +1,292 @@
+// am_frontier.cu -- region hash set and the append-only region store.
+//
+// The reference keeps visited regions as 32-bit FNV-1 fingerprints in an
+// open-addressing table and accepts a region as new when its fingerprint is
+// absent (backend/inc/hash.h:33-67) -- two different regions with the same
+// fingerprint silently lose one.  This store keeps every region's full
+// packed key; a table slot holds (fingerprint, id) and a fingerprint match
+// is confirmed by comparing the keys.
+//
+// New regions are appended in candidate order: winners of the insert are
+// flagged, counted per block, scanned, and written at tail + prefix, so the
+// region ids of a run do not depend on thread scheduling.
+#include <cuda/atomic>
+#include <cuda_runtime.h>
+
+#include "am_device.cuh"
+#include "am_internal.h"
+
+namespace am {
+
+namespace {
+
+constexpr int kScanBlock = 1024;
+
+__device__ __forceinline__ unsigned long long load_slot(const unsigned long long *p)
+{
+    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> a(*const_cast<unsigned long long *>(p));
+    return a.load(cuda::memory_order_relaxed);
+}
+
+// Exclusive scan over the block; returns this thread's prefix, writes the total.
+__device__ int block_exclusive_scan(int v, int *total)
+{
+    __shared__ int wsum[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+        int s = lane < nw ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) wsum[lane] = s;
+    }
+    __syncthreads();
+    const int before = wid > 0 ? wsum[wid - 1] : 0;
+    *total = wsum[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void seed_pack_kernel(const uint8_t *states, int S, int N, int W, uint32_t *keys, uint64_t *hash)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const uint8_t *row = states + (size_t)s * N;
+    uint64_t h = 0;
+    for (int w = 0; w < W; ++w) {
+        uint32_t word = 0;
+        const int lim = min(32, N - 32 * w);
+        for (int b = 0; b < lim; ++b)
+            if (row[32 * w + b]) word |= 1u << b;
+        keys[(size_t)s * W + w] = word;
+        h += word_term(word, w);
+    }
+    hash[s] = h;
+}
+
+__global__ void seed_insert_kernel(const uint32_t *keys, const uint64_t *hash, int S, int W, HashDev hs, int32_t *rec,
+                                   int *err)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const uint64_t h = hash[s];
+    const uint32_t fp = fp_of(h);
+    const unsigned long long mine = slot_value(fp, 1, (uint32_t)s);
+    const uint32_t *key = keys + (size_t)s * W;
+    unsigned long long slot = h & hs.mask;
+    int r = -1, probe = 0;
+    for (; probe < kMaxProbes; ++probe) {
+        unsigned long long cur = load_slot(hs.slots + slot);
+        if (cur == kEmpty) {
+            const unsigned long long old = atomicCAS(hs.slots + slot, kEmpty, mine);
+            if (old == kEmpty) {
+                r = (int)slot;
+                break;
+            }
+            cur = old;
+        }
+        if ((uint32_t)(cur >> 32) == fp) {
+            const uint32_t *other = keys + (size_t)((uint32_t)cur & 0x7fffffffu) * W;
+            bool eq = true;
+            for (int w = 0; w < W && eq; ++w) eq = (other[w] == key[w]);
+            if (eq) {
+                atomicMin(hs.slots + slot, mine);
+                r = (int)slot;
+                break;
+            }
+        }
+        slot = (slot + (unsigned long long)probe + 1ull) & hs.mask;
+    }
+    if (probe == kMaxProbes) atomicOr(err, kErrTableFull);
+    rec[s] = r;
+}
+
+struct AppendArgs {
+    int mode;              // 0 children of a chunk, 1 seeds
+    NetDev net;
+    RegionsDev reg;
+    ChunkDev ch;
+    HashDev hs;
+    const uint32_t *seed_keys;
+    const uint64_t *seed_hash;
+    const void *seed_points; // [S][3] TS
+    int n_items;
+    long long *tail;
+    int *blockoff;
+    int *err;
+};
+
+__device__ __forceinline__ int is_winner(const AppendArgs &a, int q)
+{
+    if (q >= a.n_items) return 0;
+    const int rec = a.ch.rec[q];
+    if (rec < 0) return 0;
+    uint32_t myid;
+    if (a.mode == 1) {
+        myid = (uint32_t)q;
+    } else {
+        const long long rl = q / kVMax;
+        const int i = q % kVMax;
+        const int k = a.reg.edges[(size_t)(a.ch.head + rl) * kVMax + i];
+        myid = (uint32_t)(rl * a.net.ALL + k);
+    }
+    const unsigned long long cur = load_slot(a.hs.slots + rec);
+    return ((uint32_t)cur == ((1u << 31) | (myid & 0x7fffffffu))) ? 1 : 0;
+}
+
+__global__ void __launch_bounds__(kScanBlock) append_count_kernel(AppendArgs a)
+{
+    const int q = blockIdx.x * kScanBlock + threadIdx.x;
+    int total;
+    const int f = is_winner(a, q);
+    block_exclusive_scan(f, &total);
+    if (threadIdx.x == 0) a.blockoff[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanBlock) append_offsets_kernel(AppendArgs a, int nblocks)
+{
+    __shared__ long long base;
+    if (threadIdx.x == 0) base = *a.tail;
+    __syncthreads();
+    for (int b0 = 0; b0 < nblocks; b0 += kScanBlock) {
+        const int b = b0 + threadIdx.x;
+        const int v = b < nblocks ? a.blockoff[b] : 0;
+        int total;
+        const int pre = block_exclusive_scan(v, &total);
+        if (b < nblocks) a.blockoff[b] = (int)(base + pre);
+        __syncthreads();
+        if (threadIdx.x == 0) base += total;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *a.tail = base;
+}
+
+template <typename TS>
+__global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
+{
+    const int q = blockIdx.x * kScanBlock + threadIdx.x;
+    int total;
+    const int f = is_winner(a, q);
+    const int pre = block_exclusive_scan(f, &total);
+    if (!f) return;
+    const long long rid = (long long)a.blockoff[blockIdx.x] + pre;
+    if (rid >= a.reg.cap) {
+        atomicOr(a.err, kErrCapacity);
+        return;
+    }
+    const int W = a.net.W;
+    uint32_t *key = a.reg.keys + (size_t)rid * W;
+    TS *mid = (TS *)a.reg.mid + (size_t)rid * 4;
+    uint64_t h;
+    if (a.mode == 1) {
+        const uint32_t *sk = a.seed_keys + (size_t)q * W;
+        for (int w = 0; w < W; ++w) key[w] = sk[w];
+        h = a.seed_hash[q];
+        const TS *pt = (const TS *)a.seed_points + (size_t)q * 3;
+        mid[0] = pt[0];
+        mid[1] = pt[1];
+        mid[2] = pt[2];
+        mid[3] = TS(0);
+        a.reg.start[rid] = -1;
+    } else {
+        const long long parent = a.ch.head + q / kVMax;
+        const int i = q % kVMax;
+        const int k = a.reg.edges[(size_t)parent * kVMax + i];
+        const uint32_t *pk = a.reg.keys + (size_t)parent * W;
+        for (int w = 0; w < W; ++w) key[w] = pk[w];
+        key[k >> 5] ^= 1u << (k & 31);
+        h = flip_hash(a.reg.hash[parent], pk[k >> 5], k);
+        const int n = a.reg.nv[parent];
+        const TS *v0 = (const TS *)a.reg.verts + ((size_t)parent * kVMax + i) * 3;
+        const TS *v1 = (const TS *)a.reg.verts + ((size_t)parent * kVMax + (i + 1) % n) * 3;
+        mid[0] = (v0[0] + v1[0]) / TS(2);
+        mid[1] = (v0[1] + v1[1]) / TS(2);
+        mid[2] = (v0[2] + v1[2]) / TS(2);
+        mid[3] = TS(0);
+        a.reg.start[rid] = k;
+    }
+    a.reg.hash[rid] = h;
+    a.reg.nv[rid] = 0;
+    a.reg.status[rid] = 0;
+    a.hs.slots[a.ch.rec[q]] = slot_value(fp_of(h), 0, (uint32_t)rid);
+}
+
+__global__ void rehash_kernel(RegionsDev reg, long long n, HashDev hs, int *err)
+{
+    const long long rid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (rid >= n) return;
+    const uint64_t h = reg.hash[rid];
+    const unsigned long long v = slot_value(fp_of(h), 0, (uint32_t)rid);
+    unsigned long long slot = h & hs.mask;
+    for (int probe = 0; probe < kMaxProbes; ++probe) {
+        if (atomicCAS(hs.slots + slot, kEmpty, v) == kEmpty) return;
+        slot = (slot + (unsigned long long)probe + 1ull) & hs.mask;
+    }
+    atomicOr(err, kErrTableFull);
+}
+
+} // namespace
+
+void launch_seed_pack(const uint8_t *states, int S, int N, int W, uint32_t *keys, uint64_t *hash, cudaStream_t st)
+{
+    if (S <= 0) return;
+    seed_pack_kernel<<<(S + 127) / 128, 128, 0, st>>>(states, S, N, W, keys, hash);
+}
+
+void launch_seed_insert(const uint32_t *keys, const uint64_t *hash, int S, int W, const HashDev &hs, int32_t *rec,
+                        int *d_err, cudaStream_t st)
+{
+    if (S <= 0) return;
+    seed_insert_kernel<<<(S + 127) / 128, 128, 0, st>>>(keys, hash, S, W, hs, rec, d_err);
+}
+
+void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs,
+                   const uint32_t *seed_keys, const uint64_t *seed_hash, const void *seed_points, int n_items,
+                   long long *d_tail, int *d_blocksum, int nblocks_cap, int *d_err, cudaStream_t st)
+{
+    if (n_items <= 0) return;
+    AppendArgs a;
+    a.mode = mode;
+    a.net = net;
+    a.reg = reg;
+    a.ch = ch;
+    a.hs = hs;
+    a.seed_keys = seed_keys;
+    a.seed_hash = seed_hash;
+    a.seed_points = seed_points;
+    a.n_items = n_items;
+    a.tail = d_tail;
+    a.blockoff = d_blocksum;
+    a.err = d_err;
+    const int nb = (n_items + kScanBlock - 1) / kScanBlock;
+    if (nb > nblocks_cap) { // the host sizes d_blocksum for the largest chunk
+        int e = kErrCapacity;
+        cudaMemcpyAsync(d_err, &e, sizeof(int), cudaMemcpyHostToDevice, st);
+        return;
+    }
+    append_count_kernel<<<nb, kScanBlock, 0, st>>>(a);
+    append_offsets_kernel<<<1, kScanBlock, 0, st>>>(a, nb);
+    if (prec == kFloat32)
+        append_write_kernel<float><<<nb, kScanBlock, 0, st>>>(a);
+    else
+        append_write_kernel<double><<<nb, kScanBlock, 0, st>>>(a);
+}
+
+void launch_rehash(const RegionsDev &reg, long long n, const HashDev &hs, int *d_err, cudaStream_t st)
+{
+    if (n <= 0) return;
+    rehash_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(reg, n, hs, d_err);
+}
+
+} // namespace am

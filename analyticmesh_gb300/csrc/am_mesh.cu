@@ -1,0 +1,255 @@
+// am_mesh.cu -- CombineMesh on the device: weld the vertices of all face
+// polygons and index the faces.
+//
+// Same quantisation as the reference's PolyMesh (backend/inc/polymesh.h:
+// 174-335, int(v * 1e6) for fp32 data, int(v * 1e9) for fp64), but the weld
+// compares the quantised coordinates exactly instead of by a 32-bit
+// fingerprint (polymesh.h:305), and vertex / face numbering follows region
+// order (first occurrence), independent of thread scheduling.  Vertices of
+// polygons with fewer than 3 corners are welded too, as in the reference;
+// only polygons with 3 or more corners become faces.
+#include <cuda/atomic>
+#include <cuda_runtime.h>
+
+#include "am_device.cuh"
+#include "am_internal.h"
+#include "am_mesh.h"
+
+namespace am {
+
+namespace {
+
+constexpr int kScanBlock = 1024;
+
+template <typename TS>
+__device__ __forceinline__ void qkey(const TS *v, double mul, long long *q)
+{
+    // the reference converts v * MUL in the working precision to int
+    q[0] = (long long)(int)(v[0] * (TS)mul);
+    q[1] = (long long)(int)(v[1] * (TS)mul);
+    q[2] = (long long)(int)(v[2] * (TS)mul);
+}
+
+__device__ __forceinline__ uint64_t qhash(const long long *q)
+{
+    return mix64((uint64_t)q[0] * 0x9E3779B97F4A7C15ull ^ mix64((uint64_t)q[1] + 0x632BE59BD9B4E019ull) ^
+                 mix64((uint64_t)q[2] * 0xD6E8FEB86659FD93ull + 7));
+}
+
+template <typename TS>
+__global__ void weld_insert_kernel(RegionsDev reg, long long R, unsigned long long *table, unsigned long long mask,
+                                   double mul, int *err)
+{
+    const long long sid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (sid >= R * kVMax) return;
+    const long long r = sid / kVMax;
+    const int i = (int)(sid % kVMax);
+    if (i >= reg.nv[r]) return;
+    long long q[3];
+    qkey<TS>((const TS *)reg.verts + (size_t)sid * 3, mul, q);
+    unsigned long long slot = qhash(q) & mask;
+    for (int probe = 0; probe < kMaxProbes; ++probe) {
+        unsigned long long cur = atomicCAS(table + slot, kEmpty, (unsigned long long)sid);
+        if (cur == kEmpty) return;
+        long long o[3];
+        qkey<TS>((const TS *)reg.verts + (size_t)cur * 3, mul, o);
+        if (o[0] == q[0] && o[1] == q[1] && o[2] == q[2]) {
+            atomicMin(table + slot, (unsigned long long)sid);
+            return;
+        }
+        slot = (slot + (unsigned long long)probe + 1ull) & mask;
+    }
+    atomicOr(err, kErrTableFull);
+}
+
+template <typename TS>
+__global__ void weld_rep_kernel(RegionsDev reg, long long R, const unsigned long long *table, unsigned long long mask,
+                                double mul, long long *rep, int *flag)
+{
+    const long long sid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (sid >= R * kVMax) return;
+    const long long r = sid / kVMax;
+    const int i = (int)(sid % kVMax);
+    if (i >= reg.nv[r]) {
+        flag[sid] = 0;
+        rep[sid] = -1;
+        return;
+    }
+    long long q[3];
+    qkey<TS>((const TS *)reg.verts + (size_t)sid * 3, mul, q);
+    unsigned long long slot = qhash(q) & mask;
+    long long found = -1;
+    for (int probe = 0; probe < kMaxProbes; ++probe) {
+        const unsigned long long cur = table[slot];
+        if (cur == kEmpty) break;
+        long long o[3];
+        qkey<TS>((const TS *)reg.verts + (size_t)cur * 3, mul, o);
+        if (o[0] == q[0] && o[1] == q[1] && o[2] == q[2]) {
+            found = (long long)cur;
+            break;
+        }
+        slot = (slot + (unsigned long long)probe + 1ull) & mask;
+    }
+    rep[sid] = found;
+    flag[sid] = (found == sid) ? 1 : 0;
+}
+
+template <typename TS>
+__global__ void weld_verts_kernel(RegionsDev reg, long long R, const long long *rep, const int *vidx, TS scale, TS cx,
+                                  TS cy, TS cz, TS *out)
+{
+    const long long sid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (sid >= R * kVMax) return;
+    if (rep[sid] != sid) return;
+    const TS *v = (const TS *)reg.verts + (size_t)sid * 3;
+    TS *o = out + (size_t)vidx[sid] * 3;
+    o[0] = v[0] * scale + cx;
+    o[1] = v[1] * scale + cy;
+    o[2] = v[2] * scale + cz;
+}
+
+__global__ void face_counts_kernel(RegionsDev reg, long long R, int *fflag, int *fsize)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const int n = reg.nv[r];
+    fflag[r] = n >= 3 ? 1 : 0;
+    fsize[r] = n >= 3 ? n : 0;
+}
+
+__global__ void faces_kernel(RegionsDev reg, long long R, const long long *rep, const int *vidx, const int *fid,
+                             const int *foff, int flip, int *face_sizes, int *face_idx)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const int n = reg.nv[r];
+    if (n < 3) return;
+    face_sizes[fid[r]] = n;
+    int *o = face_idx + foff[r];
+    for (int j = 0; j < n; ++j) {
+        const int i = flip ? (n - 1 - j) : j;
+        const long long rp = rep[r * kVMax + i];
+        o[j] = rp >= 0 ? vidx[rp] : -1;
+    }
+}
+
+__global__ void __launch_bounds__(kScanBlock) scan_count_kernel(const int *in, long long n, int *bsum)
+{
+    __shared__ int ws[32];
+    const long long q = blockIdx.x * (long long)kScanBlock + threadIdx.x;
+    int v = q < n ? in[q] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int s = ws[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) bsum[blockIdx.x] = s;
+    }
+}
+
+__device__ int block_scan(int v, int *total)
+{
+    __shared__ int wsum[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int s = wsum[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        wsum[lane] = s;
+    }
+    __syncthreads();
+    const int before = wid > 0 ? wsum[wid - 1] : 0;
+    *total = wsum[31];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanBlock) scan_offsets_kernel(int *bsum, long long nb, long long *total)
+{
+    __shared__ long long base;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (long long b0 = 0; b0 < nb; b0 += kScanBlock) {
+        const long long b = b0 + threadIdx.x;
+        const int v = b < nb ? bsum[b] : 0;
+        int tot;
+        const int pre = block_scan(v, &tot);
+        if (b < nb) bsum[b] = (int)(base + pre);
+        __syncthreads();
+        if (threadIdx.x == 0) base += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = base;
+}
+
+__global__ void __launch_bounds__(kScanBlock) scan_apply_kernel(const int *in, long long n, const int *bsum, int *out)
+{
+    const long long q = blockIdx.x * (long long)kScanBlock + threadIdx.x;
+    const int v = q < n ? in[q] : 0;
+    int tot;
+    const int pre = block_scan(v, &tot);
+    if (q < n) out[q] = bsum[blockIdx.x] + pre;
+}
+
+} // namespace
+
+void scan_exclusive(const int *in, long long n, int *out, int *bsum, long long *d_total, cudaStream_t st)
+{
+    if (n <= 0) {
+        cudaMemsetAsync(d_total, 0, sizeof(long long), st);
+        return;
+    }
+    const long long nb = (n + kScanBlock - 1) / kScanBlock;
+    scan_count_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(in, n, bsum);
+    scan_offsets_kernel<<<1, kScanBlock, 0, st>>>(bsum, nb, d_total);
+    scan_apply_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(in, n, bsum, out);
+}
+
+void launch_weld(int prec, const RegionsDev &reg, long long R, const WeldBuffers &wb, double scale,
+                 const double *center, int flip, int *d_err, cudaStream_t st)
+{
+    const long long nslots = R * kVMax;
+    const unsigned g1 = (unsigned)((nslots + 255) / 256);
+    const unsigned g2 = (unsigned)((R + 255) / 256);
+    cudaMemsetAsync(wb.table, 0xff, sizeof(unsigned long long) * (size_t)(wb.mask + 1), st);
+    const bool f64 = (prec != kFloat32);
+    const double mul = (prec == kFloat64) ? 1e9 : 1e6;
+    if (R <= 0) {
+        cudaMemsetAsync(wb.counts, 0, sizeof(long long) * 3, st);
+        return;
+    }
+    if (f64) {
+        weld_insert_kernel<double><<<g1, 256, 0, st>>>(reg, R, wb.table, wb.mask, mul, d_err);
+        weld_rep_kernel<double><<<g1, 256, 0, st>>>(reg, R, wb.table, wb.mask, mul, wb.rep, wb.flag);
+    } else {
+        weld_insert_kernel<float><<<g1, 256, 0, st>>>(reg, R, wb.table, wb.mask, mul, d_err);
+        weld_rep_kernel<float><<<g1, 256, 0, st>>>(reg, R, wb.table, wb.mask, mul, wb.rep, wb.flag);
+    }
+    scan_exclusive(wb.flag, nslots, wb.vidx, wb.bsum, wb.counts + 0, st);
+    if (f64)
+        weld_verts_kernel<double><<<g1, 256, 0, st>>>(reg, R, wb.rep, wb.vidx, scale, center[0], center[1], center[2],
+                                                      (double *)wb.out_verts);
+    else
+        weld_verts_kernel<float><<<g1, 256, 0, st>>>(reg, R, wb.rep, wb.vidx, (float)scale, (float)center[0],
+                                                     (float)center[1], (float)center[2], (float *)wb.out_verts);
+    face_counts_kernel<<<g2, 256, 0, st>>>(reg, R, wb.fflag, wb.fsize);
+    scan_exclusive(wb.fflag, R, wb.fid, wb.bsum, wb.counts + 1, st);
+    scan_exclusive(wb.fsize, R, wb.foff, wb.bsum, wb.counts + 2, st);
+    faces_kernel<<<g2, 256, 0, st>>>(reg, R, wb.rep, wb.vidx, wb.fid, wb.foff, flip, wb.face_sizes, wb.face_idx);
+}
+
+} // namespace am

@@ -1,0 +1,395 @@
+// am_polygon.cu -- face polygon of every region of a chunk, warp per face,
+// plus the frontier insert of its neighbours.
+//
+// The face of a region is the polygon {x : w_eq.x + b_eq = 0, C_k(x) <= 0 for
+// all k}.  The reference finds it by a pivot walk that tries candidate planes
+// in order of distance from a seed point, one 3x3 solve plus an N-row
+// feasibility scan per candidate, one candidate per region per round with a
+// host round trip between rounds (backend/inc/kernel.h:1258-1320).  Here one
+// warp owns a face: the region's constraint rows are staged in shared memory
+// and the walk is ray shooting along the current edge line -- a single pass
+// over the rows gives the first plane the line hits, and the vertex is the
+// 3x3 solve of (edge plane, hit plane, face plane).  The walk goes
+// counter-clockwise about w_eq, which is the orientation the reference's
+// correctNormalDirection enforces (kernel.h:1325-1370).  Zero-length edges
+// (vertices closer than FP_SAME_EPS in L1) are merged and spawn no neighbour,
+// as in cudaUpdateVert_kernel (kernel.h:1197-1205).
+//
+// Seed regions (start == -1) first find a polygon vertex exactly as the
+// reference's calcStartIdx does (kernel.h:799-856): planes ordered by signed
+// geometric distance from the seed point, pairs enumerated by get_i_j up to
+// x = min((ALL-1)(ALL-2), 812), the first pair whose vertex satisfies every
+// other constraint within FP_EPS wins.  Those pairs only involve the 57
+// nearest planes, so a partial selection replaces the reference's full sort.
+//
+// Every edge on a hidden unit's plane gives a neighbour: the key with that
+// bit flipped.  Its hash is updated in O(1) and it is inserted into the
+// region hash set (full-key comparison on fingerprint match); among equal new
+// keys the smallest (parent, plane) id wins, so the result is deterministic.
+#include <cuda/atomic>
+#include <cuda_runtime.h>
+
+#include "am_device.cuh"
+#include "am_internal.h"
+
+namespace am {
+
+namespace {
+
+template <typename T>
+__device__ __forceinline__ unsigned long long order_key(T d);
+template <>
+__device__ __forceinline__ unsigned long long order_key<float>(float d)
+{
+    if (d != d) return 0ull;
+    uint32_t u = __float_as_uint(d);
+    u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    return (unsigned long long)u;
+}
+template <>
+__device__ __forceinline__ unsigned long long order_key<double>(double d)
+{
+    if (d != d) return 0ull;
+    unsigned long long u = (unsigned long long)__double_as_longlong(d);
+    u = (u >> 63) ? ~u : (u | 0x8000000000000000ull);
+    return u;
+}
+
+// (key, index) pairs: a is ahead of b when its distance is larger, ties by lower index
+__device__ __forceinline__ bool ahead(unsigned long long ka, int ia, unsigned long long kb, int ib)
+{
+    return ka > kb || (ka == kb && ia < ib);
+}
+
+template <typename TS, typename TC>
+__device__ __forceinline__ void row_of(const vec4_t<TC> *rows, int k, TS *r)
+{
+    const vec4_t<TC> v = rows[k];
+    r[0] = (TS)v.x;
+    r[1] = (TS)v.y;
+    r[2] = (TS)v.z;
+    r[3] = (TS)v.w;
+}
+
+__device__ __forceinline__ unsigned long long load_slot(const unsigned long long *p)
+{
+    cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> a(*const_cast<unsigned long long *>(p));
+    return a.load(cuda::memory_order_relaxed);
+}
+
+// Does the key stored behind slot value `cur` equal parent_key ^ flip(k)?
+// Region entries (tag 0) point at the region store; candidate entries (tag 1)
+// carry (chunk-local parent, plane) and point at the parent's key.
+__device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long long head, int ALL, int W,
+                            const uint32_t *pkey, int k)
+{
+    const uint32_t id = (uint32_t)cur & 0x7fffffffu;
+    const bool cand = (cur >> 31) & 1ull;
+    const uint32_t *other;
+    int ok2 = -1;
+    if (cand) {
+        other = reg.keys + (size_t)(head + id / ALL) * W;
+        ok2 = (int)(id % ALL);
+    } else {
+        other = reg.keys + (size_t)id * W;
+    }
+    const int kw = k >> 5;
+    const uint32_t kb = 1u << (k & 31);
+    const int ow = ok2 >= 0 ? (ok2 >> 5) : -1;
+    const uint32_t ob = ok2 >= 0 ? (1u << (ok2 & 31)) : 0u;
+    for (int w = 0; w < W; ++w) {
+        uint32_t a = pkey[w] ^ (w == kw ? kb : 0u);
+        uint32_t b = other[w] ^ (w == ow ? ob : 0u);
+        if (a != b) return false;
+    }
+    return true;
+}
+
+template <typename TC, typename TS>
+__global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
+                                                      int *err, int staged)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const int ALL = net.ALL;
+    const int N = net.N;
+    const int W = net.W;
+    vec4_t<TC> *srows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)wib * net.ALLP;
+    const TS eps = (TS)tol.eps, same_eps = (TS)tol.same_eps, par_eps = (TS)tol.par_eps;
+
+    for (long long rl = (long long)blockIdx.x * wpb + wib; rl < ch.count; rl += (long long)gridDim.x * wpb) {
+        const long long rid = ch.head + rl;
+        const vec4_t<TC> *grows = reinterpret_cast<const vec4_t<TC> *>((const TC *)ch.cons + (size_t)rl * net.ALLP * 4);
+        const vec4_t<TC> *rows = grows;
+        if (staged) {
+            for (int q = lane; q < ALL; q += 32) srows[q] = grows[q];
+            __syncwarp();
+            rows = srows;
+        }
+        TS eqv[4];
+        {
+            const vec4_t<TC> e = ld4<TC>((const TC *)ch.eq + (size_t)rl * 4);
+            eqv[0] = (TS)e.x;
+            eqv[1] = (TS)e.y;
+            eqv[2] = (TS)e.z;
+            eqv[3] = (TS)e.w;
+        }
+        const TS *midp = (const TS *)reg.mid + (size_t)rid * 4;
+        TS p[3] = {midp[0], midp[1], midp[2]};
+        int s = reg.start[rid];
+        const bool is_seed = (s < 0);
+        int8_t status = kOk;
+
+        // ---------------------------------------------------- seed start search
+        if (is_seed) {
+            // pairs x <= 812 reach sorted positions up to 56: keep the 64 nearest,
+            // position q in lane q % 32, register q / 32
+            const int ksel = ALL < kTopK ? ALL : kTopK;
+            int top0 = -1, top1 = -1;
+            unsigned long long pk = ~0ull;
+            int pi = -1;
+            for (int sel = 0; sel < ksel; ++sel) {
+                unsigned long long bk = 0ull;
+                int bi = 0x7fffffff;
+                for (int k = lane; k < ALL; k += 32) {
+                    const vec4_t<TC> v = rows[k];
+                    const TC acc = v.x * (TC)p[0] + v.y * (TC)p[1] + v.z * (TC)p[2] + v.w;
+                    const TC d = acc * (TC(1) / sqrt(v.x * v.x + v.y * v.y + v.z * v.z));
+                    const unsigned long long key = order_key<TC>(d);
+                    const bool below = key < pk || (key == pk && k > pi);
+                    if (below && ahead(key, k, bk, bi)) {
+                        bk = key;
+                        bi = k;
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const unsigned long long ok = __shfl_xor_sync(0xffffffffu, bk, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ahead(ok, oi, bk, bi)) {
+                        bk = ok;
+                        bi = oi;
+                    }
+                }
+                if (lane == (sel & 31)) {
+                    if (sel < 32) top0 = bi;
+                    else top1 = bi;
+                }
+                pk = bk;
+                pi = bi;
+            }
+            int x_max = (ALL - 1) * (ALL - 2);
+            if (x_max > 812) x_max = 812;
+            if (x_max < 0) x_max = 0;
+            s = -1;
+            for (int x = 0; x <= x_max; ++x) {
+                int i, j;
+                get_i_j(x, ALL, i, j);
+                const int ri = i < 32 ? __shfl_sync(0xffffffffu, top0, i) : __shfl_sync(0xffffffffu, top1, i - 32);
+                const int rj = j < 32 ? __shfl_sync(0xffffffffu, top0, j) : __shfl_sync(0xffffffffu, top1, j - 32);
+                TS r0[4], r1[4], v[3];
+                row_of<TS, TC>(rows, ri, r0);
+                row_of<TS, TC>(rows, rj, r1);
+                solve3<TS>(r0, r1, eqv, v);
+                bool bad = false;
+                for (int k = lane; k < ALL; k += 32) {
+                    if (k == ri || k == rj) continue;
+                    TS r[4];
+                    row_of<TS, TC>(rows, k, r);
+                    const TS ans = r[0] * v[0] + r[1] * v[1] + r[2] * v[2] + r[3];
+                    const TS rs = TS(1) / sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+                    if (ans * rs > eps) bad = true;
+                }
+                if (!__any_sync(0xffffffffu, bad)) {
+                    s = ri;
+                    p[0] = v[0];
+                    p[1] = v[1];
+                    p[2] = v[2];
+                    break;
+                }
+            }
+            if (s < 0) status = kNoStart;
+        }
+
+        // ---------------------------------------------------- walk
+        // lane i holds vertex i and the plane of the edge leaving it
+        TS vx = 0, vy = 0, vz = 0;
+        int ve = -1;
+        int n = 0;
+        bool closed = false;
+        if (s >= 0) {
+            int e = s, prev = -1;
+            TS cur[3] = {p[0], p[1], p[2]};
+            for (int step = 0; step < kWalkSteps; ++step) {
+                TS re[4];
+                row_of<TS, TC>(rows, e, re);
+                const TS d0 = eqv[1] * re[2] - eqv[2] * re[1];
+                const TS d1 = eqv[2] * re[0] - eqv[0] * re[2];
+                const TS d2 = eqv[0] * re[1] - eqv[1] * re[0];
+                const TS dn = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+                TS bt = TS(INFINITY);
+                int bk = 0x7fffffff;
+                for (int k = lane; k < ALL; k += 32) {
+                    if (k == e || k == prev) continue;
+                    TS r[4];
+                    row_of<TS, TC>(rows, k, r);
+                    const TS a = r[0] * d0 + r[1] * d1 + r[2] * d2;
+                    const TS wn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+                    if (!(a > par_eps * wn * dn)) continue; // parallel or receding
+                    const TS g = r[0] * cur[0] + r[1] * cur[1] + r[2] * cur[2] + r[3];
+                    TS t = -g / a;
+                    if (!(t > TS(0))) t = TS(0); // plane through (or behind) the current point
+                    if (t < bt || (t == bt && k < bk)) {
+                        bt = t;
+                        bk = k;
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const TS ot = __shfl_xor_sync(0xffffffffu, bt, o);
+                    const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+                    if (ot < bt || (ot == bt && ok < bk)) {
+                        bt = ot;
+                        bk = ok;
+                    }
+                }
+                if (bk == 0x7fffffff) { // the edge line never leaves the region
+                    status = kOpen;
+                    break;
+                }
+                TS rk[4], V[3];
+                row_of<TS, TC>(rows, bk, rk);
+                solve3<TS>(re, rk, eqv, V);
+                if (!(isfinite(V[0]) && isfinite(V[1]) && isfinite(V[2]))) {
+                    status = kSingular;
+                    break;
+                }
+                bool appended = false;
+                if (n > 0) {
+                    const TS lx = __shfl_sync(0xffffffffu, vx, n - 1);
+                    const TS ly = __shfl_sync(0xffffffffu, vy, n - 1);
+                    const TS lz = __shfl_sync(0xffffffffu, vz, n - 1);
+                    const TS fx = __shfl_sync(0xffffffffu, vx, 0);
+                    const TS fy = __shfl_sync(0xffffffffu, vy, 0);
+                    const TS fz = __shfl_sync(0xffffffffu, vz, 0);
+                    if (fabs(V[0] - lx) + fabs(V[1] - ly) + fabs(V[2] - lz) < same_eps) {
+                        if (lane == n - 1) ve = bk; // zero-length edge on e: merge
+                    } else if (bk == s && fabs(V[0] - fx) + fabs(V[1] - fy) + fabs(V[2] - fz) < same_eps) {
+                        // zero-length closing edge on the start plane
+                    } else {
+                        appended = true;
+                    }
+                } else {
+                    appended = true;
+                }
+                if (appended) {
+                    if (lane == n) {
+                        vx = V[0];
+                        vy = V[1];
+                        vz = V[2];
+                        ve = bk;
+                    }
+                    n++;
+                }
+                if (bk == s) {
+                    closed = true;
+                    break;
+                }
+                if (n >= kVMax) {
+                    status = kTruncated;
+                    break;
+                }
+                prev = e;
+                e = bk;
+                cur[0] = V[0];
+                cur[1] = V[1];
+                cur[2] = V[2];
+            }
+            if (!closed && status == kOk) status = kTruncated;
+        }
+
+        // ---------------------------------------------------- outputs
+        if (lane == 0) {
+            reg.nv[rid] = n;
+            reg.status[rid] = status;
+        }
+        if (lane < n) {
+            TS *vo = (TS *)reg.verts + ((size_t)rid * kVMax + lane) * 3;
+            vo[0] = vx;
+            vo[1] = vy;
+            vo[2] = vz;
+            reg.edges[(size_t)rid * kVMax + lane] = ve;
+        }
+
+        // ---------------------------------------------------- neighbours
+        int rec = -1;
+        const uint32_t *pkey = reg.keys + (size_t)rid * W;
+        const bool spawn = lane < n && ve >= 0 && ve < N && (closed || lane < n - 1) && !(!is_seed && ve == s);
+        if (spawn) {
+            const int k = ve;
+            const uint64_t h = flip_hash(reg.hash[rid], pkey[k >> 5], k);
+            const uint32_t fp = fp_of(h);
+            const uint32_t myid = (uint32_t)(rl * ALL + k);
+            const unsigned long long mine = slot_value(fp, 1, myid);
+            unsigned long long slot = h & hs.mask;
+            int probe = 0;
+            for (; probe < kMaxProbes; ++probe) {
+                unsigned long long cur = load_slot(hs.slots + slot);
+                if (cur == kEmpty) {
+                    const unsigned long long old = atomicCAS(hs.slots + slot, kEmpty, mine);
+                    if (old == kEmpty) {
+                        rec = (int)slot;
+                        break;
+                    }
+                    cur = old;
+                }
+                if ((uint32_t)(cur >> 32) == fp && key_matches(cur, reg, ch.head, ALL, W, pkey, k)) {
+                    if ((cur >> 31) & 1ull) {
+                        atomicMin(hs.slots + slot, mine);
+                        rec = (int)slot;
+                    }
+                    break;
+                }
+                slot = (slot + (unsigned long long)probe + 1ull) & hs.mask;
+            }
+            if (probe == kMaxProbes) atomicOr(err, kErrTableFull);
+        }
+        if (lane < kVMax) ch.rec[(size_t)rl * kVMax + lane] = rec;
+        __syncwarp();
+    }
+}
+
+} // namespace
+
+void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs,
+                    const Tolerances &tol, int *d_err, cudaStream_t st)
+{
+    if (ch.count <= 0) return;
+    const size_t row_bytes = (prec == kFloat64 ? sizeof(double4) : sizeof(float4)) * (size_t)net.ALLP;
+    int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96u * 1024u) / std::max<size_t>(row_bytes, 1)));
+    int staged = row_bytes <= 200u * 1024u ? 1 : 0;
+    if (!staged) wpb = 8;
+    const size_t smem = staged ? row_bytes * wpb : 0;
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long need = (ch.count + wpb - 1) / wpb;
+    const int grid = (int)std::min<long long>(need, (long long)sms * 16);
+    if (prec == kFloat64) {
+        auto k = polygon_kernel<double, double>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err, staged);
+    } else if (prec == kMixed) {
+        auto k = polygon_kernel<float, double>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err, staged);
+    } else {
+        auto k = polygon_kernel<float, float>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err, staged);
+    }
+}
+
+} // namespace am

@@ -1,0 +1,120 @@
+/*
+ * analyticmesh_gb300.h -- C ABI of the GB300 Analytic Marching engine.
+ *
+ * The first five entry points are the reference's pybind11 module `cuam`
+ * (backend/src/cuam.cpp:186-217, imported by backend/main.py:13) restated as
+ * plain C: same call order (Init -> AnalyticMarching -> CombineMesh ->
+ * ExportMesh, Destroy at re-initialisation or exit), same argument meaning,
+ * but an explicit engine handle instead of the reference's global singleton
+ * (backend/src/cuam_kernel.cu:23) and status codes instead of exit() / silent
+ * prints.  Float arrays are float32 for float_type "float32" and "mixed",
+ * float64 for "float64".  Every pointer argument may be host or device
+ * memory; the engine detects which.  Calls on one engine must not overlap;
+ * separate engines are independent.
+ */
+#ifndef ANALYTICMESH_GB300_H
+#define ANALYTICMESH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct am_engine am_engine;
+
+typedef enum {
+    AM_OK = 0,
+    AM_ERR_INVALID_ARGUMENT = 1, /* the reference: TORCH_CHECK -> RuntimeError */
+    AM_ERR_NOT_INITIALIZED = 2,  /* the reference: prints and returns (cuam.cpp:107-111) */
+    AM_ERR_CUDA = 3,             /* the reference: exit(code) (utilities.h:87-101) */
+    AM_ERR_OUT_OF_MEMORY = 4,
+    AM_ERR_TABLE_FULL = 5,       /* hash probe bound hit; the reference spins forever (hash.h:56-64) */
+    AM_ERR_NO_RESULT = 6,        /* CombineMesh / ExportMesh before AnalyticMarching (cuam_kernel.cu:193-197) */
+    AM_ERR_IO = 7,
+    AM_ERR_CAPACITY = 8
+} am_status;
+
+/* Init -- backend/src/cuam.cpp:58-95 and backend/src/cuam_kernel.cu:128-148.
+ * float_type: "float32" (plain FP32 form), "float64", or "mixed" (float32
+ * inputs; tensor-core composition, FP64 vertex solves).  nodesnum: layer
+ * widths including the input (3) and the output (1), at least 3 entries.
+ * arc_table: (num_nodes - 2) rows x arc_cols int32, row i = connections into
+ * linear layer i + 1: [count, src_0, tm_0, src_1, tm_1, ...]. */
+int am_init(am_engine **engine, const char *float_type, const int32_t *nodesnum, int num_nodes,
+            const int32_t *arc_table, int arc_rows, int arc_cols, int num_extra_constraints);
+
+/* AnalyticMarching -- backend/src/cuam.cpp:97-184 and cuam_kernel.cu:104-123.
+ * weights[i]: nodesnum[i+1] x nodesnum[i] row-major, biases[i]: nodesnum[i+1];
+ * states: num_points x N bytes (0/1), N = sum of hidden widths;
+ * points: num_points x 3; arc_tm[t]: arc_tm_shapes[2t] x arc_tm_shapes[2t+1]
+ * (0 x 0 = identity); w_extra: E x 3, b_extra: E (E from am_init).
+ * stream: a cudaStream_t, or NULL for the engine's own stream.  Returns when
+ * the marching is complete. */
+int am_analytic_marching(am_engine *engine, const void *const *weights, const void *const *biases,
+                         const uint8_t *states, const void *points, int num_points, const void *const *arc_tm,
+                         const int32_t *arc_tm_shapes, int num_arc_tm, const void *w_extra, const void *b_extra,
+                         double iso, int flip_insideout, void *stream);
+
+/* CombineMesh -- backend/src/cuam_kernel.cu:185-200: weld vertices, index
+ * faces; output vertex = vertex * scale + center. */
+int am_combine_mesh(am_engine *engine, double scale, const double *center3);
+
+/* ExportMesh -- backend/src/cuam_kernel.cu:205-246 (binary little-endian PLY,
+ * polygons or triangle fans, float or double vertices, polymesh.h:350-423). */
+int am_export_mesh(am_engine *engine, const char *file_path, int is_polymesh, int is_float32);
+
+/* Destroy -- backend/src/cuam_kernel.cu:153-179. */
+int am_destroy(am_engine *engine);
+
+const char *am_strerror(int status);
+/* Detail of the last failure on this engine (CUDA error text, which check failed). */
+const char *am_last_error(const am_engine *engine);
+
+/* ---- results: no counterpart in the reference, which only writes a PLY. */
+typedef struct {
+    int64_t num_regions;      /* regions visited */
+    int64_t num_faces;        /* face polygons with >= 3 vertices */
+    int64_t num_seeds;        /* seed regions after de-duplication */
+    int64_t num_nostart;      /* seed regions without a feasible start vertex */
+    int64_t num_open;         /* walks that found no closing vertex */
+    int64_t num_truncated;    /* polygons that hit the vertex capacity */
+    int64_t num_singular;
+    int64_t mesh_num_verts;   /* after am_combine_mesh */
+    int64_t mesh_num_faces;
+    int64_t mesh_num_indices;
+    int32_t chunks;
+    int32_t max_polygon_verts;
+    double am_time_ms;        /* device time of the marching loop (seeds to last chunk) */
+    double compose_ms;        /* per-phase device time, when AM_OPT_PHASE_TIMING is set */
+    double polygon_ms;
+    double frontier_ms;
+    int64_t kernel_launches;  /* launches inside the marching loop */
+} am_stats;
+
+int am_get_stats(const am_engine *engine, am_stats *out);
+
+/* Welded mesh after am_combine_mesh: verts mesh_num_verts x 3, face_sizes
+ * mesh_num_faces, face_indices mesh_num_indices (host memory). */
+int am_get_mesh(am_engine *engine, double *verts, int32_t *face_sizes, int32_t *face_indices);
+
+/* Per-region records in region-id order (host memory, any may be NULL):
+ * bits num_regions x ceil(N/32); nverts num_regions; verts num_regions x
+ * vert_capacity x 3; edges num_regions x vert_capacity (plane of the edge
+ * leaving each vertex); status num_regions; seeds num_regions x 3 (seed point
+ * or parent edge midpoint); start num_regions (start plane, -1 for seeds). */
+int am_get_regions(am_engine *engine, uint32_t *bits, int32_t *nverts, double *verts, int32_t *edges, int8_t *status,
+                   double *seeds, int32_t *start);
+int am_vert_capacity(void);
+
+typedef enum {
+    AM_OPT_CHUNK = 1,         /* regions per chunk (default: sized to ~1 GiB of constraint rows) */
+    AM_OPT_PHASE_TIMING = 2   /* 1: time compose / polygon / frontier separately */
+} am_option;
+int am_set_option(am_engine *engine, int option, int64_t value);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,167 @@
+"""CUDA engine parity through the C ABI (GPU tests).
+
+The engine processes regions in a different order from the reference (FIFO
+chunks instead of LIFO batches of 1024) and builds each face polygon by ray
+shooting instead of a sorted candidate scan, so the comparison is order-free
+(oracle/compare.py:canonical): identical region sets (activation bit
+strings) and, per region, the same polygon up to rotation within 1e-5.
+"""
+import numpy as np
+import pytest
+import torch
+
+from analyticmesh_gb300 import engine, workloads as wl
+from oracle import compare as CM
+from oracle import oracle as O
+
+from golden_io import load, names
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"float32": 1e-5, "float64": 1e-9}
+
+
+def f_at(net, pts):
+    """FP64 forward pass of the network at pts (N, 3)."""
+    x = np.asarray(pts, np.float64)
+    srcs = {}
+    n_lin = len(net.nodes) - 1
+    for i in range(n_lin):
+        srcs[i] = x
+        y = x @ net.W[i].T + net.b[i]
+        if i >= 1:
+            row = net.arc_table[i - 1]
+            for c in range(int(row[0])):
+                src, t = int(row[1 + 2 * c]), int(row[2 + 2 * c])
+                tm = net.tms[t]
+                y = y + (srcs[src] if tm.size == 0 else srcs[src] @ tm.T)
+        x = np.maximum(y, 0.0) if i < n_lin - 1 else y
+    return x[:, 0]
+
+
+def _golden_cases():
+    return [n for n in names() if not n.startswith("polytope")]
+
+
+@pytest.mark.parametrize("name", _golden_cases())
+def test_engine_matches_reference_golden(name):
+    g = load(name)
+    eng = engine.march(g["net"], g["states"], g["points"], g["dtype"], iso=g["iso"], flip_insideout=g["flip"])
+    reg = eng.regions()
+    c = CM.canonical(reg, g["regions"], tol=TOL[g["dtype"]])
+    assert c["only_a"] == 0 and c["only_b"] == 0, c
+    assert c["faces_only_a"] == 0 and c["faces_only_b"] == 0 and c["faces_mismatch"] == 0, c
+    eng.close()
+
+
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+@pytest.mark.parametrize("factory,nseed", [
+    (lambda: wl.geometric([32, 32], 7), 128),
+    (lambda: wl.geometric([48, 48, 48], 12, perturb=0.05), 256),
+    (lambda: wl.geometric([24, 24, 24, 24], 9, skips=[[0], [1, 1, 0], [1, 0, 1], [0]], tm_shapes=[[0, 0], [24, 3]]), 256),
+], ids=["plain", "perturbed", "skips"])
+def test_engine_matches_oracle(factory, nseed, dtype):
+    m = factory()
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=nseed, seed=3)
+    eng = engine.march(net, st, pt, dtype)
+    reg = eng.regions()
+    ref = O.run_oracle(net, st, pt, dtype=dtype)
+    c = CM.canonical(reg, ref, tol=TOL[dtype])
+    assert c["only_a"] == 0 and c["only_b"] == 0, c
+    assert c["faces_only_a"] == 0 and c["faces_only_b"] == 0 and c["faces_mismatch"] == 0, c
+    # every vertex on the zero level set
+    v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in range(reg.num) if reg.nverts[i] >= 3])
+    assert np.abs(f_at(net, v)).max() <= (1e-5 if dtype == "float32" else 1e-10)
+    eng.close()
+
+
+def test_sphere_config_parity_and_accuracy():
+    m = wl.sphere()
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=1024, seed=1)
+    eng = engine.march(net, st, pt, "float32")
+    reg = eng.regions()
+    ref = O.run_oracle(net, st, pt, dtype="float32")
+    c = CM.canonical(reg, ref, tol=1e-5)
+    assert c["only_a"] == 0 and c["only_b"] == 0, c
+    assert c["faces_mismatch"] == 0, c
+    v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in range(reg.num) if reg.nverts[i] >= 3])
+    assert np.abs(f_at(net, v)).max() <= 1e-5
+    eng.close()
+
+
+def test_output_skip_connections_are_composed():
+    # a skip into the output layer (the reference ignores it, process.h:42)
+    m = wl.geometric([20, 20, 20], 31, skips=[[0], [1, 1, 0]], tm_shapes=[[1, 20]])
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=4)
+    eng = engine.march(net, st, pt, "float64")
+    reg = eng.regions()
+    assert reg.num > 0
+    v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in range(reg.num) if reg.nverts[i] >= 3])
+    assert np.abs(f_at(net, v)).max() <= 1e-10
+    eng.close()
+
+
+def test_polytope_known_answer():
+    """3 -> 14 -> 1: f = sum_k |a_k . x| - 2 over 7 directions; every mesh
+    vertex lies on that surface and every edge is shared by two faces."""
+    m = wl.polytope()
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=256, seed=5)
+    eng = engine.march(net, st, pt, "float64")
+    mesh = eng.combine()
+    assert len(mesh.face_sizes) > 0
+    dirs = np.array([[1, 1, 1], [0, 1, 1], [1, 0, 1], [1, 1, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    f = np.abs(mesh.verts @ dirs.T).sum(1) - 2.0
+    assert np.abs(f).max() < 1e-5
+    eng.close()
+
+
+def test_mesh_combine_matches_oracle():
+    m = wl.geometric([32, 32], 7)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=11)
+    eng = engine.march(net, st, pt, "float32")
+    mesh = eng.combine(scale=2.0, center=(0.1, -0.2, 0.3))
+    _, om = O.run_oracle(net, st, pt, dtype="float32", combine=(2.0, [0.1, -0.2, 0.3]))
+    assert mesh.verts.shape == om.verts.shape
+    assert len(mesh.face_sizes) == len(om.faces)
+    key = lambda vs, f: tuple(sorted(tuple(np.round(vs[i], 5)) for i in f))
+    a = sorted(key(mesh.verts, f) for f in mesh.faces)
+    b = sorted(key(om.verts, f) for f in om.faces)
+    assert a == b
+    eng.close()
+
+
+def test_watertight_sphere_mesh():
+    m = wl.sphere()
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=1024, seed=1)
+    eng = engine.march(net, st, pt, "float32")
+    mesh = eng.combine()
+    edges = {}
+    for f in mesh.faces:
+        for a, b in zip(f, f[1:] + f[:1]):
+            e = (min(a, b), max(a, b))
+            edges[e] = edges.get(e, 0) + 1
+    counts = np.array(list(edges.values()))
+    assert (counts == 2).mean() > 0.999
+    eng.close()
+
+
+def test_host_and_device_inputs_agree():
+    m = wl.geometric([32, 32], 7)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=11)
+    e1 = engine.march(net, st, pt, "float32")
+    dev = torch.device("cuda")
+    e2 = engine.Engine("float32", net.nodes, net.arc_table, 0)
+    e2.run([torch.tensor(w, dtype=torch.float32, device=dev) for w in net.W],
+           [torch.tensor(b, dtype=torch.float32, device=dev) for b in net.b],
+           torch.tensor(st, dtype=torch.bool, device=dev), torch.tensor(pt, dtype=torch.float32, device=dev))
+    r1, r2 = e1.regions(), e2.regions()
+    assert np.array_equal(r1.bits, r2.bits) and np.array_equal(r1.nverts, r2.nverts)
+    e1.close()
+    e2.close()
