@@ -30,6 +30,7 @@ class AmStats(C.Structure):
 
 AM_OPT_CHUNK = 1
 AM_OPT_PHASE_TIMING = 2
+AM_OPT_WELD = 3
 
 
 class AmError(RuntimeError):

@@ -128,6 +128,7 @@ struct am_engine {
     std::string last_error;
     int64_t chunk_opt = 0;
     bool phase_timing = false;
+    int weld_mode = 0;
 
     // network
     DevBuf wt[kMaxLayers], bias[kMaxLayers], w0, tmt[64], wext, bext, scratch;
@@ -330,6 +331,8 @@ int am_init(am_engine **out, const char *float_type, const int32_t *nodesnum, in
         e->ALL = e->N + e->E;
         e->ALLP = (e->ALL + 7) / 8 * 8;
         e->W = (e->N + 31) / 32;
+        AM_CHECK((size_t)e->ALLP * 4 * (e->prec == kFloat64 ? 8 : 4) <= 200u * 1024u,
+                 "too many constraint rows for one face (sum of hidden widths + extra constraints)");
         AM_CUDA(cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking));
         e->st = e->own;
         AM_CUDA(e->d_tail.alloc(sizeof(long long)));
@@ -349,6 +352,11 @@ int am_set_option(am_engine *e, int option, int64_t value)
     }
     if (option == AM_OPT_PHASE_TIMING) {
         e->phase_timing = value != 0;
+        return AM_OK;
+    }
+    if (option == AM_OPT_WELD) {
+        if (value != 0 && value != 1) return AM_ERR_INVALID_ARGUMENT;
+        e->weld_mode = (int)value;
         return AM_OK;
     }
     return AM_ERR_INVALID_ARGUMENT;
@@ -657,7 +665,8 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
         wb.counts = e->w_counts.as<long long>();
         const double c0[3] = {0, 0, 0};
         AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
-        launch_weld(e->prec, e->regions(), R, wb, scale, center3 ? center3 : c0, e->flip, e->d_err.as<int>(), st);
+        launch_weld(e->prec, e->weld_mode, e->N, e->W, e->regions(), R, wb, scale, center3 ? center3 : c0, e->flip,
+                    e->d_err.as<int>(), st);
         AM_CUDA(cudaGetLastError());
         long long cnt[3] = {0, 0, 0};
         AM_CUDA(cudaMemcpyAsync(cnt, wb.counts, sizeof(cnt), cudaMemcpyDeviceToHost, st));

@@ -1,13 +1,21 @@
 // am_mesh.cu -- CombineMesh on the device: weld the vertices of all face
 // polygons and index the faces.
 //
-// Same quantisation as the reference's PolyMesh (backend/inc/polymesh.h:
-// 174-335, int(v * 1e6) for fp32 data, int(v * 1e9) for fp64), but the weld
-// compares the quantised coordinates exactly instead of by a 32-bit
-// fingerprint (polymesh.h:305), and vertex / face numbering follows region
-// order (first occurrence), independent of thread scheduling.  Vertices of
-// polygons with fewer than 3 corners are welded too, as in the reference;
-// only polygons with 3 or more corners become faces.
+// Two weld keys:
+// * topological (default): a polygon vertex is the intersection of the face
+//   plane with the two planes of its edges (p, q).  Every region meeting at
+//   that mesh vertex differs only in the bits of p and q, so (p, q, region
+//   key with bits p and q cleared) names the vertex exactly and the mesh is
+//   watertight whatever the rounding of the coordinates.
+// * quantised, as the reference's PolyMesh (backend/inc/polymesh.h:174-335):
+//   int(v * 1e6) for fp32 data, int(v * 1e9) for fp64, compared exactly
+//   rather than by a 32-bit fingerprint (polymesh.h:305).  With fp32
+//   coordinates this splits vertices whose copies round to different grid
+//   cells.
+// Vertex / face numbering follows region order (first occurrence), so it does
+// not depend on thread scheduling.  Vertices of polygons with fewer than 3
+// corners are welded too, as in the reference; only polygons with 3 or more
+// corners become faces.
 #include <cuda/atomic>
 #include <cuda_runtime.h>
 
@@ -21,39 +29,97 @@ namespace {
 
 constexpr int kScanBlock = 1024;
 
-template <typename TS>
-__device__ __forceinline__ void qkey(const TS *v, double mul, long long *q)
-{
-    // the reference converts v * MUL in the working precision to int
-    q[0] = (long long)(int)(v[0] * (TS)mul);
-    q[1] = (long long)(int)(v[1] * (TS)mul);
-    q[2] = (long long)(int)(v[2] * (TS)mul);
-}
-
 __device__ __forceinline__ uint64_t qhash(const long long *q)
 {
     return mix64((uint64_t)q[0] * 0x9E3779B97F4A7C15ull ^ mix64((uint64_t)q[1] + 0x632BE59BD9B4E019ull) ^
                  mix64((uint64_t)q[2] * 0xD6E8FEB86659FD93ull + 7));
 }
 
+struct VKey {
+    uint64_t h;
+    long long q[3]; // quantised coordinates, or (p, q, -) for the topological key
+};
+
+// planes of the two edges meeting at vertex i of region r
+__device__ __forceinline__ void vertex_planes(const RegionsDev &reg, long long r, int i, int n, int &p, int &q)
+{
+    p = reg.edges[(size_t)r * kVMax + (i + n - 1) % n];
+    q = reg.edges[(size_t)r * kVMax + i];
+    if (p > q) {
+        const int t = p;
+        p = q;
+        q = t;
+    }
+}
+
+__device__ __forceinline__ uint32_t pq_mask(int w, int p, int q, int N)
+{
+    uint32_t m = 0u;
+    if (p >= 0 && p < N && (p >> 5) == w) m |= 1u << (p & 31);
+    if (q >= 0 && q < N && (q >> 5) == w) m |= 1u << (q & 31);
+    return m;
+}
+
 template <typename TS>
-__global__ void weld_insert_kernel(RegionsDev reg, long long R, unsigned long long *table, unsigned long long mask,
-                                   double mul, int *err)
+__device__ bool make_key(const RegionsDev &reg, int mode, int N, int W, double mul, long long sid, VKey &k)
+{
+    const long long r = sid / kVMax;
+    const int i = (int)(sid % kVMax);
+    const int n = reg.nv[r];
+    if (i >= n) return false;
+    if (mode == 0) {
+        int p, q;
+        vertex_planes(reg, r, i, n, p, q);
+        const uint32_t *key = reg.keys + (size_t)r * W;
+        uint64_t h = reg.hash[r];
+        // clear bits p and q through the additive hash, word by word
+        const int wp = p >= 0 && p < N ? p >> 5 : -1, wq = q >= 0 && q < N ? q >> 5 : -1;
+        if (wp >= 0) h = h - word_term(key[wp], wp) + word_term(key[wp] & ~pq_mask(wp, p, q, N), wp);
+        if (wq >= 0 && wq != wp) h = h - word_term(key[wq], wq) + word_term(key[wq] & ~pq_mask(wq, p, q, N), wq);
+        k.q[0] = p;
+        k.q[1] = q;
+        k.q[2] = 0;
+        k.h = mix64(h ^ mix64(((uint64_t)(uint32_t)p << 32) | (uint32_t)q));
+    } else {
+        const TS *v = (const TS *)reg.verts + (size_t)sid * 3;
+        k.q[0] = (long long)(int)(v[0] * (TS)mul);
+        k.q[1] = (long long)(int)(v[1] * (TS)mul);
+        k.q[2] = (long long)(int)(v[2] * (TS)mul);
+        k.h = qhash(k.q);
+    }
+    return true;
+}
+
+__device__ bool same_vertex(const RegionsDev &reg, int mode, int N, int W, const VKey &a, long long sa, const VKey &b,
+                            long long sb)
+{
+    if (a.q[0] != b.q[0] || a.q[1] != b.q[1] || a.q[2] != b.q[2]) return false;
+    if (mode != 0) return true;
+    const uint32_t *ka = reg.keys + (size_t)(sa / kVMax) * W;
+    const uint32_t *kb = reg.keys + (size_t)(sb / kVMax) * W;
+    const int p = (int)a.q[0], q = (int)a.q[1];
+    for (int w = 0; w < W; ++w) {
+        const uint32_t m = ~pq_mask(w, p, q, N);
+        if ((ka[w] & m) != (kb[w] & m)) return false;
+    }
+    return true;
+}
+
+template <typename TS>
+__global__ void weld_insert_kernel(RegionsDev reg, long long R, int mode, int N, int W, unsigned long long *table,
+                                   unsigned long long mask, double mul, int *err)
 {
     const long long sid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (sid >= R * kVMax) return;
-    const long long r = sid / kVMax;
-    const int i = (int)(sid % kVMax);
-    if (i >= reg.nv[r]) return;
-    long long q[3];
-    qkey<TS>((const TS *)reg.verts + (size_t)sid * 3, mul, q);
-    unsigned long long slot = qhash(q) & mask;
+    VKey k;
+    if (!make_key<TS>(reg, mode, N, W, mul, sid, k)) return;
+    unsigned long long slot = k.h & mask;
     for (int probe = 0; probe < kMaxProbes; ++probe) {
-        unsigned long long cur = atomicCAS(table + slot, kEmpty, (unsigned long long)sid);
+        const unsigned long long cur = atomicCAS(table + slot, kEmpty, (unsigned long long)sid);
         if (cur == kEmpty) return;
-        long long o[3];
-        qkey<TS>((const TS *)reg.verts + (size_t)cur * 3, mul, o);
-        if (o[0] == q[0] && o[1] == q[1] && o[2] == q[2]) {
+        VKey o;
+        make_key<TS>(reg, mode, N, W, mul, (long long)cur, o);
+        if (o.h == k.h && same_vertex(reg, mode, N, W, k, sid, o, (long long)cur)) {
             atomicMin(table + slot, (unsigned long long)sid);
             return;
         }
@@ -63,28 +129,25 @@ __global__ void weld_insert_kernel(RegionsDev reg, long long R, unsigned long lo
 }
 
 template <typename TS>
-__global__ void weld_rep_kernel(RegionsDev reg, long long R, const unsigned long long *table, unsigned long long mask,
-                                double mul, long long *rep, int *flag)
+__global__ void weld_rep_kernel(RegionsDev reg, long long R, int mode, int N, int W, const unsigned long long *table,
+                                unsigned long long mask, double mul, long long *rep, int *flag)
 {
     const long long sid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (sid >= R * kVMax) return;
-    const long long r = sid / kVMax;
-    const int i = (int)(sid % kVMax);
-    if (i >= reg.nv[r]) {
+    VKey k;
+    if (!make_key<TS>(reg, mode, N, W, mul, sid, k)) {
         flag[sid] = 0;
         rep[sid] = -1;
         return;
     }
-    long long q[3];
-    qkey<TS>((const TS *)reg.verts + (size_t)sid * 3, mul, q);
-    unsigned long long slot = qhash(q) & mask;
+    unsigned long long slot = k.h & mask;
     long long found = -1;
     for (int probe = 0; probe < kMaxProbes; ++probe) {
         const unsigned long long cur = table[slot];
         if (cur == kEmpty) break;
-        long long o[3];
-        qkey<TS>((const TS *)reg.verts + (size_t)cur * 3, mul, o);
-        if (o[0] == q[0] && o[1] == q[1] && o[2] == q[2]) {
+        VKey o;
+        make_key<TS>(reg, mode, N, W, mul, (long long)cur, o);
+        if (o.h == k.h && same_vertex(reg, mode, N, W, k, sid, o, (long long)cur)) {
             found = (long long)cur;
             break;
         }
@@ -219,8 +282,8 @@ void scan_exclusive(const int *in, long long n, int *out, int *bsum, long long *
     scan_apply_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(in, n, bsum, out);
 }
 
-void launch_weld(int prec, const RegionsDev &reg, long long R, const WeldBuffers &wb, double scale,
-                 const double *center, int flip, int *d_err, cudaStream_t st)
+void launch_weld(int prec, int mode, int N, int W, const RegionsDev &reg, long long R, const WeldBuffers &wb,
+                 double scale, const double *center, int flip, int *d_err, cudaStream_t st)
 {
     const long long nslots = R * kVMax;
     const unsigned g1 = (unsigned)((nslots + 255) / 256);
@@ -233,11 +296,11 @@ void launch_weld(int prec, const RegionsDev &reg, long long R, const WeldBuffers
         return;
     }
     if (f64) {
-        weld_insert_kernel<double><<<g1, 256, 0, st>>>(reg, R, wb.table, wb.mask, mul, d_err);
-        weld_rep_kernel<double><<<g1, 256, 0, st>>>(reg, R, wb.table, wb.mask, mul, wb.rep, wb.flag);
+        weld_insert_kernel<double><<<g1, 256, 0, st>>>(reg, R, mode, N, W, wb.table, wb.mask, mul, d_err);
+        weld_rep_kernel<double><<<g1, 256, 0, st>>>(reg, R, mode, N, W, wb.table, wb.mask, mul, wb.rep, wb.flag);
     } else {
-        weld_insert_kernel<float><<<g1, 256, 0, st>>>(reg, R, wb.table, wb.mask, mul, d_err);
-        weld_rep_kernel<float><<<g1, 256, 0, st>>>(reg, R, wb.table, wb.mask, mul, wb.rep, wb.flag);
+        weld_insert_kernel<float><<<g1, 256, 0, st>>>(reg, R, mode, N, W, wb.table, wb.mask, mul, d_err);
+        weld_rep_kernel<float><<<g1, 256, 0, st>>>(reg, R, mode, N, W, wb.table, wb.mask, mul, wb.rep, wb.flag);
     }
     scan_exclusive(wb.flag, nslots, wb.vidx, wb.bsum, wb.counts + 0, st);
     if (f64)

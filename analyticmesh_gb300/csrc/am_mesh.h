@@ -22,7 +22,8 @@ struct WeldBuffers {
 };
 
 void scan_exclusive(const int *in, long long n, int *out, int *bsum, long long *d_total, cudaStream_t st);
-void launch_weld(int prec, const RegionsDev &reg, long long R, const WeldBuffers &wb, double scale,
-                 const double *center, int flip, int *d_err, cudaStream_t st);
+// mode 0: topological vertex key, 1: quantised coordinates (the reference's weld)
+void launch_weld(int prec, int mode, int N, int W, const RegionsDev &reg, long long R, const WeldBuffers &wb,
+                 double scale, const double *center, int flip, int *d_err, cudaStream_t st);
 
 } // namespace am

@@ -105,9 +105,13 @@ __device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long 
     return true;
 }
 
+// Rows are staged normalised (|w| = 1, zero rows become 0.x + sign(b) inf):
+// signed geometric distances are then plain dot products, the same quantity
+// the reference's feasibility test computes as (w.x + b) * rsqrt(|w|^2)
+// (kernel.h:729-795).  TC is the scan precision, TS the solve precision.
 template <typename TC, typename TS>
 __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
-                                                      int *err, int staged)
+                                                      int *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -116,18 +120,28 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
     const int ALL = net.ALL;
     const int N = net.N;
     const int W = net.W;
-    vec4_t<TC> *srows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)wib * net.ALLP;
-    const TS eps = (TS)tol.eps, same_eps = (TS)tol.same_eps, par_eps = (TS)tol.par_eps;
+    vec4_t<TC> *rows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)wib * net.ALLP;
+    const TC eps = (TC)tol.eps, par_eps = (TC)tol.par_eps;
+    const TS same_eps = (TS)tol.same_eps;
 
     for (long long rl = (long long)blockIdx.x * wpb + wib; rl < ch.count; rl += (long long)gridDim.x * wpb) {
         const long long rid = ch.head + rl;
         const vec4_t<TC> *grows = reinterpret_cast<const vec4_t<TC> *>((const TC *)ch.cons + (size_t)rl * net.ALLP * 4);
-        const vec4_t<TC> *rows = grows;
-        if (staged) {
-            for (int q = lane; q < ALL; q += 32) srows[q] = grows[q];
-            __syncwarp();
-            rows = srows;
+        for (int q = lane; q < ALL; q += 32) {
+            vec4_t<TC> v = grows[q];
+            const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
+            if (n2 > TC(0)) {
+                const TC inv = TC(1) / sqrt(n2);
+                v.x *= inv;
+                v.y *= inv;
+                v.z *= inv;
+                v.w *= inv;
+            } else {
+                v.w = v.w > TC(0) ? TC(INFINITY) : (v.w < TC(0) ? TC(-INFINITY) : TC(NAN));
+            }
+            rows[q] = v;
         }
+        __syncwarp();
         TS eqv[4];
         {
             const vec4_t<TC> e = ld4<TC>((const TC *)ch.eq + (size_t)rl * 4);
@@ -150,13 +164,13 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
             int top0 = -1, top1 = -1;
             unsigned long long pk = ~0ull;
             int pi = -1;
+            const TC pc[3] = {(TC)p[0], (TC)p[1], (TC)p[2]};
             for (int sel = 0; sel < ksel; ++sel) {
                 unsigned long long bk = 0ull;
                 int bi = 0x7fffffff;
                 for (int k = lane; k < ALL; k += 32) {
                     const vec4_t<TC> v = rows[k];
-                    const TC acc = v.x * (TC)p[0] + v.y * (TC)p[1] + v.z * (TC)p[2] + v.w;
-                    const TC d = acc * (TC(1) / sqrt(v.x * v.x + v.y * v.y + v.z * v.z));
+                    const TC d = v.x * pc[0] + v.y * pc[1] + v.z * pc[2] + v.w;
                     const unsigned long long key = order_key<TC>(d);
                     const bool below = key < pk || (key == pk && k > pi);
                     if (below && ahead(key, k, bk, bi)) {
@@ -193,14 +207,12 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                 row_of<TS, TC>(rows, ri, r0);
                 row_of<TS, TC>(rows, rj, r1);
                 solve3<TS>(r0, r1, eqv, v);
+                const TC vc[3] = {(TC)v[0], (TC)v[1], (TC)v[2]};
                 bool bad = false;
                 for (int k = lane; k < ALL; k += 32) {
                     if (k == ri || k == rj) continue;
-                    TS r[4];
-                    row_of<TS, TC>(rows, k, r);
-                    const TS ans = r[0] * v[0] + r[1] * v[1] + r[2] * v[2] + r[3];
-                    const TS rs = TS(1) / sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-                    if (ans * rs > eps) bad = true;
+                    const vec4_t<TC> r = rows[k];
+                    if (r.x * vc[0] + r.y * vc[1] + r.z * vc[2] + r.w > eps) bad = true;
                 }
                 if (!__any_sync(0xffffffffu, bad)) {
                     s = ri;
@@ -225,30 +237,32 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
             for (int step = 0; step < kWalkSteps; ++step) {
                 TS re[4];
                 row_of<TS, TC>(rows, e, re);
-                const TS d0 = eqv[1] * re[2] - eqv[2] * re[1];
-                const TS d1 = eqv[2] * re[0] - eqv[0] * re[2];
-                const TS d2 = eqv[0] * re[1] - eqv[1] * re[0];
-                const TS dn = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-                TS bt = TS(INFINITY);
+                const TC d0 = (TC)(eqv[1] * re[2] - eqv[2] * re[1]);
+                const TC d1 = (TC)(eqv[2] * re[0] - eqv[0] * re[2]);
+                const TC d2 = (TC)(eqv[0] * re[1] - eqv[1] * re[0]);
+                const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+                const TC c0 = (TC)cur[0], c1 = (TC)cur[1], c2 = (TC)cur[2];
+                // first hit along the edge line: min over crossing planes of
+                // t = max(0, -g) / a, compared as fractions
+                TC bnum = TC(1), bden = TC(0);
                 int bk = 0x7fffffff;
                 for (int k = lane; k < ALL; k += 32) {
-                    if (k == e || k == prev) continue;
-                    TS r[4];
-                    row_of<TS, TC>(rows, k, r);
-                    const TS a = r[0] * d0 + r[1] * d1 + r[2] * d2;
-                    const TS wn = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-                    if (!(a > par_eps * wn * dn)) continue; // parallel or receding
-                    const TS g = r[0] * cur[0] + r[1] * cur[1] + r[2] * cur[2] + r[3];
-                    TS t = -g / a;
-                    if (!(t > TS(0))) t = TS(0); // plane through (or behind) the current point
-                    if (t < bt || (t == bt && k < bk)) {
-                        bt = t;
+                    const vec4_t<TC> r = rows[k];
+                    const TC a = r.x * d0 + r.y * d1 + r.z * d2;
+                    if (!(a > thr) || k == e || k == prev) continue;
+                    TC num = -(r.x * c0 + r.y * c1 + r.z * c2 + r.w);
+                    num = num > TC(0) ? num : TC(0);
+                    const TC lhs = num * bden, rhs = bnum * a;
+                    if (lhs < rhs || (lhs == rhs && k < bk)) {
+                        bnum = num;
+                        bden = a;
                         bk = k;
                     }
                 }
+                TC bt = bk == 0x7fffffff ? TC(INFINITY) : bnum / bden;
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
-                    const TS ot = __shfl_xor_sync(0xffffffffu, bt, o);
+                    const TC ot = __shfl_xor_sync(0xffffffffu, bt, o);
                     const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
                     if (ot < bt || (ot == bt && ok < bk)) {
                         bt = ot;
@@ -368,10 +382,8 @@ void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const Ch
 {
     if (ch.count <= 0) return;
     const size_t row_bytes = (prec == kFloat64 ? sizeof(double4) : sizeof(float4)) * (size_t)net.ALLP;
-    int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96u * 1024u) / std::max<size_t>(row_bytes, 1)));
-    int staged = row_bytes <= 200u * 1024u ? 1 : 0;
-    if (!staged) wpb = 8;
-    const size_t smem = staged ? row_bytes * wpb : 0;
+    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96u * 1024u) / std::max<size_t>(row_bytes, 1)));
+    const size_t smem = row_bytes * wpb; // the host rejects networks whose rows do not fit (am_init)
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -380,15 +392,15 @@ void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const Ch
     if (prec == kFloat64) {
         auto k = polygon_kernel<double, double>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err, staged);
+        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err);
     } else if (prec == kMixed) {
         auto k = polygon_kernel<float, double>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err, staged);
+        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err);
     } else {
         auto k = polygon_kernel<float, float>;
         if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err, staged);
+        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err);
     }
 }
 

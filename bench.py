@@ -1,0 +1,372 @@
+"""Analytic Marching throughput on GB300: analytic faces / second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--form mixed|float32|float64] [--workload sphere|deep|large_skip|polytope]
+
+Workload (default): the sphere network 3 -> [128] x 4 -> 1 (geometric init,
+seed 1, fp32 weights) with 1024 dichotomy seed points (seed 1); synthetic,
+seeded.  One step = one complete Analytic Marching of that network (every
+region visited, every face polygon built), the window of the reference's
+am_time (backend/main.py:455-465): seed init and mesh export are outside.
+
+``value``: faces / second with inputs resident in HBM, CUDA-event timed on
+the launching stream, L2 flushed (256 MiB write) before every timed step.
+``e2e``: the same through the C ABI with host buffers -- the weights, biases,
+seed states and points are copied host -> device inside the step and the
+welded mesh is read back (am_combine_mesh + am_get_mesh).
+
+``--impl reference`` times the reference's own marching loop compiled for the
+host cores (oracle/_ref, all host threads) on a bounded sample of the same
+workload (the first 65536 regions).  Under torchrun every rank runs an
+independent replica (the path does not shard); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+REF_SAMPLE_REGIONS = 65536
+FLOPS_PER_REGION = {}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--form", default="mixed", choices=["mixed", "float32", "float64"])
+    p.add_argument("--workload", default="sphere", choices=["sphere", "deep", "large_skip", "polytope"])
+    p.add_argument("--seeds", type=int, default=1024)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile", action="store_true",
+                   help="warm-up + timed steps only (for ncu launch lists): no e2e, phase, plain or CPU legs")
+    return p.parse_args()
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+
+        if args.impl == "ours":
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def composition_flops(nodes, arc_table, tms):
+    """Algorithmic FLOPs of one region's composition: 4 columns x 2 flop per
+    multiply-add over every layer product and transformed skip."""
+    macs = sum(nodes[i] * nodes[i + 1] for i in range(1, len(nodes) - 1))
+    for row in arc_table:
+        for c in range(int(row[0])):
+            src, t = int(row[1 + 2 * c]), int(row[2 + 2 * c])
+            if tms[t].size and src >= 1:
+                macs += tms[t].shape[0] * tms[t].shape[1]
+    return 8 * macs
+
+
+def workload(name, nseeds):
+    from analyticmesh_gb300 import workloads as wl
+
+    model = {"sphere": wl.sphere, "deep": wl.deep, "large_skip": wl.large_skip, "polytope": wl.polytope}[name]()
+    net = wl.net_arrays(model)
+    states, points = wl.seeds_for(model, init_num=nseeds, seed=1)
+    desc = {"sphere": "sphere MLP 3-[128]x4-1, seed 1", "deep": "perturbed MLP 3-[256]x6-1, seed 2",
+            "large_skip": "skip MLP 3-[512]x8-1 (input into layer 4), seed 3",
+            "polytope": "polytope MLP 3-14-1, seed 0"}[name]
+    return net, states, points, desc
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+            os.unlink(self.path)
+        except Exception:
+            return out
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() in ("active", "1"):
+                        reasons.add(nm)
+            except Exception:
+                pass
+        if sm:
+            out.update(sm_mhz=statistics.median(sm), sm_max_mhz=mx, reasons=sorted(reasons), samples=len(sm))
+        return out
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p["bf16_tflops"]), "measured"
+    except Exception:
+        return 6800.0, 1900.0, "fallback"
+
+
+def run_reference(args, rank, ws):
+    """--impl reference: the reference's own loop on the host cores."""
+    if rank != 0:
+        return
+    net, states, points, desc = workload(args.workload, args.seeds)
+    from oracle import build_ref
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    try:
+        if not O.ref_available():
+            build_ref.build_ref()
+        kind = "reference" if O.ref_available() else "port"
+    except Exception:
+        kind = "port"
+    dtype = "float64" if args.form == "float64" else "float32"
+    rates = []
+    steps_done = 0
+    for i in range(args.warmup + args.steps):
+        tm = {}
+        if kind == "reference":
+            r = O.run_ref(net, states, points, dtype=dtype, threads=threads, region_budget=REF_SAMPLE_REGIONS, timing=tm)
+            secs = tm["am_seconds"]
+        else:
+            t0 = time.perf_counter()
+            r = O.run_oracle(net, states, points, dtype=dtype)
+            secs = time.perf_counter() - t0
+        faces = int((r.nverts >= 3).sum())
+        if i >= args.warmup:
+            rates.append(faces / secs)
+            steps_done += 1
+    value = statistics.mean(rates)
+    line = {
+        "impl": "reference", "metric": "analytic_faces_per_sec", "value": value, "unit": "faces/s",
+        "n_gpus": args.gpus, "steps": steps_done, "warmup": args.warmup, "ms_per_step": 1e3 * faces / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dtype == "float32" else "f64",
+        "data": "synthetic (seeded network and dichotomy seeds)",
+        "config": {"workload": desc, "seeds": args.seeds, "sample": "first %d regions per step" % REF_SAMPLE_REGIONS},
+        "cpu_baseline": {"value": value, "unit": "faces/s", "cores": threads, "kind": kind,
+                         "sample": "first %d regions of the workload per step, reference loop built for the host "
+                                   "(OpenMP, %d threads)" % (REF_SAMPLE_REGIONS, threads)},
+        "e2e": {"value": value, "unit": "faces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline(net, states, points, dtype):
+    from oracle import build_ref
+    from oracle import oracle as O
+
+    threads = os.cpu_count() or 1
+    try:
+        if not O.ref_available():
+            build_ref.build_ref()
+        tm = {}
+        r = O.run_ref(net, states, points, dtype=dtype, threads=threads, region_budget=REF_SAMPLE_REGIONS, timing=tm)
+        return {"value": float((r.nverts >= 3).sum()) / tm["am_seconds"], "unit": "faces/s", "cores": threads,
+                "kind": "reference", "sample": "first %d regions of the workload (reference loop built for the host, "
+                                                "OpenMP %d threads)" % (REF_SAMPLE_REGIONS, threads)}
+    except Exception as exc:
+        t0 = time.perf_counter()
+        r = O.run_oracle(net, states, points, dtype=dtype)
+        secs = time.perf_counter() - t0
+        return {"value": float((r.nverts >= 3).sum()) / secs, "unit": "faces/s", "cores": threads, "kind": "port",
+                "sample": "full workload, oracle restatement (%s)" % type(exc).__name__}
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, ws)
+        return
+    import numpy as np
+    import torch
+
+    from analyticmesh_gb300 import _lib, engine
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    net, states, points, desc = workload(args.workload, args.seeds)
+    form = args.form
+    ft = np.float64 if form == "float64" else np.float32
+    tt = torch.float64 if form == "float64" else torch.float32
+    # inputs resident in HBM
+    W = [torch.tensor(w, dtype=tt, device=dev) for w in net.W]
+    B = [torch.tensor(b, dtype=tt, device=dev) for b in net.b]
+    TM = [torch.tensor(t, dtype=tt, device=dev) for t in net.tms]
+    S = torch.tensor(states, dtype=torch.uint8, device=dev)
+    P = torch.tensor(points, dtype=tt, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    eng = engine.Engine(form, net.nodes, net.arc_table, net.num_extra)
+
+    def step():
+        return eng.run(W, B, S, P, TM, None, None, 0.0, False, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    times, faces, launches = [], [], 0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            s = step()
+            ev1.record(stream)
+            ev1.synchronize()
+            times.append(ev0.elapsed_time(ev1) / 1e3)
+            faces.append(s["num_faces"])
+            launches += s["kernel_launches"] + 1
+    torch.cuda.synchronize()
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"metric": "analytic_faces_per_sec", "value": sum(faces) / sum(times), "unit": "faces/s",
+                              "profile": True, "steps": args.steps, "launches": launches}), flush=True)
+        eng.close()
+        return
+    total = sum(times)
+    if ws > 1:
+        t = torch.tensor([total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total = float(t.item())
+        torch.distributed.barrier()
+    value = ws * sum(faces) / total
+    clocks = clk.summary()
+
+    # end to end through the C ABI with host buffers
+    e2e_rates, h2d, d2h = [], 0, 0
+    for i in range(max(2, args.steps // 2) + 1):
+        t0 = time.perf_counter()
+        s = eng.run(net.W, net.b, states.astype(np.uint8), points, net.tms, None, None, 0.0, False)
+        mesh = eng.combine()
+        dt = time.perf_counter() - t0
+        if i > 0:
+            e2e_rates.append(s["num_faces"] / dt)
+        h2d = sum(np.asarray(x, ft).nbytes for x in net.W + net.b + net.tms) + states.size + points.astype(ft).nbytes
+        d2h = mesh.verts.nbytes + mesh.face_sizes.nbytes + mesh.face_indices.nbytes
+    e2e = statistics.mean(e2e_rates) * ws
+
+    # per-phase breakdown and the dominant kernel's roofline (separate, untimed run)
+    eng.set_option(_lib.AM_OPT_PHASE_TIMING, 1)
+    sp = step()
+    eng.set_option(_lib.AM_OPT_PHASE_TIMING, 0)
+    phases = {"compose_ms": sp["compose_ms"], "polygon_ms": sp["polygon_ms"], "frontier_ms": sp["frontier_ms"]}
+    hbm, tflops, peak_kind = measured_peaks()
+    regions = sp["num_regions"]
+    ALL = int(sum(net.nodes[1:-1])) + net.num_extra
+    flops = composition_flops(net.nodes, net.arc_table, net.tms) * regions
+    elem = 8 if form == "float64" else 4
+    poly_bytes = regions * (ALL * 4 * elem + 4 * elem + 12 * 6)
+    if phases["compose_ms"] >= phases["polygon_ms"]:
+        ach = flops / (phases["compose_ms"] / 1e3) / 1e12
+        roof = {"kernel": "compose", "bound": "tensor", "achieved": ach, "peak": tflops, "unit": "TFLOP/s",
+                "frac": ach / tflops, "traffic": None, "peak_kind": peak_kind,
+                "algorithmic": "%d FLOP/region x %d regions" % (flops // max(regions, 1), regions)}
+    else:
+        ach = poly_bytes / (phases["polygon_ms"] / 1e3) / 1e9
+        roof = {"kernel": "polygon", "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "traffic": None, "peak_kind": peak_kind,
+                "algorithmic": "%d B/region x %d regions" % (poly_bytes // max(regions, 1), regions)}
+
+    plain = None
+    if form != "float32":
+        ep = engine.Engine("float32", net.nodes, net.arc_table, net.num_extra)
+        W32 = [w.float() for w in W]
+        B32 = [b.float() for b in B]
+        T32 = [t.float() for t in TM]
+        P32 = P.float()
+        for _ in range(2):
+            ep.run(W32, B32, S, P32, T32, None, None, 0.0, False, stream=stream)
+        pt = []
+        for _ in range(max(3, args.steps // 2)):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s2 = ep.run(W32, B32, S, P32, T32, None, None, 0.0, False, stream=stream)
+            e1.record(stream)
+            e1.synchronize()
+            pt.append(s2["num_faces"] / (e0.elapsed_time(e1) / 1e3))
+        plain = statistics.mean(pt) * ws
+        ep.close()
+
+    if rank != 0:
+        return
+    cpu = None
+    if ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(net, states, points, "float64" if form == "float64" else "float32")
+    line = {
+        "metric": "analytic_faces_per_sec", "value": value, "unit": "faces/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"float32": "f32", "float64": "f64", "mixed": "f32 (bf16x3 composition, f64 solves)"}[form],
+        "data": "synthetic (seeded network weights and dichotomy seed points)",
+        "config": {"workload": desc, "seeds": args.seeds, "form": form, "faces_per_step": faces[-1],
+                   "regions_per_step": regions, "l2": "256 MiB flush before every timed step",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": "faces/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": roof, "phases_ms": phases, "plain_fp32_value": plain,
+        "chosen_vs_plain": (value / plain) if plain else None, "cpu_baseline": cpu, "clocks": clocks,
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -76,6 +76,9 @@ def _rewrite(name: str, text: str) -> str:
         old = "inferAndAppend(states_buffer, batch_size, var);"
         assert old in text
         text = text.replace(old, "amref_record(var, states_buffer, faces_buffer, batch_size);\n        " + old)
+        old = "var.polymesh.append_verts(var.vertices_buffer, batch_size);"
+        assert old in text
+        text = text.replace(old, old + "\n        amref_after_batch(var);")
     assert "<<<" not in re.sub(r"//[^\n]*", "", text), "unconverted launch in %s" % name
     return text
 

@@ -110,3 +110,45 @@ def canonical(a_regions, b_regions, tol=1e-5):
     return dict(regions_a=len(ka), regions_b=len(kb), only_a=len(ka - kb), only_b=len(kb - ka),
                 faces_a=len(pa), faces_b=len(pb), faces_only_a=len(set(pa) - set(pb)),
                 faces_only_b=len(set(pb) - set(pa)), faces_mismatch=bad, max_vertex_diff=worst)
+
+
+def clean_walks(r):
+    """Mask of oracle / reference records whose walk closed without a
+    rejected pivot or merge (tab = [s, ..., s], no negative entries)."""
+    ok = np.zeros(r.num, bool)
+    for i in range(r.num):
+        nt = int(r.ntab[i])
+        t = r.tab[i, :nt]
+        ok[i] = nt >= 4 and t[0] == t[nt - 1] and (t >= 0).all()
+    return ok
+
+
+def parity_report(a, b, tol=1e-5):
+    """Order-free comparison split into combinatorial and numeric parts.
+
+    regions_only_a / _b: activation states visited by one side only;
+    faces_count_mismatch: common regions whose polygons have different
+    vertex counts (combinatorial disagreement); faces_beyond_tol: same
+    count but some vertex further than tol after the best rotation /
+    orientation; max_diff over all common faces of equal size."""
+    ka = {x.tobytes() for x in a.bits}
+    kb = {x.tobytes() for x in b.bits}
+    pa = Polygons.from_regions(a, min_verts=1).faces
+    pb = Polygons.from_regions(b, min_verts=1).faces
+    common = set(pa) & set(pb)
+    count_mm = beyond = 0
+    worst = 0.0
+    for k in common:
+        if pa[k].shape != pb[k].shape:
+            count_mm += 1
+            continue
+        d = cycle_distance(pa[k], pb[k])
+        if not np.isfinite(d) or d > tol:
+            beyond += 1
+        if np.isfinite(d):
+            worst = max(worst, d)
+    fa = sum(1 for k in pa if pa[k].shape[0] >= 3)
+    fb = sum(1 for k in pb if pb[k].shape[0] >= 3)
+    return dict(regions_a=len(ka), regions_b=len(kb), regions_only_a=len(ka - kb), regions_only_b=len(kb - ka),
+                faces_a=fa, faces_b=fb, common_polygons=len(common), faces_count_mismatch=count_mm,
+                faces_beyond_tol=beyond, max_diff=worst)

@@ -96,6 +96,8 @@ def ref_lib():
         lib.amref_get_regions.argtypes = [C.c_void_p] * 7
         lib.amref_get_mesh.argtypes = [C.c_void_p, C.c_void_p]
         lib.amref_export.argtypes = [C.c_char_p, C.c_int, C.c_int]
+        lib.amref_last_seconds.restype = C.c_double
+        lib.amref_set_region_budget.argtypes = [C.c_long]
         _REF = lib
     return _REF
 
@@ -182,14 +184,18 @@ def _read_mesh(nv, nf, getter):
     return Mesh(verts=v[:nv].copy(), faces=faces)
 
 
-def run_ref(net, states, points, iso=0.0, flip=False, dtype="float32", combine=None, export=None, threads=1):
+def run_ref(net, states, points, iso=0.0, flip=False, dtype="float32", combine=None, export=None, threads=1,
+            region_budget=0, timing=None):
     """Run the reference's own loop on the CPU.  ``threads=1`` executes every
     launch in thread-index order (deterministic, the parity setting);
-    ``export=(path, poly, f32)`` writes its PLY after combining."""
+    ``export=(path, poly, f32)`` writes its PLY after combining;
+    ``region_budget`` stops the loop after that many regions (timed samples);
+    ``timing`` (a dict) receives the wall time of the marching call."""
     lib = ref_lib()
     if lib is None:
         raise RuntimeError("reference CPU build unavailable")
     lib.amref_set_threads(int(threads))
+    lib.amref_set_region_budget(int(region_budget))
     p = _Packed(net, dtype)
     st, pt = _inputs(states, points, p.npt)
     rc = lib.amref_run(1 if dtype == "float64" else 0, len(net.nodes) - 1, p.nodes.ctypes.data_as(C.c_void_p), p.Wp,
@@ -199,6 +205,8 @@ def run_ref(net, states, points, iso=0.0, flip=False, dtype="float32", combine=N
                        st.shape[0], C.c_double(iso), 1 if flip else 0)
     if rc != 0:
         raise RuntimeError("reference run failed: %d" % rc)
+    if timing is not None:
+        timing["am_seconds"] = lib.amref_last_seconds()
     R = lib.amref_num_regions()
     N = lib.amref_state_len()
     d = _alloc_regions(R, N)

@@ -11,6 +11,7 @@
  */
 #include "am_ref_shim.h"
 
+#include <chrono>
 #include <omp.h>
 
 #include "kernel.cu"
@@ -26,6 +27,7 @@ struct HostNet {
 };
 HostNet g_net;
 int g_is_f64 = 0;
+double g_am_seconds = 0.0;
 
 torch::Tensor view(const void *p, int64_t d0, int64_t d1, int ndim, at::ScalarType st)
 {
@@ -79,9 +81,16 @@ int amref_run(int is_f64, int n_lin, const int *nodes, const void *const *W, con
     torch::Tensor pt = view(points, S, 3, 2, ft);
     torch::Tensor we = view(w_extra, E, 3, 2, ft);
     torch::Tensor be = view(b_extra, E, 0, 1, ft);
+    const auto t0 = std::chrono::steady_clock::now();
     AnalyticMarching_cuda(ws, bs, st, pt, tms, we, be, iso, flip != 0);
+    g_am_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return 0;
 }
+
+/* wall time of the last AnalyticMarching_cuda call (the reference's am_time window) */
+double amref_last_seconds(void) { return g_am_seconds; }
+/* stop after this many regions (0 = no bound) */
+void amref_set_region_budget(long n) { g_amref_region_budget = n; }
 
 int amref_num_regions(void) { return (int)g_amref_rec.nverts.size(); }
 int amref_state_len(void) { return g_amref_rec.N; }

@@ -350,6 +350,9 @@ struct amref_records {
     }
 };
 static amref_records g_amref_rec;
+/* Optional bound on the regions the loop processes (timed samples): once
+ * reached, the stack is emptied after the current batch. */
+static long g_amref_region_budget = 0;
 
 template <class V, class T, class FD>
 inline void amref_record(V &var, const T *states_buffer, const FD *faces, int batch)
@@ -374,6 +377,13 @@ inline void amref_record(V &var, const T *states_buffer, const FD *faces, int ba
         for (int q = 0; q < 3; ++q) r.mid.push_back((double)faces[b].midpoint[q]);
         r.start.push_back(faces[b].start_idx);
     }
+}
+
+/* end of a batch (after cuam_kernel.cu:96): apply the region budget */
+template <class V>
+inline void amref_after_batch(V &var)
+{
+    if (g_amref_region_budget > 0 && (long)g_amref_rec.nverts.size() >= g_amref_region_budget) var.states.states_num = 0;
 }
 
 #endif
