@@ -18,6 +18,7 @@
 #include "../../include/analyticmesh_gb300.h"
 #include "am_internal.h"
 #include "am_mesh.h"
+#include "am_tc.h"
 
 using namespace am;
 
@@ -133,6 +134,9 @@ struct am_engine {
     // network
     DevBuf wt[kMaxLayers], bias[kMaxLayers], w0, tmt[64], wext, bext, scratch;
     NetDev net{};
+    // tensor-core composition (mixed form): bf16 hi/lo weights
+    DevBuf tc_lin[kMaxLayers], tc_skip[kMaxLayers][kMaxSkips];
+    TcNet tcnet{};
     // regions
     DevBuf keys, hash, mid, start, nv, status, verts, edges;
     long long cap = 0;
@@ -472,6 +476,44 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
         }
         net.w_extra = e->wext.p;
         net.b_extra = e->bext.p;
+        if (prec == kMixed) {
+            // bf16 hi/lo splits, padded to 128-row x 64-column blocks
+            TcNet &tc = e->tcnet;
+            memset(&tc, 0, sizeof(tc));
+            int mtiles_max = 1;
+            auto split = [&](DevBuf &buf, const void *src_fp32, int M, int K, TcMat &m) {
+                const int Mp = (M + 127) / 128 * 128, Kp = (K + 63) / 64 * 64;
+                upload(e->scratch, src_fp32, sizeof(float) * (size_t)M * K, st);
+                AM_CUDA(buf.alloc(2 * sizeof(uint16_t) * (size_t)Mp * Kp));
+                uint16_t *hi = buf.as<uint16_t>(), *lo = hi + (size_t)Mp * Kp;
+                launch_split_weights(e->scratch.as<float>(), M, K, Mp, Kp, hi, lo, st);
+                AM_CUDA(cudaStreamSynchronize(st));
+                m.hi = (const __nv_bfloat16 *)hi;
+                m.lo = (const __nv_bfloat16 *)lo;
+                m.Mp = Mp;
+                m.Kp = Kp;
+                tc.kp_max = std::max(tc.kp_max, Kp);
+                mtiles_max = std::max(mtiles_max, Mp / 128);
+            };
+            for (int i = 1; i <= e->n_lin - 2; ++i) {
+                split(e->tc_lin[i], weights[i], e->nodes[i + 1], e->nodes[i], tc.lin[i]);
+                const int *row = e->arc.data() + (size_t)(i - 1) * e->arc_cols;
+                for (int c = 0; c < row[0]; ++c) {
+                    const int from = row[1 + 2 * c], t = row[2 + 2 * c];
+                    const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
+                    if ((h || w) && from >= 1) split(e->tc_skip[i][c], arc_tm[t], h, w, tc.skip[i][c]);
+                }
+            }
+            tc.kp_max = std::max(tc.kp_max, 64);
+            int ncols = std::min(256, std::min(32768 / tc.kp_max, 512 / mtiles_max));
+            ncols = ncols / 16 * 16;
+            AM_CHECK(ncols >= 16, "layer widths too large for the tensor-core composition tile");
+            tc.ncols = ncols;
+            int tcols = 32;
+            while (tcols < mtiles_max * ncols) tcols <<= 1;
+            tc.tmem_cols = tcols;
+            AM_CHECK(tc_smem_bytes(tc) <= 227u * 1024u, "tensor-core composition tile exceeds shared memory");
+        }
         AM_CUDA(cudaGetLastError());
 
         // ---------------------------------------------------------- seeds
@@ -547,7 +589,10 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             const HashDev hs = e->hashdev();
             float ms = 0;
             if (e->phase_timing) AM_CUDA(cudaEventRecord(pa, st));
-            launch_compose(prec == kMixed ? kFloat32 : prec, net, reg, ch, iso, st);
+            if (prec == kMixed)
+                launch_compose_tc(net, e->tcnet, reg, ch, iso, e->d_err.as<int>(), st);
+            else
+                launch_compose(prec, net, reg, ch, iso, st);
             if (e->phase_timing) {
                 AM_CUDA(cudaEventRecord(pb, st));
                 AM_CUDA(cudaEventSynchronize(pb));

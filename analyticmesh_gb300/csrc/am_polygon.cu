@@ -203,10 +203,16 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                 get_i_j(x, ALL, i, j);
                 const int ri = i < 32 ? __shfl_sync(0xffffffffu, top0, i) : __shfl_sync(0xffffffffu, top1, i - 32);
                 const int rj = j < 32 ? __shfl_sync(0xffffffffu, top0, j) : __shfl_sync(0xffffffffu, top1, j - 32);
-                TS r0[4], r1[4], v[3];
-                row_of<TS, TC>(rows, ri, r0);
-                row_of<TS, TC>(rows, rj, r1);
-                solve3<TS>(r0, r1, eqv, v);
+                TS v[3] = {TS(0), TS(0), TS(0)};
+                if (lane == 0) { // one lane solves, the warp shares the vertex
+                    TS r0[4], r1[4];
+                    row_of<TS, TC>(rows, ri, r0);
+                    row_of<TS, TC>(rows, rj, r1);
+                    solve3<TS>(r0, r1, eqv, v);
+                }
+                v[0] = __shfl_sync(0xffffffffu, v[0], 0);
+                v[1] = __shfl_sync(0xffffffffu, v[1], 0);
+                v[2] = __shfl_sync(0xffffffffu, v[2], 0);
                 const TC vc[3] = {(TC)v[0], (TC)v[1], (TC)v[2]};
                 bool bad = false;
                 for (int k = lane; k < ALL; k += 32) {
@@ -235,11 +241,12 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
             int e = s, prev = -1;
             TS cur[3] = {p[0], p[1], p[2]};
             for (int step = 0; step < kWalkSteps; ++step) {
-                TS re[4];
-                row_of<TS, TC>(rows, e, re);
-                const TC d0 = (TC)(eqv[1] * re[2] - eqv[2] * re[1]);
-                const TC d1 = (TC)(eqv[2] * re[0] - eqv[0] * re[2]);
-                const TC d2 = (TC)(eqv[0] * re[1] - eqv[1] * re[0]);
+                // direction of the edge line: w_eq x w_e (counter-clockwise about w_eq)
+                const vec4_t<TC> ref_ = rows[e];
+                const TC eq0 = (TC)eqv[0], eq1 = (TC)eqv[1], eq2 = (TC)eqv[2];
+                const TC d0 = eq1 * ref_.z - eq2 * ref_.y;
+                const TC d1 = eq2 * ref_.x - eq0 * ref_.z;
+                const TC d2 = eq0 * ref_.y - eq1 * ref_.x;
                 const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
                 const TC c0 = (TC)cur[0], c1 = (TC)cur[1], c2 = (TC)cur[2];
                 // first hit along the edge line: min over crossing planes of
@@ -273,9 +280,16 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                     status = kOpen;
                     break;
                 }
-                TS rk[4], V[3];
-                row_of<TS, TC>(rows, bk, rk);
-                solve3<TS>(re, rk, eqv, V);
+                TS V[3] = {TS(0), TS(0), TS(0)};
+                if (lane == 0) { // vertex = 3x3 solve of (edge plane, hit plane, face plane)
+                    TS re[4], rk[4];
+                    row_of<TS, TC>(rows, e, re);
+                    row_of<TS, TC>(rows, bk, rk);
+                    solve3<TS>(re, rk, eqv, V);
+                }
+                V[0] = __shfl_sync(0xffffffffu, V[0], 0);
+                V[1] = __shfl_sync(0xffffffffu, V[1], 0);
+                V[2] = __shfl_sync(0xffffffffu, V[2], 0);
                 if (!(isfinite(V[0]) && isfinite(V[1]) && isfinite(V[2]))) {
                     status = kSingular;
                     break;

@@ -117,6 +117,12 @@ typedef enum {
 } am_option;
 int am_set_option(am_engine *engine, int option, int64_t value);
 
+/* ---- self-test of the tensor-core tile used by the mixed-precision
+ * composition (no counterpart in the reference): D (128 x N, fp32) =
+ * A (128 x K, bf16, row-major) . B (N x K, bf16, row-major)^T on one CTA,
+ * 16 <= N <= 256, N % 16 == 0, K % 64 == 0; device pointers. */
+int am_selftest_umma(const void *A, const void *B, void *D, int N, int K);
+
 #ifdef __cplusplus
 }
 #endif

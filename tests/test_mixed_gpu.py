@@ -1,0 +1,64 @@
+"""The mixed-precision form (tensor-core bf16x3 composition, FP64 vertex
+solves) against the FP64 oracle: same regions as the oracle's own fp32 run
+gets (up to near-degenerate ones), every vertex on the zero level set."""
+import numpy as np
+import pytest
+
+from analyticmesh_gb300 import engine, workloads as wl
+from oracle import compare as CM
+from oracle import oracle as O
+
+from test_engine_gpu import f_at
+
+pytestmark = pytest.mark.gpu
+
+NETS = {
+    "plain48x3": (lambda: wl.geometric([48, 48, 48], 12, perturb=0.05), 256),
+    "odd_widths": (lambda: wl.geometric([20, 50, 20, 80, 20], 13, skips=[[0], [1, 1, 0], [1, 1, 1], [0]],
+                                        tm_shapes=[[0, 0], [80, 20]]), 256),
+    "skips24x4": (lambda: wl.geometric([24, 24, 24, 24], 9, skips=[[0], [1, 1, 0], [1, 0, 1], [0]],
+                                       tm_shapes=[[0, 0], [24, 3]]), 256),
+    "wide256x3": (lambda: wl.geometric([256, 256, 256], 14, perturb=0.02), 256),
+    "input_skip": (lambda: wl.geometric([64] * 5, 15, perturb=0.01, skips=[[0], [0], [1, 0, 0], [0]],
+                                        tm_shapes=[[64, 3]]), 256),
+}
+
+
+@pytest.mark.parametrize("name", list(NETS))
+def test_mixed_against_fp64_oracle(name):
+    factory, nseed = NETS[name]
+    m = factory()
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=nseed, seed=7)
+    eng = engine.march(net, st, pt, "mixed")
+    reg = eng.regions()
+    o64 = O.run_oracle(net, st, pt, dtype="float64")
+    o32 = O.run_oracle(net, st, pt, dtype="float32")
+    ce = CM.parity_report(reg, o64, tol=1e-5)
+    co = CM.parity_report(o32, o64, tol=1e-5)
+    d_mixed = ce["regions_only_a"] + ce["regions_only_b"]
+    d_fp32 = co["regions_only_a"] + co["regions_only_b"]
+    assert d_mixed <= 2 * d_fp32 + max(2, ce["regions_b"] // 5000), (ce, co)
+    assert ce["faces_count_mismatch"] <= 2 * co["faces_count_mismatch"] + max(2, ce["faces_b"] // 2000), (ce, co)
+    v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in range(reg.num) if reg.nverts[i] >= 3])
+    assert np.abs(f_at(net, v)).max() <= 1e-5
+    eng.close()
+
+
+def test_mixed_sphere_config():
+    """Config 2: the mixed form's region set against the FP64 oracle is as
+    close as the plain fp32 form's, and max |f(v)| <= 1e-5."""
+    m = wl.sphere()
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=1024, seed=1)
+    em = engine.march(net, st, pt, "mixed")
+    ep = engine.march(net, st, pt, "float32")
+    o64 = O.run_oracle(net, st, pt, dtype="float64")
+    cm = CM.parity_report(em.regions(), o64, tol=1e-5)
+    cp = CM.parity_report(ep.regions(), o64, tol=1e-5)
+    assert cm["regions_only_a"] + cm["regions_only_b"] <= cp["regions_only_a"] + cp["regions_only_b"] + 10, (cm, cp)
+    reg = em.regions()
+    v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in range(reg.num) if reg.nverts[i] >= 3])
+    assert np.abs(f_at(net, v)).max() <= 1e-5
+    em.close()
+    ep.close()
