@@ -7,11 +7,14 @@
 // (4 columns each, N = 4 x regions <= 256) and keeps the masked operand
 // X_l = diag(s_l) A_l on chip the whole way through the network: as bf16
 // hi/lo splits in 128B-swizzled K-major shared memory, the B operand of
-// tcgen05.mma.  The layer weights, pre-split into bf16 hi/lo and padded to
-// 128-row x 64-column blocks, are the A operand, staged block by block.  Each
-// block issues three products accumulating in fp32 in TMEM
-// (W_hi X_hi + W_hi X_lo + W_lo X_hi: the bf16x3 split product, relative
-// error ~2^-17 per product).  The epilogue reads the accumulators with
+// tcgen05.mma.  The layer weights, pre-split the same way and padded to
+// 128-row x 64-column blocks, are the A operand, staged block by block.
+// Every operand is split into three bf16 terms, x = hi + mid + lo (24
+// significant bits, as fp32); a block issues the six products whose weight is
+// at least 2^-16 -- hh, hm, mh, hl, lh, mm -- accumulating in fp32 in TMEM.
+// A two-term split leaves ~2^-17 of every operand unrepresented, which moved
+// vertices by ~1.5e-5 and changed near-degenerate walk decisions; the
+// three-term split gives fp32-level constraint rows.  The epilogue reads the accumulators with
 // tcgen05.ld (one TMEM lane per output unit), adds bias and skips, writes the
 // sign-flipped constraint rows to HBM for the polygon kernel, and writes the
 // next layer's masked operand straight back into shared memory.  The face
@@ -32,17 +35,21 @@ namespace {
 constexpr int kThreads = 128;
 constexpr int kWaitIters = 1 << 22;
 
-__device__ __forceinline__ void put_split(uint8_t *xs_hi, uint8_t *xs_lo, int n, int k, int ncols, float v)
+// x = hi + mid + lo in bf16; the operand buffers are `xbytes` apart
+__device__ __forceinline__ void put_split(uint8_t *xs, size_t xbytes, int n, int k, int ncols, float v)
 {
     const __nv_bfloat16 h = __float2bfloat16_rn(v);
-    const __nv_bfloat16 l = __float2bfloat16_rn(v - __bfloat162float(h));
+    const float r1 = v - __bfloat162float(h);
+    const __nv_bfloat16 m = __float2bfloat16_rn(r1);
+    const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
     const uint32_t off = umma::sw128_offset(n, k, ncols);
-    *reinterpret_cast<__nv_bfloat16 *>(xs_hi + off) = h;
-    *reinterpret_cast<__nv_bfloat16 *>(xs_lo + off) = l;
+    *reinterpret_cast<__nv_bfloat16 *>(xs + off) = h;
+    *reinterpret_cast<__nv_bfloat16 *>(xs + xbytes + off) = m;
+    *reinterpret_cast<__nv_bfloat16 *>(xs + 2 * xbytes + off) = l;
 }
 
 // X[n = 4r + c][k] = s_k(r) ? -C[r][src + k][c] : 0 for k < K, 0 up to Kp
-__device__ void stage_x_from_rows(uint8_t *xs_hi, uint8_t *xs_lo, int ncols, const float *cons, size_t rstride,
+__device__ void stage_x_from_rows(uint8_t *xs, size_t xbytes, int ncols, const float *cons, size_t rstride,
                                   const uint32_t *keys, int W, int nreg, int src, int K, int Kp)
 {
     const int R = ncols / 4;
@@ -60,22 +67,21 @@ __device__ void stage_x_from_rows(uint8_t *xs_hi, uint8_t *xs_lo, int ncols, con
             }
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) put_split(xs_hi, xs_lo, 4 * r + c, k, ncols, x[c]);
+        for (int c = 0; c < 4; ++c) put_split(xs, xbytes, 4 * r + c, k, ncols, x[c]);
     }
 }
 
-// one 128-row x 64-column block of a pre-split weight into the stage buffer
-__device__ void stage_w_block(uint8_t *ws_hi, uint8_t *ws_lo, const TcMat &m, int mt, int kb)
+// one 128-row x 64-column block of a pre-split weight (three terms) into the
+// stage buffers (16 KB apart)
+__device__ void stage_w_block(uint8_t *ws, const TcMat &m, int mt, int kb)
 {
-    const __nv_bfloat16 *hi = m.hi + (size_t)(mt * 128) * m.Kp + (size_t)kb * 64;
-    const __nv_bfloat16 *lo = m.lo + (size_t)(mt * 128) * m.Kp + (size_t)kb * 64;
-    for (int q = threadIdx.x; q < 128 * 8; q += kThreads) {
-        const int row = q >> 3, ch = q & 7;
-        const uint4 vh = *reinterpret_cast<const uint4 *>(hi + (size_t)row * m.Kp + ch * 8);
-        const uint4 vl = *reinterpret_cast<const uint4 *>(lo + (size_t)row * m.Kp + ch * 8);
-        const uint32_t off = (uint32_t)(row * 128 + (((ch ^ (row & 7)) & 7) << 4));
-        *reinterpret_cast<uint4 *>(ws_hi + off) = vh;
-        *reinterpret_cast<uint4 *>(ws_lo + off) = vl;
+    const size_t plane = (size_t)m.Mp * m.Kp;
+    const __nv_bfloat16 *src = m.hi + (size_t)(mt * 128) * m.Kp + (size_t)kb * 64;
+    for (int q = threadIdx.x; q < 3 * 128 * 8; q += kThreads) {
+        const int t = q / (128 * 8), rq = q % (128 * 8);
+        const int row = rq >> 3, ch = rq & 7;
+        const uint4 v = *reinterpret_cast<const uint4 *>(src + t * plane + (size_t)row * m.Kp + ch * 8);
+        *reinterpret_cast<uint4 *>(ws + t * 16384 + row * 128 + (((ch ^ (row & 7)) & 7) << 4)) = v;
     }
 }
 
@@ -85,30 +91,34 @@ struct Pipe {
     int *err;
 };
 
-// D[mt] (+)= M_mat . X over all K blocks of the operand in shared memory
-__device__ void gemm_accumulate(const TcMat &m, int mtiles, uint8_t *ws_hi, uint8_t *ws_lo, uint8_t *xs_hi,
-                                uint8_t *xs_lo, int ncols, uint32_t tmem, bool first, Pipe &pp)
+// D[mt] (+)= M . X over all K blocks of the operand in shared memory: six
+// products per K step (terms t, u of weight 2^-8(t+u), t + u <= 2)
+__device__ void gemm_accumulate(const TcMat &m, int mtiles, uint8_t *ws, uint8_t *xs, size_t xbytes, int ncols,
+                                uint32_t tmem, bool first, Pipe &pp)
 {
     const uint32_t idesc = umma::idesc_bf16(128, ncols);
     const int kblocks = m.Kp / 64;
     for (int mt = 0; mt < mtiles; ++mt) {
         for (int kb = 0; kb < kblocks; ++kb) {
-            stage_w_block(ws_hi, ws_lo, m, mt, kb);
+            stage_w_block(ws, m, mt, kb);
             umma::fence_proxy_async();
             __syncthreads();
             if (threadIdx.x == 0) {
                 umma::fence_after();
-                const uint32_t a_hi = umma::smem_addr(ws_hi), a_lo = umma::smem_addr(ws_lo);
-                const uint32_t b_hi = umma::smem_addr(xs_hi) + (uint32_t)(kb * ncols * 128);
-                const uint32_t b_lo = umma::smem_addr(xs_lo) + (uint32_t)(kb * ncols * 128);
+                const uint32_t a0 = umma::smem_addr(ws);
+                const uint32_t b0 = umma::smem_addr(xs) + (uint32_t)(kb * ncols * 128);
                 const uint32_t d = tmem + (uint32_t)(mt * ncols);
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const uint32_t o = (uint32_t)(j * 32);
-                    const uint32_t acc0 = (first && kb == 0 && j == 0) ? 0u : 1u;
-                    umma::mma_bf16(d, umma::desc_sw128(a_hi + o), umma::desc_sw128(b_hi + o), idesc, acc0);
-                    umma::mma_bf16(d, umma::desc_sw128(a_hi + o), umma::desc_sw128(b_lo + o), idesc, 1u);
-                    umma::mma_bf16(d, umma::desc_sw128(a_lo + o), umma::desc_sw128(b_hi + o), idesc, 1u);
+#pragma unroll
+                    for (int t = 0; t < 3; ++t)
+#pragma unroll
+                        for (int u = 0; u + t < 3; ++u) {
+                            const uint32_t acc = (first && kb == 0 && j == 0 && t == 0 && u == 0) ? 0u : 1u;
+                            umma::mma_bf16(d, umma::desc_sw128(a0 + t * 16384u + o),
+                                           umma::desc_sw128(b0 + (uint32_t)(u * xbytes) + o), idesc, acc);
+                        }
                 }
                 umma::commit(umma::smem_addr(pp.bar));
             }
@@ -138,11 +148,9 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     const uint32_t *keys = reg.keys + (size_t)(ch.head + rl0) * net.W;
 
     uint8_t *base = smem_raw + ((1024u - (umma::smem_addr(smem_raw) & 1023u)) & 1023u);
-    const size_t xbytes = (size_t)ncols * tc.kp_max * 2;
-    uint8_t *xs_hi = base;
-    uint8_t *xs_lo = base + xbytes;
-    uint8_t *ws_hi = base + 2 * xbytes;
-    uint8_t *ws_lo = ws_hi + 128 * 128;
+    const size_t xbytes = (size_t)ncols * tc.kp_max * 2; // one bf16 term of the operand
+    uint8_t *xs = base;                                  // hi, mid, lo: 3 x xbytes
+    uint8_t *ws = base + 3 * xbytes;                     // 3 x 16 KB weight block
 
     if (tid == 0) umma::mbar_init(&bar, 1);
     if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tc.tmem_cols);
@@ -177,7 +185,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                 x[3] = b0[k];
             }
 #pragma unroll
-            for (int c = 0; c < 4; ++c) put_split(xs_hi, xs_lo, 4 * r + c, k, ncols, x[c]);
+            for (int c = 0; c < 4; ++c) put_split(xs, xbytes, 4 * r + c, k, ncols, x[c]);
         }
     }
     umma::fence_proxy_async();
@@ -190,16 +198,16 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     for (int i = 1; i <= net.n_lin - 2; ++i) {
         const int M = net.nodes[i + 1];
         const int mtiles = (M + 127) / 128;
-        gemm_accumulate(tc.lin[i], mtiles, ws_hi, ws_lo, xs_hi, xs_lo, ncols, tmem, true, pp);
+        gemm_accumulate(tc.lin[i], mtiles, ws, xs, xbytes, ncols, tmem, true, pp);
         for (int s = 0; s < net.nskip[i]; ++s) {
             const SkipDev &sk = net.skip[i][s];
             if (sk.kind == 1 && sk.from >= 1) {
                 __syncthreads();
-                stage_x_from_rows(xs_hi, xs_lo, ncols, cons, rstride, keys, net.W, nreg, net.hoff[sk.from],
+                stage_x_from_rows(xs, xbytes, ncols, cons, rstride, keys, net.W, nreg, net.hoff[sk.from],
                                   net.nodes[sk.from], tc.skip[i][s].Kp);
                 umma::fence_proxy_async();
                 __syncthreads();
-                gemm_accumulate(tc.skip[i][s], mtiles, ws_hi, ws_lo, xs_hi, xs_lo, ncols, tmem, false, pp);
+                gemm_accumulate(tc.skip[i][s], mtiles, ws, xs, xbytes, ncols, tmem, false, pp);
             }
         }
         umma::fence_after();
@@ -209,7 +217,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         for (int q = tid; q < R * (Kn - M > 0 ? Kn - M : 0); q += kThreads) {
             const int r = q / (Kn - M), k = M + q % (Kn - M);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) put_split(xs_hi, xs_lo, 4 * r + c, k, ncols, 0.f);
+            for (int c = 0; c < 4; ++c) put_split(xs, xbytes, 4 * r + c, k, ncols, 0.f);
         }
         for (int mt = 0; mt < mtiles; ++mt) {
             const int m = mt * 128 + warp * 32 + lane;
@@ -260,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                     }
                     if (Kn > 0) {
 #pragma unroll
-                        for (int c = 0; c < 4; ++c) put_split(xs_hi, xs_lo, 4 * r + c, m, ncols, x[c]);
+                        for (int c = 0; c < 4; ++c) put_split(xs, xbytes, 4 * r + c, m, ncols, x[c]);
                     }
                 }
             }
@@ -309,22 +317,24 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     if (warp == 0) umma::tmem_dealloc(tmem, (uint32_t)tc.tmem_cols);
 }
 
-__global__ void split_weights_kernel(const float *src, int M, int K, int Mp, int Kp, __nv_bfloat16 *hi,
-                                     __nv_bfloat16 *lo)
+__global__ void split_weights_kernel(const float *src, int M, int K, int Mp, int Kp, __nv_bfloat16 *dst)
 {
     const long long n = (long long)Mp * Kp;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const int m = (int)(q / Kp), k = (int)(q % Kp);
         const float v = (m < M && k < K) ? src[(size_t)m * K + k] : 0.f;
         const __nv_bfloat16 h = __float2bfloat16_rn(v);
-        hi[q] = h;
-        lo[q] = __float2bfloat16_rn(v - __bfloat162float(h));
+        const float r1 = v - __bfloat162float(h);
+        const __nv_bfloat16 md = __float2bfloat16_rn(r1);
+        dst[q] = h;
+        dst[n + q] = md;
+        dst[2 * n + q] = __float2bfloat16_rn(r1 - __bfloat162float(md));
     }
 }
 
 } // namespace
 
-size_t tc_smem_bytes(const TcNet &tc) { return 1024 + 2 * (size_t)tc.ncols * tc.kp_max * 2 + 2 * 128 * 128; }
+size_t tc_smem_bytes(const TcNet &tc) { return 1024 + 3 * (size_t)tc.ncols * tc.kp_max * 2 + 3 * 128 * 128; }
 
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,
                        int *d_err, cudaStream_t st)
@@ -337,12 +347,12 @@ void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg
     compose_tc_kernel<<<grid, kThreads, smem, st>>>(net, tc, reg, ch, (float)iso, d_err);
 }
 
-void launch_split_weights(const float *src, int M, int K, int Mp, int Kp, void *hi, void *lo, cudaStream_t st)
+void launch_split_weights(const float *src, int M, int K, int Mp, int Kp, void *dst, cudaStream_t st)
 {
     const long long n = (long long)Mp * Kp;
     if (n <= 0) return;
     const int grid = (int)std::min<long long>((n + 255) / 256, 4096);
-    split_weights_kernel<<<grid, 256, 0, st>>>(src, M, K, Mp, Kp, (__nv_bfloat16 *)hi, (__nv_bfloat16 *)lo);
+    split_weights_kernel<<<grid, 256, 0, st>>>(src, M, K, Mp, Kp, (__nv_bfloat16 *)dst);
 }
 
 } // namespace am

@@ -484,12 +484,10 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             auto split = [&](DevBuf &buf, const void *src_fp32, int M, int K, TcMat &m) {
                 const int Mp = (M + 127) / 128 * 128, Kp = (K + 63) / 64 * 64;
                 upload(e->scratch, src_fp32, sizeof(float) * (size_t)M * K, st);
-                AM_CUDA(buf.alloc(2 * sizeof(uint16_t) * (size_t)Mp * Kp));
-                uint16_t *hi = buf.as<uint16_t>(), *lo = hi + (size_t)Mp * Kp;
-                launch_split_weights(e->scratch.as<float>(), M, K, Mp, Kp, hi, lo, st);
+                AM_CUDA(buf.alloc(3 * sizeof(uint16_t) * (size_t)Mp * Kp));
+                launch_split_weights(e->scratch.as<float>(), M, K, Mp, Kp, buf.p, st);
                 AM_CUDA(cudaStreamSynchronize(st));
-                m.hi = (const __nv_bfloat16 *)hi;
-                m.lo = (const __nv_bfloat16 *)lo;
+                m.hi = (const __nv_bfloat16 *)buf.p;
                 m.Mp = Mp;
                 m.Kp = Kp;
                 tc.kp_max = std::max(tc.kp_max, Kp);
@@ -505,7 +503,8 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
                 }
             }
             tc.kp_max = std::max(tc.kp_max, 64);
-            int ncols = std::min(256, std::min(32768 / tc.kp_max, 512 / mtiles_max));
+            // three operand terms: 3 x ncols x kp_max x 2 bytes <= 128 KB
+            int ncols = std::min(256, std::min(21845 / tc.kp_max, 512 / mtiles_max));
             ncols = ncols / 16 * 16;
             AM_CHECK(ncols >= 16, "layer widths too large for the tensor-core composition tile");
             tc.ncols = ncols;

@@ -294,24 +294,22 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                     status = kSingular;
                     break;
                 }
-                bool appended = false;
+                // 0 append, 1 zero-length edge on e (merge), 2 zero-length closing edge
+                int decision = 0;
                 if (n > 0) {
                     const TS lx = __shfl_sync(0xffffffffu, vx, n - 1);
                     const TS ly = __shfl_sync(0xffffffffu, vy, n - 1);
                     const TS lz = __shfl_sync(0xffffffffu, vz, n - 1);
-                    const TS fx = __shfl_sync(0xffffffffu, vx, 0);
-                    const TS fy = __shfl_sync(0xffffffffu, vy, 0);
-                    const TS fz = __shfl_sync(0xffffffffu, vz, 0);
-                    if (fabs(V[0] - lx) + fabs(V[1] - ly) + fabs(V[2] - lz) < same_eps) {
-                        if (lane == n - 1) ve = bk; // zero-length edge on e: merge
-                    } else if (bk == s && fabs(V[0] - fx) + fabs(V[1] - fy) + fabs(V[2] - fz) < same_eps) {
-                        // zero-length closing edge on the start plane
-                    } else {
-                        appended = true;
+                    if (lane == 0) { // in the solve precision, on one lane
+                        if (fabs(V[0] - lx) + fabs(V[1] - ly) + fabs(V[2] - lz) < same_eps)
+                            decision = 1;
+                        else if (bk == s && fabs(V[0] - vx) + fabs(V[1] - vy) + fabs(V[2] - vz) < same_eps)
+                            decision = 2;
                     }
-                } else {
-                    appended = true;
+                    decision = __shfl_sync(0xffffffffu, decision, 0);
                 }
+                if (decision == 1 && lane == n - 1) ve = bk; // the edge on e has zero length
+                const bool appended = (decision == 0);
                 if (appended) {
                     if (lane == n) {
                         vx = V[0];

@@ -9,11 +9,11 @@
 
 namespace am {
 
-// A weight pre-split into bf16 hi + lo (w = hi + lo to ~2^-17), zero-padded
-// to Mp (multiple of 128) rows x Kp (multiple of 64) columns, row-major.
+// A weight pre-split into three bf16 terms (w = hi + mid + lo, 24 bits),
+// zero-padded to Mp (multiple of 128) rows x Kp (multiple of 64) columns,
+// row-major; the three planes are contiguous starting at `hi`.
 struct TcMat {
     const __nv_bfloat16 *hi;
-    const __nv_bfloat16 *lo;
     int Mp, Kp;
 };
 
@@ -28,6 +28,6 @@ struct TcNet {
 size_t tc_smem_bytes(const TcNet &tc);
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,
                        int *d_err, cudaStream_t st);
-void launch_split_weights(const float *src, int M, int K, int Mp, int Kp, void *hi, void *lo, cudaStream_t st);
+void launch_split_weights(const float *src, int M, int K, int Mp, int Kp, void *dst, cudaStream_t st);
 
 } // namespace am
