@@ -60,6 +60,7 @@ def lib():
     L.am_get_mesh.argtypes = [vp, vp, vp, vp]
     L.am_get_regions.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.am_set_option.argtypes = [vp, C.c_int, C.c_int64]
+    L.am_region_rows.argtypes = [vp, C.c_int64, C.c_int, vp, vp]
     _LIB = L
     return L
 

@@ -151,6 +151,9 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     const size_t xbytes = (size_t)ncols * tc.kp_max * 2; // one bf16 term of the operand
     uint8_t *xs = base;                                  // hi, mid, lo: 3 x xbytes
     uint8_t *ws = base + 3 * xbytes;                     // 3 x 16 KB weight block
+    uint32_t *skeys = reinterpret_cast<uint32_t *>(ws + 3 * 16384); // the tile's activation bits
+    for (int q = tid; q < R * net.W; q += kThreads) skeys[q] = q < nreg * net.W ? keys[q] : 0u;
+    keys = skeys;
 
     if (tid == 0) umma::mbar_init(&bar, 1);
     if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tc.tmem_cols);
@@ -174,7 +177,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                        make_float4(we[3 * e], we[3 * e + 1], we[3 * e + 2], be[e]));
         }
         // X_1 = diag(s_1) [W0 | b0]
-        const int Kp = net.n_lin >= 3 ? tc.lin[1].Kp : 0;
+        const int Kp = (n1 + 63) / 64 * 64;
         for (int q = tid; q < R * Kp; q += kThreads) {
             const int r = q / Kp, k = q % Kp;
             float x[4] = {0.f, 0.f, 0.f, 0.f};
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         umma::fence_after();
         // epilogue: accumulators -> constraint rows (HBM) and the next operand (smem)
         const float *bias = (const float *)net.bias[i];
-        const int Kn = (i + 1 <= net.n_lin - 2) ? tc.lin[i + 1].Kp : 0; // next operand's padded K
+        const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
         for (int q = tid; q < R * (Kn - M > 0 ? Kn - M : 0); q += kThreads) {
             const int r = q / (Kn - M), k = M + q % (Kn - M);
 #pragma unroll
@@ -279,7 +282,8 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         umma::fence_after();
     }
 
-    // face plane: w_eq = W_L . X_L (+ b_L, + connections into the output layer), fp32
+    // face plane: w_eq = W_L . X_L (+ b_L, + connections into the output layer)
+    // in fp32, from the operand in shared memory (hi + mid + lo is exact)
     {
         const int i = net.n_lin - 1;
         const int K = net.nodes[i];
@@ -287,13 +291,17 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         const int Mp = net.Mp[i];
         const float bl = ((const float *)net.bias[i])[0];
         for (int q = tid; q < nreg * 4; q += kThreads) {
-            const int r = q >> 2, c = q & 3;
+            const int r = q >> 2, c = q & 3, n = 4 * r + c;
+            float acc = 0.f;
+            for (int k = 0; k < K; ++k) {
+                const uint32_t off = umma::sw128_offset(n, k, ncols);
+                const float x = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + off)) +
+                                __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + xbytes + off)) +
+                                __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + 2 * xbytes + off));
+                acc += __ldg(wl + (size_t)k * Mp) * x;
+            }
             const uint32_t *key = keys + (size_t)r * net.W;
             const float *cr = cons + (size_t)r * rstride;
-            float acc = 0.f;
-            const int src = net.hoff[i];
-            for (int k = 0; k < K; ++k)
-                if (key_bit(key, src + k)) acc -= wl[(size_t)k * Mp] * cr[(size_t)(src + k) * 4 + c];
             for (int s = 0; s < net.nskip[i]; ++s) {
                 const SkipDev &sk = net.skip[i][s];
                 if (sk.kind == 0) {
@@ -334,7 +342,10 @@ __global__ void split_weights_kernel(const float *src, int M, int K, int Mp, int
 
 } // namespace
 
-size_t tc_smem_bytes(const TcNet &tc) { return 1024 + 3 * (size_t)tc.ncols * tc.kp_max * 2 + 3 * 128 * 128; }
+size_t tc_smem_bytes(const TcNet &tc, int W)
+{
+    return 1024 + 3 * (size_t)tc.ncols * tc.kp_max * 2 + 3 * 128 * 128 + (size_t)(tc.ncols / 4) * W * 4;
+}
 
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,
                        int *d_err, cudaStream_t st)
@@ -342,7 +353,7 @@ void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg
     if (ch.count <= 0) return;
     const int R = tc.ncols / 4;
     const int grid = (ch.count + R - 1) / R;
-    const size_t smem = tc_smem_bytes(tc);
+    const size_t smem = tc_smem_bytes(tc, net.W);
     cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     compose_tc_kernel<<<grid, kThreads, smem, st>>>(net, tc, reg, ch, (float)iso, d_err);
 }

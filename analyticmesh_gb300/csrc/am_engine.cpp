@@ -154,6 +154,7 @@ struct am_engine {
     long long num_regions = 0;
     am_stats stats{};
     int flip = 0;
+    double iso = 0.0;
     // mesh
     DevBuf w_table, w_rep, w_flag, w_vidx, w_bsum, w_fflag, w_fsize, w_fid, w_foff, w_verts, w_fs, w_fi, w_counts;
     std::vector<double> mesh_verts;
@@ -502,7 +503,9 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
                     if ((h || w) && from >= 1) split(e->tc_skip[i][c], arc_tm[t], h, w, tc.skip[i][c]);
                 }
             }
-            tc.kp_max = std::max(tc.kp_max, 64);
+            // the operand also holds hidden layer 1 and the last hidden layer
+            tc.kp_max = std::max(tc.kp_max, (e->nodes[1] + 63) / 64 * 64);
+            tc.kp_max = std::max(tc.kp_max, (e->nodes[e->n_lin - 1] + 63) / 64 * 64);
             // three operand terms: 3 x ncols x kp_max x 2 bytes <= 128 KB
             int ncols = std::min(256, std::min(21845 / tc.kp_max, 512 / mtiles_max));
             ncols = ncols / 16 * 16;
@@ -511,7 +514,7 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             int tcols = 32;
             while (tcols < mtiles_max * ncols) tcols <<= 1;
             tc.tmem_cols = tcols;
-            AM_CHECK(tc_smem_bytes(tc) <= 227u * 1024u, "tensor-core composition tile exceeds shared memory");
+            AM_CHECK(tc_smem_bytes(tc, e->W) <= 227u * 1024u, "tensor-core composition tile exceeds shared memory");
         }
         AM_CUDA(cudaGetLastError());
 
@@ -657,6 +660,7 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             }
         }
         e->flip = flip_insideout ? 1 : 0;
+        e->iso = iso;
         e->has_am = true;
     });
 }
@@ -829,6 +833,45 @@ int am_get_regions(am_engine *e, uint32_t *bits, int32_t *nverts, double *verts,
                                                       : (double)((const float *)mb.data())[4 * r + c];
         }
         AM_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int am_region_rows(am_engine *e, int64_t first, int count, double *rows, double *eq)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (!e->has_am) return AM_ERR_NO_RESULT;
+    if (first < 0 || count < 0 || first + count > e->num_regions) return AM_ERR_INVALID_ARGUMENT;
+    return guarded(e, [&] {
+        cudaStream_t st = e->st;
+        if (count == 0) return;
+        e->ensure_chunk(count);
+        ChunkDev ch;
+        ch.head = first;
+        ch.count = count;
+        ch.cons = e->cons.p;
+        ch.eq = e->eq.p;
+        ch.rec = e->rec.as<int32_t>();
+        AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
+        if (e->prec == kMixed)
+            launch_compose_tc(e->net, e->tcnet, e->regions(), ch, e->iso, e->d_err.as<int>(), st);
+        else
+            launch_compose(e->prec, e->net, e->regions(), ch, e->iso, st);
+        AM_CUDA(cudaGetLastError());
+        const size_t nrow = (size_t)count * e->ALLP * 4;
+        std::vector<unsigned char> rb(nrow * e->tc), eb((size_t)count * 4 * e->tc);
+        AM_CUDA(cudaMemcpyAsync(rb.data(), e->cons.p, rb.size(), cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaMemcpyAsync(eb.data(), e->eq.p, eb.size(), cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        e->check_err();
+        auto get = [&](const std::vector<unsigned char> &b, size_t q) {
+            return e->tc == 8 ? ((const double *)b.data())[q] : (double)((const float *)b.data())[q];
+        };
+        for (int r = 0; r < count; ++r)
+            for (int k = 0; k < e->ALL; ++k)
+                for (int c = 0; c < 4; ++c)
+                    if (rows) rows[((size_t)r * e->ALL + k) * 4 + c] = get(rb, ((size_t)r * e->ALLP + k) * 4 + c);
+        if (eq)
+            for (size_t q = 0; q < (size_t)count * 4; ++q) eq[q] = get(eb, q);
     });
 }
 

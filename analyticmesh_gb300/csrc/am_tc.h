@@ -25,7 +25,7 @@ struct TcNet {
     int tmem_cols;                      // TMEM columns per CTA (power of two)
 };
 
-size_t tc_smem_bytes(const TcNet &tc);
+size_t tc_smem_bytes(const TcNet &tc, int W);
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,
                        int *d_err, cudaStream_t st);
 void launch_split_weights(const float *src, int M, int K, int Mp, int Kp, void *dst, cudaStream_t st);

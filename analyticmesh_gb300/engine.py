@@ -172,6 +172,15 @@ class Engine:
         _lib.check(_lib.lib().am_export_mesh(self.h, path.encode(), 1 if is_polymesh else 0, 1 if is_float32 else 0),
                    self.h)
 
+    def region_rows(self, first: int, count: int):
+        """Constraint rows (count, ALL, 4) and face planes (count, 4) of
+        regions [first, first + count), recomposed on the device."""
+        ALL = self.N + self.E
+        rows = np.zeros((count, ALL, 4))
+        eq = np.zeros((count, 4))
+        _lib.check(_lib.lib().am_region_rows(self.h, int(first), int(count), rows.ctypes.data, eq.ctypes.data), self.h)
+        return rows, eq
+
     def regions(self) -> Regions:
         s = self.stats()
         R = int(s["num_regions"])

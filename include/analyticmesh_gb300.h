@@ -107,6 +107,13 @@ int am_get_regions(am_engine *engine, uint32_t *bits, int32_t *nverts, double *v
                    double *seeds, int32_t *start);
 int am_vert_capacity(void);
 
+/* Constraint rows of regions [first, first + count) of the last run,
+ * recomposed with the engine's composition path (no counterpart in the
+ * reference, where they live only inside a batch): rows count x ALL x 4
+ * (w0, w1, w2, b, sign-flipped as in backend/inc/process.h:181-192, ALL =
+ * hidden units + extra constraints), eq count x 4 (face plane, b - iso). */
+int am_region_rows(am_engine *engine, int64_t first, int count, double *rows, double *eq);
+
 typedef enum {
     AM_OPT_CHUNK = 1,         /* regions per chunk (default: sized to ~1 GiB of constraint rows) */
     AM_OPT_PHASE_TIMING = 2,  /* 1: time compose / polygon / frontier separately */
