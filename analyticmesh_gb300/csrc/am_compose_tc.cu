@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     uint32_t *skeys = reinterpret_cast<uint32_t *>(ws + 3 * 16384); // the tile's activation bits
     for (int q = tid; q < R * net.W; q += kThreads) skeys[q] = q < nreg * net.W ? keys[q] : 0u;
     keys = skeys;
+    __syncthreads(); // every thread reads every region's bits below
 
     if (tid == 0) umma::mbar_init(&bar, 1);
     if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tc.tmem_cols);

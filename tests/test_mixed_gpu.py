@@ -14,12 +14,12 @@ pytestmark = pytest.mark.gpu
 
 NETS = {
     "plain48x3": (lambda: wl.geometric([48, 48, 48], 12, perturb=0.05), 256),
-    "odd_widths": (lambda: wl.geometric([20, 50, 20, 80, 20], 13, skips=[[0], [1, 1, 0], [1, 1, 1], [0]],
+    "odd_widths": (lambda: wl.geometric([20, 50, 20, 80, 20], 13, skips=[[0], [1, 1, 0], [1, 1, 1], [0], [0]],
                                         tm_shapes=[[0, 0], [80, 20]]), 256),
     "skips24x4": (lambda: wl.geometric([24, 24, 24, 24], 9, skips=[[0], [1, 1, 0], [1, 0, 1], [0]],
                                        tm_shapes=[[0, 0], [24, 3]]), 256),
     "wide256x3": (lambda: wl.geometric([256, 256, 256], 14, perturb=0.02), 256),
-    "input_skip": (lambda: wl.geometric([64] * 5, 15, perturb=0.01, skips=[[0], [0], [1, 0, 0], [0]],
+    "input_skip": (lambda: wl.geometric([64] * 5, 15, perturb=0.01, skips=[[0], [0], [1, 0, 0], [0], [0]],
                                         tm_shapes=[[64, 3]]), 256),
 }
 
