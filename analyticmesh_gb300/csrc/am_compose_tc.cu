@@ -11,10 +11,13 @@
 // 128-row x 64-column blocks, are the A operand, staged block by block.
 // Every operand is split into three bf16 terms, x = hi + mid + lo (24
 // significant bits, as fp32); a block issues the six products whose weight is
-// at least 2^-16 -- hh, hm, mh, hl, lh, mm -- accumulating in fp32 in TMEM.
-// A two-term split leaves ~2^-17 of every operand unrepresented, which moved
-// vertices by ~1.5e-5 and changed near-degenerate walk decisions; the
-// three-term split gives fp32-level constraint rows.  The epilogue reads the accumulators with
+// at least 2^-16 -- hh, hm, mh, hl, lh, mm.  A two-term split leaves ~2^-17
+// of every operand unrepresented, which moved vertices by ~1.5e-5 and changed
+// near-degenerate walk decisions.  The tensor core's fp32 accumulation error
+// grows with the number of accumulate steps into one accumulator, so the
+// dominant hh product and the five small correction products accumulate in
+// two separate TMEM accumulators that the epilogue adds once: fp32-level
+// constraint rows.  The epilogue reads the accumulators with
 // tcgen05.ld (one TMEM lane per output unit), adds bias and skips, writes the
 // sign-flipped constraint rows to HBM for the polygon kernel, and writes the
 // next layer's masked operand straight back into shared memory.  The face
@@ -107,17 +110,24 @@ __device__ void gemm_accumulate(const TcMat &m, int mtiles, uint8_t *ws, uint8_t
                 umma::fence_after();
                 const uint32_t a0 = umma::smem_addr(ws);
                 const uint32_t b0 = umma::smem_addr(xs) + (uint32_t)(kb * ncols * 128);
-                const uint32_t d = tmem + (uint32_t)(mt * ncols);
+                const uint32_t d_main = tmem + (uint32_t)(mt * ncols);            // hh
+                const uint32_t d_corr = tmem + (uint32_t)((mtiles + mt) * ncols); // the rest
+                const bool fresh = first && kb == 0;
 #pragma unroll
                 for (int j = 0; j < 4; ++j) {
                     const uint32_t o = (uint32_t)(j * 32);
+                    umma::mma_bf16(d_main, umma::desc_sw128(a0 + o), umma::desc_sw128(b0 + o), idesc,
+                                   (fresh && j == 0) ? 0u : 1u);
+                    int q = 0;
 #pragma unroll
                     for (int t = 0; t < 3; ++t)
 #pragma unroll
                         for (int u = 0; u + t < 3; ++u) {
-                            const uint32_t acc = (first && kb == 0 && j == 0 && t == 0 && u == 0) ? 0u : 1u;
-                            umma::mma_bf16(d, umma::desc_sw128(a0 + t * 16384u + o),
-                                           umma::desc_sw128(b0 + (uint32_t)(u * xbytes) + o), idesc, acc);
+                            if (t == 0 && u == 0) continue;
+                            umma::mma_bf16(d_corr, umma::desc_sw128(a0 + t * 16384u + o),
+                                           umma::desc_sw128(b0 + (uint32_t)(u * xbytes) + o), idesc,
+                                           (fresh && j == 0 && q == 0) ? 0u : 1u);
+                            ++q;
                         }
                 }
                 umma::commit(umma::smem_addr(pp.bar));
@@ -226,8 +236,12 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         for (int mt = 0; mt < mtiles; ++mt) {
             const int m = mt * 128 + warp * 32 + lane;
             for (int cb = 0; cb < ncols / 16; ++cb) {
-                float v[16];
-                umma::tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(mt * ncols + cb * 16), v);
+                float v[16], vc[16];
+                const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+                umma::tmem_ld16(lane_base + (uint32_t)(mt * ncols + cb * 16), v);
+                umma::tmem_ld16(lane_base + (uint32_t)((mtiles + mt) * ncols + cb * 16), vc);
+#pragma unroll
+                for (int z = 0; z < 16; ++z) v[z] += vc[z];
                 if (m >= M) continue;
 #pragma unroll
                 for (int qq = 0; qq < 4; ++qq) {

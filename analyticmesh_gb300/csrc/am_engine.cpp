@@ -507,12 +507,13 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             tc.kp_max = std::max(tc.kp_max, (e->nodes[1] + 63) / 64 * 64);
             tc.kp_max = std::max(tc.kp_max, (e->nodes[e->n_lin - 1] + 63) / 64 * 64);
             // three operand terms: 3 x ncols x kp_max x 2 bytes <= 128 KB
-            int ncols = std::min(256, std::min(21845 / tc.kp_max, 512 / mtiles_max));
+            // two accumulators (main + correction) per M tile in 512 TMEM columns
+            int ncols = std::min(256, std::min(21845 / tc.kp_max, 256 / mtiles_max));
             ncols = ncols / 16 * 16;
             AM_CHECK(ncols >= 16, "layer widths too large for the tensor-core composition tile");
             tc.ncols = ncols;
             int tcols = 32;
-            while (tcols < mtiles_max * ncols) tcols <<= 1;
+            while (tcols < 2 * mtiles_max * ncols) tcols <<= 1;
             tc.tmem_cols = tcols;
             AM_CHECK(tc_smem_bytes(tc, e->W) <= 227u * 1024u, "tensor-core composition tile exceeds shared memory");
         }

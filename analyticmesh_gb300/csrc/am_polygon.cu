@@ -143,13 +143,11 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
         }
         __syncwarp();
         TS eqv[4];
-        {
-            const vec4_t<TC> e = ld4<TC>((const TC *)ch.eq + (size_t)rl * 4);
-            eqv[0] = (TS)e.x;
-            eqv[1] = (TS)e.y;
-            eqv[2] = (TS)e.z;
-            eqv[3] = (TS)e.w;
-        }
+        const vec4_t<TC> eqc = ld4<TC>((const TC *)ch.eq + (size_t)rl * 4); // scan precision copy
+        eqv[0] = (TS)eqc.x;
+        eqv[1] = (TS)eqc.y;
+        eqv[2] = (TS)eqc.z;
+        eqv[3] = (TS)eqc.w;
         const TS *midp = (const TS *)reg.mid + (size_t)rid * 4;
         TS p[3] = {midp[0], midp[1], midp[2]};
         int s = reg.start[rid];
@@ -210,10 +208,13 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                     row_of<TS, TC>(rows, rj, r1);
                     solve3<TS>(r0, r1, eqv, v);
                 }
+                TC vc[3] = {(TC)v[0], (TC)v[1], (TC)v[2]};
                 v[0] = __shfl_sync(0xffffffffu, v[0], 0);
                 v[1] = __shfl_sync(0xffffffffu, v[1], 0);
                 v[2] = __shfl_sync(0xffffffffu, v[2], 0);
-                const TC vc[3] = {(TC)v[0], (TC)v[1], (TC)v[2]};
+                vc[0] = __shfl_sync(0xffffffffu, vc[0], 0);
+                vc[1] = __shfl_sync(0xffffffffu, vc[1], 0);
+                vc[2] = __shfl_sync(0xffffffffu, vc[2], 0);
                 bool bad = false;
                 for (int k = lane; k < ALL; k += 32) {
                     if (k == ri || k == rj) continue;
@@ -239,16 +240,15 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
         bool closed = false;
         if (s >= 0) {
             int e = s, prev = -1;
-            TS cur[3] = {p[0], p[1], p[2]};
+            TC curc[3] = {(TC)p[0], (TC)p[1], (TC)p[2]}; // current point, scan precision
             for (int step = 0; step < kWalkSteps; ++step) {
                 // direction of the edge line: w_eq x w_e (counter-clockwise about w_eq)
                 const vec4_t<TC> ref_ = rows[e];
-                const TC eq0 = (TC)eqv[0], eq1 = (TC)eqv[1], eq2 = (TC)eqv[2];
-                const TC d0 = eq1 * ref_.z - eq2 * ref_.y;
-                const TC d1 = eq2 * ref_.x - eq0 * ref_.z;
-                const TC d2 = eq0 * ref_.y - eq1 * ref_.x;
+                const TC d0 = eqc.y * ref_.z - eqc.z * ref_.y;
+                const TC d1 = eqc.z * ref_.x - eqc.x * ref_.z;
+                const TC d2 = eqc.x * ref_.y - eqc.y * ref_.x;
                 const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-                const TC c0 = (TC)cur[0], c1 = (TC)cur[1], c2 = (TC)cur[2];
+                const TC c0 = curc[0], c1 = curc[1], c2 = curc[2];
                 // first hit along the edge line: min over crossing planes of
                 // t = max(0, -g) / a, compared as fractions
                 TC bnum = TC(1), bden = TC(0);
@@ -287,10 +287,16 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                     row_of<TS, TC>(rows, bk, rk);
                     solve3<TS>(re, rk, eqv, V);
                 }
+                TC Vc[3] = {(TC)V[0], (TC)V[1], (TC)V[2]}; // converted once, on the solving lane
+                int finite = (isfinite(V[0]) && isfinite(V[1]) && isfinite(V[2])) ? 1 : 0;
                 V[0] = __shfl_sync(0xffffffffu, V[0], 0);
                 V[1] = __shfl_sync(0xffffffffu, V[1], 0);
                 V[2] = __shfl_sync(0xffffffffu, V[2], 0);
-                if (!(isfinite(V[0]) && isfinite(V[1]) && isfinite(V[2]))) {
+                Vc[0] = __shfl_sync(0xffffffffu, Vc[0], 0);
+                Vc[1] = __shfl_sync(0xffffffffu, Vc[1], 0);
+                Vc[2] = __shfl_sync(0xffffffffu, Vc[2], 0);
+                finite = __shfl_sync(0xffffffffu, finite, 0);
+                if (!finite) {
                     status = kSingular;
                     break;
                 }
@@ -329,9 +335,9 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                 }
                 prev = e;
                 e = bk;
-                cur[0] = V[0];
-                cur[1] = V[1];
-                cur[2] = V[2];
+                curc[0] = Vc[0];
+                curc[1] = Vc[1];
+                curc[2] = Vc[2];
             }
             if (!closed && status == kOk) status = kTruncated;
         }
