@@ -202,13 +202,16 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                 const int ri = i < 32 ? __shfl_sync(0xffffffffu, top0, i) : __shfl_sync(0xffffffffu, top1, i - 32);
                 const int rj = j < 32 ? __shfl_sync(0xffffffffu, top0, j) : __shfl_sync(0xffffffffu, top1, j - 32);
                 TS v[3] = {TS(0), TS(0), TS(0)};
+                TC vc[3] = {TC(0), TC(0), TC(0)};
                 if (lane == 0) { // one lane solves, the warp shares the vertex
                     TS r0[4], r1[4];
                     row_of<TS, TC>(rows, ri, r0);
                     row_of<TS, TC>(rows, rj, r1);
                     solve3<TS>(r0, r1, eqv, v);
+                    vc[0] = (TC)v[0];
+                    vc[1] = (TC)v[1];
+                    vc[2] = (TC)v[2];
                 }
-                TC vc[3] = {(TC)v[0], (TC)v[1], (TC)v[2]};
                 v[0] = __shfl_sync(0xffffffffu, v[0], 0);
                 v[1] = __shfl_sync(0xffffffffu, v[1], 0);
                 v[2] = __shfl_sync(0xffffffffu, v[2], 0);
@@ -281,14 +284,18 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                     break;
                 }
                 TS V[3] = {TS(0), TS(0), TS(0)};
-                if (lane == 0) { // vertex = 3x3 solve of (edge plane, hit plane, face plane)
+                TC Vc[3] = {TC(0), TC(0), TC(0)};
+                int finite = 0;
+                if (lane == 0) { // vertex = 3x3 solve of (edge plane, hit plane, face plane), one lane
                     TS re[4], rk[4];
                     row_of<TS, TC>(rows, e, re);
                     row_of<TS, TC>(rows, bk, rk);
                     solve3<TS>(re, rk, eqv, V);
+                    Vc[0] = (TC)V[0];
+                    Vc[1] = (TC)V[1];
+                    Vc[2] = (TC)V[2];
+                    finite = (isfinite(V[0]) && isfinite(V[1]) && isfinite(V[2])) ? 1 : 0;
                 }
-                TC Vc[3] = {(TC)V[0], (TC)V[1], (TC)V[2]}; // converted once, on the solving lane
-                int finite = (isfinite(V[0]) && isfinite(V[1]) && isfinite(V[2])) ? 1 : 0;
                 V[0] = __shfl_sync(0xffffffffu, V[0], 0);
                 V[1] = __shfl_sync(0xffffffffu, V[1], 0);
                 V[2] = __shfl_sync(0xffffffffu, V[2], 0);
