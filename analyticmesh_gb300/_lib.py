@@ -61,6 +61,7 @@ def lib():
     L.am_get_regions.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.am_set_option.argtypes = [vp, C.c_int, C.c_int64]
     L.am_region_rows.argtypes = [vp, C.c_int64, C.c_int, vp, vp]
+    L.am_compose_rows_noalloc.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, C.c_double, vp, vp, vp]
     _LIB = L
     return L
 

@@ -130,6 +130,26 @@ int am_set_option(am_engine *engine, int option, int64_t value);
  * 16 <= N <= 256, N % 16 == 0, K % 64 == 0; device pointers. */
 int am_selftest_umma(const void *A, const void *B, void *D, int N, int K);
 
+/* ---- region composition that allocates nothing (no counterpart in the
+ * reference).  For callers that cannot let a library call cudaMalloc: code
+ * whose device memory is all owned by its own pool or budget, or that runs
+ * where an allocation (an implicitly synchronising call) is not allowed.
+ * Plain MLP without skip connections or extra constraints, FP32.  nodesnum as
+ * for am_init; weights / biases are host arrays of device pointers, weights[i]
+ * (nodesnum[i+1] x nodesnum[i]) and biases[i] per linear; the other buffers
+ * are on the device: states count x N bytes (0/1, N = hidden units,
+ * layer-major as the reference's states), rows
+ * count x N x 4 (16-byte aligned; the sign-flipped rows of
+ * backend/inc/process.h:181-192), eq count x 4 (face plane, b - iso).
+ * Scratch (transposed weights, packed keys) is one static 8 MiB device array
+ * in the library, held by every GPU that loads it until exit; the first call
+ * on each device looks its address up and should come before any stream
+ * capture.  Calls share that array, so calls that overlap on the GPU race.
+ * A network plus states larger than the array returns AM_ERR_CAPACITY. */
+int am_compose_rows_noalloc(const int32_t *nodesnum, int num_nodes, const float *const *weights,
+                            const float *const *biases, const uint8_t *states, int count, double iso,
+                            float *rows, float *eq, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,88 @@
+"""The composition entry point that allocates nothing
+(am_compose_rows_noalloc), checked against the engine's own composition of
+the same regions (am_region_rows) on two calls in a row.
+
+Named to be collected last: it must pass both in a fresh process and after
+every other test has used the library on the same device.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+import torch
+
+from analyticmesh_gb300 import _lib, engine, workloads as wl
+
+# same kernel and the same FP32 weights on both sides: the rows agree to
+# rounding of the input conversion at most
+RTOL = 1e-6
+
+
+def _unpack(bits, N):
+    """(R, words) uint32 keys -> (R, N) uint8 states, bit b of word w = unit 32 w + b."""
+    R, W = bits.shape
+    b = (bits[:, :, None] >> np.arange(32, dtype=np.uint32)[None, None, :]) & 1
+    return b.reshape(R, W * 32)[:, :N].astype(np.uint8)
+
+
+def _call(nodes, Ws, Bs, states, iso, rows, eq):
+    L = _lib.lib()
+    n = len(nodes)
+    nodes_c = (C.c_int32 * n)(*nodes)
+    wp = (C.c_void_p * (n - 1))(*[w.data_ptr() for w in Ws])
+    bp = (C.c_void_p * (n - 1))(*[b.data_ptr() for b in Bs])
+    return L.am_compose_rows_noalloc(nodes_c, n, wp, bp, C.c_void_p(states.data_ptr()), int(states.shape[0]),
+                                     C.c_double(iso), C.c_void_p(rows.data_ptr()), C.c_void_p(eq.data_ptr()),
+                                     C.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+
+@pytest.mark.gpu
+def test_noalloc_rows_match_engine_twice_in_a_row():
+    model = wl.sphere(1)  # 3 -> 128 x 4 -> 1
+    net = wl.net_arrays(model)
+    states, pts = wl.seeds_for(model, 256)
+    iso = 0.01
+    eng = engine.march(net, states, pts, "float32", iso=iso)
+    reg = eng.regions()
+    assert reg.num >= 4000, reg.num
+    N = sum(net.nodes[1:-1])
+    dev = torch.device("cuda")
+    Ws = [torch.tensor(w, dtype=torch.float32, device=dev).contiguous() for w in net.W]
+    Bs = [torch.tensor(b, dtype=torch.float32, device=dev).contiguous() for b in net.b]
+
+    # a large call, then a smaller one over other regions: the second runs on
+    # scratch that still holds the first call's contents
+    for first, count in ((0, 3000), (3000, 1000)):
+        ref_rows, ref_eq = eng.region_rows(first, count)
+        st = torch.from_numpy(_unpack(reg.bits[first:first + count], N)).to(dev)
+        rows = torch.full((count, N, 4), float("nan"), dtype=torch.float32, device=dev)
+        eq = torch.full((count, 4), float("nan"), dtype=torch.float32, device=dev)
+        assert _call(net.nodes, Ws, Bs, st, iso, rows, eq) == 0
+        torch.cuda.synchronize()
+        got_rows, got_eq = rows.double().cpu().numpy(), eq.double().cpu().numpy()
+        np.testing.assert_allclose(got_rows, ref_rows, rtol=RTOL, atol=RTOL * np.abs(ref_rows).max())
+        np.testing.assert_allclose(got_eq, ref_eq, rtol=RTOL, atol=RTOL * np.abs(ref_eq).max())
+    eng.close()
+
+
+@pytest.mark.gpu
+def test_noalloc_rejects_work_beyond_its_scratch():
+    model = wl.sphere(1)
+    net = wl.net_arrays(model)
+    dev = torch.device("cuda")
+    Ws = [torch.tensor(w, dtype=torch.float32, device=dev).contiguous() for w in net.W]
+    Bs = [torch.tensor(b, dtype=torch.float32, device=dev).contiguous() for b in net.b]
+    small = torch.zeros((1, 512), dtype=torch.uint8, device=dev)
+    rows = torch.zeros((1, 512, 4), dtype=torch.float32, device=dev)
+    eq = torch.zeros((1, 4), dtype=torch.float32, device=dev)
+    L = _lib.lib()
+    n = len(net.nodes)
+    args = [(C.c_int32 * n)(*net.nodes), n, (C.c_void_p * (n - 1))(*[w.data_ptr() for w in Ws]),
+            (C.c_void_p * (n - 1))(*[b.data_ptr() for b in Bs]), C.c_void_p(small.data_ptr())]
+    # 200000 regions x 16 key words exceed the 8 MiB scratch: rejected before
+    # any buffer is touched
+    rc = L.am_compose_rows_noalloc(*args, 200000, C.c_double(0.0), C.c_void_p(rows.data_ptr()),
+                                   C.c_void_p(eq.data_ptr()), None)
+    assert rc == 8  # AM_ERR_CAPACITY
+    assert L.am_compose_rows_noalloc(*args, 0, C.c_double(0.0), C.c_void_p(rows.data_ptr()),
+                                     C.c_void_p(eq.data_ptr()), None) == 1  # AM_ERR_INVALID_ARGUMENT: count < 1
