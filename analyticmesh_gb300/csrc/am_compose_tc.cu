@@ -3,12 +3,17 @@
 //
 // Same mathematics as am_compose.cu (the reference's fill_constraints,
 // backend/inc/process.h:18-193): for every region, A_{l+1} = W_l diag(s_l) A_l
-// (+ b_l, + skips), C = (1 - 2 s) A.  One CTA owns a tile of up to 64 regions
-// (4 columns each, N = 4 x regions <= 256) and keeps the masked operand
-// X_l = diag(s_l) A_l on chip the whole way through the network: as bf16
-// hi/lo splits in 128B-swizzled K-major shared memory, the B operand of
-// tcgen05.mma.  The layer weights, pre-split the same way and padded to
-// 128-row x 64-column blocks, are the A operand, staged block by block.
+// (+ b_l, + skips), C = (1 - 2 s) A.  One CTA owns a tile of regions (4
+// columns each, UMMA N = 4 x regions, chosen per launch from the chunk size so
+// that small frontier waves still spread over every SM) and keeps the masked
+// operand X_l = diag(s_l) A_l on chip the whole way through the network, as
+// bf16 terms in 128B-swizzled K-major shared memory: the B operand of
+// tcgen05.mma.  The layer weights are the A operand; they are pre-split and
+// stored in global memory as the exact shared-memory image of their 128 x 64
+// blocks, so one bulk copy (cp.async.bulk, completing on an mbarrier) stages a
+// block while the tensor core works on the previous one, and the first blocks
+// of the next layer land while the epilogue of this one runs.
+//
 // Every operand is split into three bf16 terms, x = hi + mid + lo (24
 // significant bits, as fp32); a block issues the six products whose weight is
 // at least 2^-16 -- hh, hm, mh, hl, lh, mm.  A two-term split leaves ~2^-17
@@ -17,12 +22,13 @@
 // grows with the number of accumulate steps into one accumulator, so the
 // dominant hh product and the five small correction products accumulate in
 // two separate TMEM accumulators that the epilogue adds once: fp32-level
-// constraint rows.  The epilogue reads the accumulators with
+// constraint rows.  The epilogue (eight warps; warps w and w + 4 share TMEM
+// lanes 32 (w % 4).. and split the columns) reads the accumulators with
 // tcgen05.ld (one TMEM lane per output unit), adds bias and skips, writes the
 // sign-flipped constraint rows to HBM for the polygon kernel, and writes the
 // next layer's masked operand straight back into shared memory.  The face
-// plane (output layer, one row) is a 4 x K dot product per region in fp32
-// from the rows just written.
+// plane (output layer, one row) is a 4 x K dot product per region in fp32,
+// one warp per region, from the operand in shared memory.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -35,20 +41,26 @@ namespace am {
 
 namespace {
 
-constexpr int kThreads = 128;
+constexpr int kThreads = 256;
 constexpr int kWaitIters = 1 << 22;
 
-// x = hi + mid + lo in bf16; the operand buffers are `xbytes` apart
-__device__ __forceinline__ void put_split(uint8_t *xs, size_t xbytes, int n, int k, int ncols, float v)
+// x = hi + mid + lo in bf16 at byte offset `off` of each term (terms `xbytes` apart)
+__device__ __forceinline__ void put_split(uint8_t *xs, size_t xbytes, uint32_t off, float v)
 {
     const __nv_bfloat16 h = __float2bfloat16_rn(v);
     const float r1 = v - __bfloat162float(h);
     const __nv_bfloat16 m = __float2bfloat16_rn(r1);
     const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-    const uint32_t off = umma::sw128_offset(n, k, ncols);
     *reinterpret_cast<__nv_bfloat16 *>(xs + off) = h;
     *reinterpret_cast<__nv_bfloat16 *>(xs + xbytes + off) = m;
     *reinterpret_cast<__nv_bfloat16 *>(xs + 2 * xbytes + off) = l;
+}
+
+__device__ __forceinline__ float get_split(const uint8_t *xs, size_t xbytes, uint32_t off)
+{
+    return __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + off)) +
+           __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + xbytes + off)) +
+           __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + 2 * xbytes + off));
 }
 
 // X[n = 4r + c][k] = s_k(r) ? -C[r][src + k][c] : 0 for k < K, 0 up to Kp
@@ -70,104 +82,164 @@ __device__ void stage_x_from_rows(uint8_t *xs, size_t xbytes, int ncols, const f
             }
         }
 #pragma unroll
-        for (int c = 0; c < 4; ++c) put_split(xs, xbytes, 4 * r + c, k, ncols, x[c]);
+        for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), x[c]);
     }
 }
 
-// one 128-row x 64-column block of a pre-split weight (three terms) into the
-// stage buffers (16 KB apart)
-__device__ void stage_w_block(uint8_t *ws, const TcMat &m, int mt, int kb)
+__device__ __forceinline__ int mat_blocks(const TcMat &m) { return (m.Mp / 128) * (m.Kp / 64); }
+__device__ __forceinline__ bool tc_skip(const SkipDev &sk) { return sk.kind == 1 && sk.from >= 1; }
+
+// global weight block g in the order the layers consume them: linear i's
+// blocks (M tile outer, K block inner), then its skip transforms
+__device__ const uint8_t *block_ptr(const NetDev &net, const TcNet &tc, int g)
 {
-    const size_t plane = (size_t)m.Mp * m.Kp;
-    const __nv_bfloat16 *src = m.hi + (size_t)(mt * 128) * m.Kp + (size_t)kb * 64;
-    for (int q = threadIdx.x; q < 3 * 128 * 8; q += kThreads) {
-        const int t = q / (128 * 8), rq = q % (128 * 8);
-        const int row = rq >> 3, ch = rq & 7;
-        const uint4 v = *reinterpret_cast<const uint4 *>(src + t * plane + (size_t)row * m.Kp + ch * 8);
-        *reinterpret_cast<uint4 *>(ws + t * 16384 + row * 128 + (((ch ^ (row & 7)) & 7) << 4)) = v;
+    for (int i = 1; i <= net.n_lin - 2; ++i) {
+        int nb = mat_blocks(tc.lin[i]);
+        if (g < nb) return tc.lin[i].blocks + (size_t)g * kWBlockBytes;
+        g -= nb;
+        for (int s = 0; s < net.nskip[i]; ++s)
+            if (tc_skip(net.skip[i][s])) {
+                nb = mat_blocks(tc.skip[i][s]);
+                if (g < nb) return tc.skip[i][s].blocks + (size_t)g * kWBlockBytes;
+                g -= nb;
+            }
     }
+    return nullptr;
 }
 
-struct Pipe {
-    uint64_t *bar;
-    uint32_t phase;
+__device__ int total_blocks(const NetDev &net, const TcNet &tc)
+{
+    int n = 0;
+    for (int i = 1; i <= net.n_lin - 2; ++i) {
+        n += mat_blocks(tc.lin[i]);
+        for (int s = 0; s < net.nskip[i]; ++s)
+            if (tc_skip(net.skip[i][s])) n += mat_blocks(tc.skip[i][s]);
+    }
+    return n;
+}
+
+// Weight-block pipeline, driven by thread 0: stage h % nstage receives block
+// h once block h - nstage's products have completed (done barrier); block
+// h's products wait for its bytes (full barrier).  Phase parity of either
+// barrier for block h is (h / nstage) & 1.
+struct WPipe {
+    uint64_t *full, *done;
+    uint8_t *ws;
+    int nstage, total, issued;
     int *err;
 };
 
-// D[mt] (+)= M . X over all K blocks of the operand in shared memory: six
-// products per K step (terms t, u of weight 2^-8(t+u), t + u <= 2)
-__device__ void gemm_accumulate(const TcMat &m, int mtiles, uint8_t *ws, uint8_t *xs, size_t xbytes, int ncols,
-                                uint32_t tmem, bool first, Pipe &pp)
+__device__ __forceinline__ void wp_wait(WPipe &p, uint64_t *bar, uint32_t parity)
+{
+    if (!umma::mbar_wait(bar, parity, kWaitIters)) {
+        atomicOr(p.err, kErrWalk);
+        umma::mbar_wait(bar, parity, kWaitIters);
+    }
+}
+
+__device__ void wp_issue(WPipe &p, const NetDev &net, const TcNet &tc)
+{
+    const int h = p.issued, s = h % p.nstage;
+    if (h >= p.nstage) wp_wait(p, p.done + s, (uint32_t)((h - p.nstage) / p.nstage) & 1u);
+    umma::mbar_expect_tx(p.full + s, (uint32_t)kWBlockBytes);
+    umma::bulk_g2s(p.ws + (size_t)s * kWBlockBytes, block_ptr(net, tc, h), (uint32_t)kWBlockBytes, p.full + s);
+    p.issued = h + 1;
+}
+
+// (thread 0) D[mt] (+)= M . X over all K blocks of the operand in shared
+// memory: six products per K step (terms t, u of weight 2^-8(t+u), t + u <= 2)
+__device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const TcMat &m, int mtiles, uint8_t *xs,
+                           size_t xbytes, int ncols, uint32_t tmem, bool first, int &g)
 {
     const uint32_t idesc = umma::idesc_bf16(128, ncols);
     const int kblocks = m.Kp / 64;
     for (int mt = 0; mt < mtiles; ++mt) {
         for (int kb = 0; kb < kblocks; ++kb) {
-            stage_w_block(ws, m, mt, kb);
-            umma::fence_proxy_async();
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                umma::fence_after();
-                const uint32_t a0 = umma::smem_addr(ws);
-                const uint32_t b0 = umma::smem_addr(xs) + (uint32_t)(kb * ncols * 128);
-                const uint32_t d_main = tmem + (uint32_t)(mt * ncols);            // hh
-                const uint32_t d_corr = tmem + (uint32_t)((mtiles + mt) * ncols); // the rest
-                const bool fresh = first && kb == 0;
+            if (p.issued <= g) wp_issue(p, net, tc);
+            const int s = g % p.nstage;
+            wp_wait(p, p.full + s, (uint32_t)(g / p.nstage) & 1u);
+            umma::fence_after();
+            const uint32_t a0 = umma::smem_addr(p.ws + (size_t)s * kWBlockBytes);
+            const uint32_t b0 = umma::smem_addr(xs) + (uint32_t)(kb * ncols * 128);
+            const uint32_t d_main = tmem + (uint32_t)(mt * ncols);            // hh
+            const uint32_t d_corr = tmem + (uint32_t)((mtiles + mt) * ncols); // the rest
+            const bool fresh = first && kb == 0;
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const uint32_t o = (uint32_t)(j * 32);
-                    umma::mma_bf16(d_main, umma::desc_sw128(a0 + o), umma::desc_sw128(b0 + o), idesc,
-                                   (fresh && j == 0) ? 0u : 1u);
-                    int q = 0;
+            for (int j = 0; j < 4; ++j) {
+                const uint32_t o = (uint32_t)(j * 32);
+                umma::mma_bf16(d_main, umma::desc_sw128(a0 + o), umma::desc_sw128(b0 + o), idesc,
+                               (fresh && j == 0) ? 0u : 1u);
+                int q = 0;
 #pragma unroll
-                    for (int t = 0; t < 3; ++t)
+                for (int t = 0; t < 3; ++t)
 #pragma unroll
-                        for (int u = 0; u + t < 3; ++u) {
-                            if (t == 0 && u == 0) continue;
-                            umma::mma_bf16(d_corr, umma::desc_sw128(a0 + t * 16384u + o),
-                                           umma::desc_sw128(b0 + (uint32_t)(u * xbytes) + o), idesc,
-                                           (fresh && j == 0 && q == 0) ? 0u : 1u);
-                            ++q;
-                        }
-                }
-                umma::commit(umma::smem_addr(pp.bar));
+                    for (int u = 0; u + t < 3; ++u) {
+                        if (t == 0 && u == 0) continue;
+                        umma::mma_bf16(d_corr, umma::desc_sw128(a0 + t * 16384u + o),
+                                       umma::desc_sw128(b0 + (uint32_t)(u * xbytes) + o), idesc,
+                                       (fresh && j == 0 && q == 0) ? 0u : 1u);
+                        ++q;
+                    }
             }
-            __syncwarp();
-            if (!umma::mbar_wait(pp.bar, pp.phase, kWaitIters)) {
-                if (threadIdx.x == 0) atomicOr(pp.err, kErrWalk);
-                umma::mbar_wait(pp.bar, pp.phase, kWaitIters);
-            }
-            pp.phase ^= 1u;
+            umma::commit(umma::smem_addr(p.done + s));
+            // refill the stage freed by the previous block
+            while (p.issued < p.total && p.issued <= g + p.nstage - 1) wp_issue(p, net, tc);
+            ++g;
         }
     }
 }
 
+// (thread 0) after the last block of a layer: wait until its products are in
+// TMEM, then start the next layer's blocks so they land during the epilogue
+__device__ void gemm_finish(WPipe &p, const NetDev &net, const TcNet &tc, int g)
+{
+    const int last = g - 1;
+    wp_wait(p, p.done + last % p.nstage, (uint32_t)(last / p.nstage) & 1u);
+    umma::fence_before();
+    while (p.issued < p.total && p.issued <= last + p.nstage) wp_issue(p, net, tc);
+}
+
+// (every thread, after the block barrier that follows gemm_finish) observe
+// the same completion before reading the accumulators
+__device__ __forceinline__ void gemm_observe(const WPipe &p, int last)
+{
+    if (!umma::mbar_wait(p.done + last % p.nstage, (uint32_t)(last / p.nstage) & 1u, kWaitIters)) atomicOr(p.err, kErrWalk);
+    umma::fence_after();
+}
+
 __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcNet tc, RegionsDev reg, ChunkDev ch,
-                                                                  float iso, int *err)
+                                                                  float iso, int ncols, int tmem_cols, int *err)
 {
     extern __shared__ uint8_t smem_raw[];
-    __shared__ uint64_t bar;
+    __shared__ uint64_t bars[4];
     __shared__ uint32_t tslot;
+    __shared__ int s_last;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int ncols = tc.ncols, R = ncols / 4;
+    const int R = ncols / 4;
     const long long rl0 = (long long)blockIdx.x * R;
     const int nreg = (int)min((long long)R, (long long)ch.count - rl0);
     if (nreg <= 0) return;
     const size_t rstride = (size_t)net.ALLP * 4;
     float *cons = (float *)ch.cons + (size_t)rl0 * rstride;
-    const uint32_t *keys = reg.keys + (size_t)(ch.head + rl0) * net.W;
+    const uint32_t *gkeys = reg.keys + (size_t)(ch.head + rl0) * net.W;
 
     uint8_t *base = smem_raw + ((1024u - (umma::smem_addr(smem_raw) & 1023u)) & 1023u);
     const size_t xbytes = (size_t)ncols * tc.kp_max * 2; // one bf16 term of the operand
     uint8_t *xs = base;                                  // hi, mid, lo: 3 x xbytes
-    uint8_t *ws = base + 3 * xbytes;                     // 3 x 16 KB weight block
-    uint32_t *skeys = reinterpret_cast<uint32_t *>(ws + 3 * 16384); // the tile's activation bits
-    for (int q = tid; q < R * net.W; q += kThreads) skeys[q] = q < nreg * net.W ? keys[q] : 0u;
-    keys = skeys;
-    __syncthreads(); // every thread reads every region's bits below
+    uint8_t *ws = base + 3 * xbytes;                     // nstage weight blocks
+    uint32_t *keys = reinterpret_cast<uint32_t *>(ws + (size_t)tc.nstage * kWBlockBytes); // the tile's bits
 
-    if (tid == 0) umma::mbar_init(&bar, 1);
-    if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tc.tmem_cols);
+    WPipe pp{bars, bars + 2, ws, tc.nstage, 0, 0, err};
+    if (tid == 0) {
+        for (int b = 0; b < 4; ++b) umma::mbar_init(bars + b, 1);
+        umma::fence_mbar_init();
+        pp.total = total_blocks(net, tc);
+        // the first weight blocks do not depend on the tile: start them now
+        while (pp.issued < pp.total && pp.issued < pp.nstage) wp_issue(pp, net, tc);
+    }
+    if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tmem_cols);
+    for (int q = tid; q < R * net.W; q += kThreads) keys[q] = q < nreg * net.W ? gkeys[q] : 0u;
+    __syncthreads(); // every thread reads every region's bits below
 
     // hidden layer 1 = linear 0 rows (sign-flipped) and the extra constraints
     {
@@ -199,7 +271,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                 x[3] = b0[k];
             }
 #pragma unroll
-            for (int c = 0; c < 4; ++c) put_split(xs, xbytes, 4 * r + c, k, ncols, x[c]);
+            for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), x[c]);
         }
     }
     umma::fence_proxy_async();
@@ -207,41 +279,53 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     __syncthreads();
     umma::fence_after();
     const uint32_t tmem = tslot;
-    Pipe pp{&bar, 0u, err};
+    int g = 0; // next weight block (thread 0)
+    const int q4 = warp & 3, half = warp >> 2;
 
     for (int i = 1; i <= net.n_lin - 2; ++i) {
         const int M = net.nodes[i + 1];
         const int mtiles = (M + 127) / 128;
-        gemm_accumulate(tc.lin[i], mtiles, ws, xs, xbytes, ncols, tmem, true, pp);
+        if (tid == 0) gemm_issue(pp, net, tc, tc.lin[i], mtiles, xs, xbytes, ncols, tmem, true, g);
         for (int s = 0; s < net.nskip[i]; ++s) {
             const SkipDev &sk = net.skip[i][s];
-            if (sk.kind == 1 && sk.from >= 1) {
+            if (tc_skip(sk)) {
+                // the operand is about to be overwritten: the products so far must be done
+                if (tid == 0) gemm_finish(pp, net, tc, g);
                 __syncthreads();
                 stage_x_from_rows(xs, xbytes, ncols, cons, rstride, keys, net.W, nreg, net.hoff[sk.from],
                                   net.nodes[sk.from], tc.skip[i][s].Kp);
                 umma::fence_proxy_async();
                 __syncthreads();
-                gemm_accumulate(tc.skip[i][s], mtiles, ws, xs, xbytes, ncols, tmem, false, pp);
+                if (tid == 0) gemm_issue(pp, net, tc, tc.skip[i][s], mtiles, xs, xbytes, ncols, tmem, false, g);
             }
         }
-        umma::fence_after();
+        if (tid == 0) {
+            gemm_finish(pp, net, tc, g);
+            s_last = g - 1;
+        }
+        __syncwarp();
+        __syncthreads();
+        gemm_observe(pp, s_last);
         // epilogue: accumulators -> constraint rows (HBM) and the next operand (smem)
         const float *bias = (const float *)net.bias[i];
         const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
-        for (int q = tid; q < R * (Kn - M > 0 ? Kn - M : 0); q += kThreads) {
+        for (int q = tid; q < R * (Kn - M); q += kThreads) {
             const int r = q / (Kn - M), k = M + q % (Kn - M);
 #pragma unroll
-            for (int c = 0; c < 4; ++c) put_split(xs, xbytes, 4 * r + c, k, ncols, 0.f);
+            for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), 0.f);
         }
         for (int mt = 0; mt < mtiles; ++mt) {
-            const int m = mt * 128 + warp * 32 + lane;
-            for (int cb = 0; cb < ncols / 16; ++cb) {
+            const int m = mt * 128 + q4 * 32 + lane;
+            const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
+            const float bm = m < M ? bias[m] : 0.f;
+            const int row = net.hoff[i + 1] + m;
+            // byte offset of (n, k = m) for n = 0 (the swizzle adds n & 7)
+            const uint32_t kofs = (uint32_t)((m >> 6) * ncols * 128 + ((m & 7) << 1));
+            const int kchunk = (m & 63) >> 3;
+            for (int cb = half; cb < ncols / 16; cb += 2) {
                 float v[16], vc[16];
-                const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
                 umma::tmem_ld16(lane_base + (uint32_t)(mt * ncols + cb * 16), v);
                 umma::tmem_ld16(lane_base + (uint32_t)((mtiles + mt) * ncols + cb * 16), vc);
-#pragma unroll
-                for (int z = 0; z < 16; ++z) v[z] += vc[z];
                 if (m >= M) continue;
 #pragma unroll
                 for (int qq = 0; qq < 4; ++qq) {
@@ -250,16 +334,17 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                     if (r < nreg) {
                         const uint32_t *key = keys + (size_t)r * net.W;
                         float *cr = cons + (size_t)r * rstride;
-                        float o[4] = {v[4 * qq], v[4 * qq + 1], v[4 * qq + 2], v[4 * qq + 3] + bias[m]};
+                        float o[4] = {v[4 * qq] + vc[4 * qq], v[4 * qq + 1] + vc[4 * qq + 1],
+                                      v[4 * qq + 2] + vc[4 * qq + 2], v[4 * qq + 3] + vc[4 * qq + 3] + bm};
                         for (int s = 0; s < net.nskip[i]; ++s) {
                             const SkipDev &sk = net.skip[i][s];
                             if (sk.kind == 0) {
                                 if (sk.from == 0) {
                                     if (m < 3) o[m] += 1.f;
                                 } else {
-                                    const int row = net.hoff[sk.from] + m;
-                                    if (key_bit(key, row)) {
-                                        const float4 c = ld4<float>(cr + (size_t)row * 4);
+                                    const int srow = net.hoff[sk.from] + m;
+                                    if (key_bit(key, srow)) {
+                                        const float4 c = ld4<float>(cr + (size_t)srow * 4);
                                         o[0] -= c.x;
                                         o[1] -= c.y;
                                         o[2] -= c.z;
@@ -273,7 +358,6 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                                 o[2] += tt[2 * (size_t)sk.Mp + m];
                             }
                         }
-                        const int row = net.hoff[i + 1] + m;
                         const bool act = key_bit(key, row);
                         const float sg = act ? -1.f : 1.f;
                         st4<float>(cr + (size_t)row * 4, make_float4(sg * o[0], sg * o[1], sg * o[2], sg * o[3]));
@@ -286,7 +370,11 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                     }
                     if (Kn > 0) {
 #pragma unroll
-                        for (int c = 0; c < 4; ++c) put_split(xs, xbytes, 4 * r + c, m, ncols, x[c]);
+                        for (int c = 0; c < 4; ++c) {
+                            const int n = 4 * r + c;
+                            put_split(xs, xbytes, kofs + (uint32_t)(n * 128) + (uint32_t)(((kchunk ^ (n & 7)) & 7) << 4),
+                                      x[c]);
+                        }
                     }
                 }
             }
@@ -298,87 +386,122 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     }
 
     // face plane: w_eq = W_L . X_L (+ b_L, + connections into the output layer)
-    // in fp32, from the operand in shared memory (hi + mid + lo is exact)
+    // in fp32, one warp per region, from the operand in shared memory
+    // (hi + mid + lo is exact)
     {
         const int i = net.n_lin - 1;
         const int K = net.nodes[i];
         const float *wl = (const float *)net.Wt[i]; // [K][Mp], column 0
         const int Mp = net.Mp[i];
         const float bl = ((const float *)net.bias[i])[0];
-        for (int q = tid; q < nreg * 4; q += kThreads) {
-            const int r = q >> 2, c = q & 3, n = 4 * r + c;
-            float acc = 0.f;
-            for (int k = 0; k < K; ++k) {
-                const uint32_t off = umma::sw128_offset(n, k, ncols);
-                const float x = __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + off)) +
-                                __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + xbytes + off)) +
-                                __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + 2 * xbytes + off));
-                acc += __ldg(wl + (size_t)k * Mp) * x;
+        for (int r = warp; r < nreg; r += kThreads / 32) {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            for (int k = lane; k < K; k += 32) {
+                const float w = __ldg(wl + (size_t)k * Mp);
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, get_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols)), acc[c]);
             }
-            const uint32_t *key = keys + (size_t)r * net.W;
-            const float *cr = cons + (size_t)r * rstride;
-            for (int s = 0; s < net.nskip[i]; ++s) {
-                const SkipDev &sk = net.skip[i][s];
-                if (sk.kind == 0) {
-                    if (sk.from >= 1 && net.nodes[sk.from] == 1 && key_bit(key, net.hoff[sk.from]))
-                        acc -= cr[(size_t)net.hoff[sk.from] * 4 + c];
-                } else if (sk.from == 0) {
-                    if (c < 3) acc += ((const float *)sk.tmt)[(size_t)c * sk.Mp];
-                } else {
-                    const float *tt = (const float *)sk.tmt; // [dec][Mp]
-                    const int hs = net.hoff[sk.from];
-                    for (int k = 0; k < net.nodes[sk.from]; ++k)
-                        if (key_bit(key, hs + k)) acc -= tt[(size_t)k * sk.Mp] * cr[(size_t)(hs + k) * 4 + c];
+#pragma unroll
+            for (int c = 0; c < 4; ++c)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+            if (lane < 4) {
+                const int c = lane;
+                float a = c == 0 ? acc[0] : (c == 1 ? acc[1] : (c == 2 ? acc[2] : acc[3]));
+                const uint32_t *key = keys + (size_t)r * net.W;
+                const float *cr = cons + (size_t)r * rstride;
+                for (int s = 0; s < net.nskip[i]; ++s) {
+                    const SkipDev &sk = net.skip[i][s];
+                    if (sk.kind == 0) {
+                        if (sk.from >= 1 && net.nodes[sk.from] == 1 && key_bit(key, net.hoff[sk.from]))
+                            a -= cr[(size_t)net.hoff[sk.from] * 4 + c];
+                    } else if (sk.from == 0) {
+                        if (c < 3) a += ((const float *)sk.tmt)[(size_t)c * sk.Mp];
+                    } else {
+                        const float *tt = (const float *)sk.tmt; // [dec][Mp]
+                        const int hs = net.hoff[sk.from];
+                        for (int k = 0; k < net.nodes[sk.from]; ++k)
+                            if (key_bit(key, hs + k)) a -= tt[(size_t)k * sk.Mp] * cr[(size_t)(hs + k) * 4 + c];
+                    }
                 }
+                if (c == 3) a += bl - iso;
+                ((float *)ch.eq)[(size_t)(rl0 + r) * 4 + c] = a;
             }
-            if (c == 3) acc += bl - iso;
-            ((float *)ch.eq)[(size_t)(rl0 + r) * 4 + c] = acc;
         }
     }
     umma::fence_before();
     __syncthreads();
-    if (warp == 0) umma::tmem_dealloc(tmem, (uint32_t)tc.tmem_cols);
+    if (warp == 0) umma::tmem_dealloc(tmem, (uint32_t)tmem_cols);
 }
 
-__global__ void split_weights_kernel(const float *src, int M, int K, int Mp, int Kp, __nv_bfloat16 *dst)
+// src (M x K fp32, row-major) -> three bf16 terms as the shared-memory image
+// of 128 x 64 blocks (K-major, 128-byte swizzle), zero padding to Mp x Kp
+__global__ void pack_weights_kernel(const float *src, int M, int K, int Mp, int Kp, uint8_t *dst)
 {
     const long long n = (long long)Mp * Kp;
+    const int kblocks = Kp / 64;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
         const int m = (int)(q / Kp), k = (int)(q % Kp);
         const float v = (m < M && k < K) ? src[(size_t)m * K + k] : 0.f;
         const __nv_bfloat16 h = __float2bfloat16_rn(v);
         const float r1 = v - __bfloat162float(h);
         const __nv_bfloat16 md = __float2bfloat16_rn(r1);
-        dst[q] = h;
-        dst[n + q] = md;
-        dst[2 * n + q] = __float2bfloat16_rn(r1 - __bfloat162float(md));
+        const __nv_bfloat16 lo = __float2bfloat16_rn(r1 - __bfloat162float(md));
+        const int mt = m >> 7, r = m & 127, kb = k >> 6, kk = k & 63;
+        uint8_t *blk = dst + (size_t)(mt * kblocks + kb) * kWBlockBytes;
+        const uint32_t off = (uint32_t)(r * 128 + ((((kk >> 3) ^ (r & 7)) & 7) << 4) + ((kk & 7) << 1));
+        *reinterpret_cast<__nv_bfloat16 *>(blk + off) = h;
+        *reinterpret_cast<__nv_bfloat16 *>(blk + 16384 + off) = md;
+        *reinterpret_cast<__nv_bfloat16 *>(blk + 32768 + off) = lo;
     }
+}
+
+int sm_count()
+{
+    static int sms[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return 148;
+    if (!sms[dev]) {
+        int n = 0;
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        sms[dev] = n > 0 ? n : 148;
+    }
+    return sms[dev];
 }
 
 } // namespace
 
-size_t tc_smem_bytes(const TcNet &tc, int W)
+size_t tc_smem_bytes(const TcNet &tc, int ncols, int W)
 {
-    return 1024 + 3 * (size_t)tc.ncols * tc.kp_max * 2 + 3 * 128 * 128 + (size_t)(tc.ncols / 4) * W * 4;
+    return 1024 + 3 * (size_t)ncols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(ncols / 4) * W * 4;
 }
 
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,
                        int *d_err, cudaStream_t st)
 {
     if (ch.count <= 0) return;
-    const int R = tc.ncols / 4;
+    // one tile per SM when the chunk is small, the widest tile otherwise
+    const int sms = sm_count();
+    const int per = (ch.count + sms - 1) / sms;
+    int ncols = (4 * per + 15) / 16 * 16;
+    ncols = std::max(16, std::min(ncols, tc.ncols_max));
+    int tcols = 32;
+    while (tcols < 2 * tc.mtiles_max * ncols) tcols <<= 1;
+    const int R = ncols / 4;
     const int grid = (ch.count + R - 1) / R;
-    const size_t smem = tc_smem_bytes(tc, net.W);
-    cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    compose_tc_kernel<<<grid, kThreads, smem, st>>>(net, tc, reg, ch, (float)iso, d_err);
+    const size_t smem = tc_smem_bytes(tc, ncols, net.W);
+    cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)tc_smem_bytes(tc, tc.ncols_max, net.W));
+    compose_tc_kernel<<<grid, kThreads, smem, st>>>(net, tc, reg, ch, (float)iso, ncols, tcols, d_err);
 }
 
-void launch_split_weights(const float *src, int M, int K, int Mp, int Kp, void *dst, cudaStream_t st)
+void launch_pack_weights(const float *src, int M, int K, int Mp, int Kp, void *dst, cudaStream_t st)
 {
     const long long n = (long long)Mp * Kp;
     if (n <= 0) return;
     const int grid = (int)std::min<long long>((n + 255) / 256, 4096);
-    split_weights_kernel<<<grid, 256, 0, st>>>(src, M, K, Mp, Kp, (__nv_bfloat16 *)dst);
+    pack_weights_kernel<<<grid, 256, 0, st>>>(src, M, K, Mp, Kp, (uint8_t *)dst);
 }
 
 } // namespace am

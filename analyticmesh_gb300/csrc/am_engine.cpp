@@ -478,21 +478,21 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
         net.w_extra = e->wext.p;
         net.b_extra = e->bext.p;
         if (prec == kMixed) {
-            // bf16 hi/lo splits, padded to 128-row x 64-column blocks
+            // three bf16 terms per weight, stored as 128 x 64 shared-memory block images
             TcNet &tc = e->tcnet;
             memset(&tc, 0, sizeof(tc));
-            int mtiles_max = 1;
+            tc.mtiles_max = 1;
             auto split = [&](DevBuf &buf, const void *src_fp32, int M, int K, TcMat &m) {
                 const int Mp = (M + 127) / 128 * 128, Kp = (K + 63) / 64 * 64;
                 upload(e->scratch, src_fp32, sizeof(float) * (size_t)M * K, st);
-                AM_CUDA(buf.alloc(3 * sizeof(uint16_t) * (size_t)Mp * Kp));
-                launch_split_weights(e->scratch.as<float>(), M, K, Mp, Kp, buf.p, st);
+                AM_CUDA(buf.alloc((size_t)(Mp / 128) * (Kp / 64) * kWBlockBytes));
+                launch_pack_weights(e->scratch.as<float>(), M, K, Mp, Kp, buf.p, st);
                 AM_CUDA(cudaStreamSynchronize(st));
-                m.hi = (const __nv_bfloat16 *)buf.p;
+                m.blocks = (const uint8_t *)buf.p;
                 m.Mp = Mp;
                 m.Kp = Kp;
                 tc.kp_max = std::max(tc.kp_max, Kp);
-                mtiles_max = std::max(mtiles_max, Mp / 128);
+                tc.mtiles_max = std::max(tc.mtiles_max, Mp / 128);
             };
             for (int i = 1; i <= e->n_lin - 2; ++i) {
                 split(e->tc_lin[i], weights[i], e->nodes[i + 1], e->nodes[i], tc.lin[i]);
@@ -506,16 +506,20 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             // the operand also holds hidden layer 1 and the last hidden layer
             tc.kp_max = std::max(tc.kp_max, (e->nodes[1] + 63) / 64 * 64);
             tc.kp_max = std::max(tc.kp_max, (e->nodes[e->n_lin - 1] + 63) / 64 * 64);
-            // three operand terms: 3 x ncols x kp_max x 2 bytes <= 128 KB
+            // widest tile: three operand terms (3 x ncols x kp_max x 2 bytes)
+            // beside two weight blocks in flight (one if that leaves no room),
             // two accumulators (main + correction) per M tile in 512 TMEM columns
-            int ncols = std::min(256, std::min(21845 / tc.kp_max, 256 / mtiles_max));
-            ncols = ncols / 16 * 16;
-            AM_CHECK(ncols >= 16, "layer widths too large for the tensor-core composition tile");
-            tc.ncols = ncols;
-            int tcols = 32;
-            while (tcols < 2 * mtiles_max * ncols) tcols <<= 1;
-            tc.tmem_cols = tcols;
-            AM_CHECK(tc_smem_bytes(tc, e->W) <= 227u * 1024u, "tensor-core composition tile exceeds shared memory");
+            const size_t smem_cap = 227u * 1024u;
+            for (tc.nstage = 2; tc.nstage >= 1; --tc.nstage) {
+                const long long room = (long long)smem_cap - 1024 - (long long)tc.nstage * kWBlockBytes - 64ll * e->W * 4;
+                int ncols = (int)std::min<long long>(256, std::max<long long>(0, room) / (6ll * tc.kp_max));
+                ncols = std::min(ncols, 256 / tc.mtiles_max) / 16 * 16;
+                tc.ncols_max = ncols;
+                if (ncols >= 16) break;
+            }
+            AM_CHECK(tc.nstage >= 1 && tc.ncols_max >= 16, "layer widths too large for the tensor-core composition tile");
+            AM_CHECK(tc_smem_bytes(tc, tc.ncols_max, e->W) <= smem_cap,
+                     "tensor-core composition tile exceeds shared memory");
         }
         AM_CUDA(cudaGetLastError());
 

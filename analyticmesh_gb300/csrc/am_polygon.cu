@@ -61,14 +61,64 @@ __device__ __forceinline__ bool ahead(unsigned long long ka, int ia, unsigned lo
     return ka > kb || (ka == kb && ia < ib);
 }
 
-template <typename TS, typename TC>
-__device__ __forceinline__ void row_of(const vec4_t<TC> *rows, int k, TS *r)
+__device__ __forceinline__ bool finite_bits(float v) { return (__float_as_uint(v) & 0x7f800000u) != 0x7f800000u; }
+__device__ __forceinline__ bool finite_bits(double v)
 {
-    const vec4_t<TC> v = rows[k];
-    r[0] = (TS)v.x;
-    r[1] = (TS)v.y;
-    r[2] = (TS)v.z;
-    r[3] = (TS)v.w;
+    return ((uint32_t)(__double_as_longlong(v) >> 52) & 0x7ffu) != 0x7ffu;
+}
+
+// The vertex of planes a, b and the face plane, solved by the warp: lanes
+// 0-7 convert the two rows' components (one conversion instruction), lane
+// L = 0..3 (and its copies L + 4, L + 8, ...) computes Cramer's determinant
+// with column L - 1 replaced by -b (L = 0: none), then divides by the lane-0
+// determinant -- the same arithmetic as solve3 on one lane, in three
+// dependent FP64 sequences (convert, determinant, divide) instead of forty,
+// which matters because the SM's FP64 pipe issues a warp instruction at the
+// same cost however few lanes are active.  Every lane returns the vertex in
+// the solve precision (V) and rounded to the scan precision (Vc); false if a
+// coordinate is not finite.
+template <typename TC, typename TS>
+__device__ __forceinline__ bool warp_solve(const vec4_t<TC> *rows, int a, int b, const TS *eqv, TS *V, TC *Vc,
+                                           int lane)
+{
+    const TC *ra = reinterpret_cast<const TC *>(rows + a);
+    const TC *rb = reinterpret_cast<const TC *>(rows + b);
+    const int c = lane & 7;
+    const TS cs = (TS)(c < 4 ? ra[c] : rb[c - 4]);
+    TS m[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) m[j] = __shfl_sync(0xffffffffu, cs, j);
+    const int L = lane & 3;
+    const TS a00 = L == 1 ? -m[3] : m[0], a01 = L == 2 ? -m[3] : m[1], a02 = L == 3 ? -m[3] : m[2];
+    const TS a10 = L == 1 ? -m[7] : m[4], a11 = L == 2 ? -m[7] : m[5], a12 = L == 3 ? -m[7] : m[6];
+    const TS a20 = L == 1 ? -eqv[3] : eqv[0], a21 = L == 2 ? -eqv[3] : eqv[1], a22 = L == 3 ? -eqv[3] : eqv[2];
+    const TS d = det3<TS>(a00, a01, a02, a10, a11, a12, a20, a21, a22);
+    const TS d0 = __shfl_sync(0xffffffffu, d, 0);
+    const TS x = d / d0;
+    const TC xc = (TC)x;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        V[j] = __shfl_sync(0xffffffffu, x, j + 1);
+        Vc[j] = __shfl_sync(0xffffffffu, xc, j + 1);
+    }
+    return finite_bits(V[0]) && finite_bits(V[1]) && finite_bits(V[2]);
+}
+
+// L1 distance test |V - P|_1 < eps.  With TS wider than TC it is decided on
+// the scan-precision copies when the rounding margin allows -- Vc and Pc are
+// V and P rounded to nearest, so the TC sum is within 2^-23 (|Vc|_1 + |Pc|_1)
+// + 3 ulp of the exact one; 2^-21 (|Vc|_1 + |Pc|_1 + d) bounds both -- and
+// returns -1 ("near") otherwise, for the caller to decide in TS.
+template <typename TC, typename TS>
+__device__ __forceinline__ int same_filter(const TC *Vc, TC px, TC py, TC pz, TS eps)
+{
+    const TC d = fabs(Vc[0] - px) + fabs(Vc[1] - py) + fabs(Vc[2] - pz);
+    const TC mag = fabs(Vc[0]) + fabs(Vc[1]) + fabs(Vc[2]) + fabs(px) + fabs(py) + fabs(pz);
+    const TC margin = TC(4.76837158203125e-7) * (mag + d); // 2^-21
+    const TC e = (TC)eps;
+    if (d >= e + margin) return 0;
+    if (d + margin < e) return 1;
+    return -1;
 }
 
 __device__ __forceinline__ unsigned long long load_slot(const unsigned long long *p)
@@ -201,23 +251,9 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                 get_i_j(x, ALL, i, j);
                 const int ri = i < 32 ? __shfl_sync(0xffffffffu, top0, i) : __shfl_sync(0xffffffffu, top1, i - 32);
                 const int rj = j < 32 ? __shfl_sync(0xffffffffu, top0, j) : __shfl_sync(0xffffffffu, top1, j - 32);
-                TS v[3] = {TS(0), TS(0), TS(0)};
-                TC vc[3] = {TC(0), TC(0), TC(0)};
-                if (lane == 0) { // one lane solves, the warp shares the vertex
-                    TS r0[4], r1[4];
-                    row_of<TS, TC>(rows, ri, r0);
-                    row_of<TS, TC>(rows, rj, r1);
-                    solve3<TS>(r0, r1, eqv, v);
-                    vc[0] = (TC)v[0];
-                    vc[1] = (TC)v[1];
-                    vc[2] = (TC)v[2];
-                }
-                v[0] = __shfl_sync(0xffffffffu, v[0], 0);
-                v[1] = __shfl_sync(0xffffffffu, v[1], 0);
-                v[2] = __shfl_sync(0xffffffffu, v[2], 0);
-                vc[0] = __shfl_sync(0xffffffffu, vc[0], 0);
-                vc[1] = __shfl_sync(0xffffffffu, vc[1], 0);
-                vc[2] = __shfl_sync(0xffffffffu, vc[2], 0);
+                TS v[3];
+                TC vc[3];
+                warp_solve<TC, TS>(rows, ri, rj, eqv, v, vc, lane);
                 bool bad = false;
                 for (int k = lane; k < ALL; k += 32) {
                     if (k == ri || k == rj) continue;
@@ -238,6 +274,7 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
         // ---------------------------------------------------- walk
         // lane i holds vertex i and the plane of the edge leaving it
         TS vx = 0, vy = 0, vz = 0;
+        TC cx = 0, cy = 0, cz = 0; // the vertex rounded to the scan precision
         int ve = -1;
         int n = 0;
         bool closed = false;
@@ -283,43 +320,44 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                     status = kOpen;
                     break;
                 }
-                TS V[3] = {TS(0), TS(0), TS(0)};
-                TC Vc[3] = {TC(0), TC(0), TC(0)};
-                int finite = 0;
-                if (lane == 0) { // vertex = 3x3 solve of (edge plane, hit plane, face plane), one lane
-                    TS re[4], rk[4];
-                    row_of<TS, TC>(rows, e, re);
-                    row_of<TS, TC>(rows, bk, rk);
-                    solve3<TS>(re, rk, eqv, V);
-                    Vc[0] = (TC)V[0];
-                    Vc[1] = (TC)V[1];
-                    Vc[2] = (TC)V[2];
-                    finite = (isfinite(V[0]) && isfinite(V[1]) && isfinite(V[2])) ? 1 : 0;
-                }
-                V[0] = __shfl_sync(0xffffffffu, V[0], 0);
-                V[1] = __shfl_sync(0xffffffffu, V[1], 0);
-                V[2] = __shfl_sync(0xffffffffu, V[2], 0);
-                Vc[0] = __shfl_sync(0xffffffffu, Vc[0], 0);
-                Vc[1] = __shfl_sync(0xffffffffu, Vc[1], 0);
-                Vc[2] = __shfl_sync(0xffffffffu, Vc[2], 0);
-                finite = __shfl_sync(0xffffffffu, finite, 0);
-                if (!finite) {
+                // vertex = 3x3 solve of (edge plane, hit plane, face plane)
+                TS V[3];
+                TC Vc[3];
+                if (!warp_solve<TC, TS>(rows, e, bk, eqv, V, Vc, lane)) {
                     status = kSingular;
                     break;
                 }
-                // 0 append, 1 zero-length edge on e (merge), 2 zero-length closing edge
+                // 0 append, 1 zero-length edge on e (merge), 2 zero-length closing edge;
+                // decided in the solve precision (on the scan-precision copies
+                // where the rounding margin settles it)
                 int decision = 0;
                 if (n > 0) {
-                    const TS lx = __shfl_sync(0xffffffffu, vx, n - 1);
-                    const TS ly = __shfl_sync(0xffffffffu, vy, n - 1);
-                    const TS lz = __shfl_sync(0xffffffffu, vz, n - 1);
-                    if (lane == 0) { // in the solve precision, on one lane
-                        if (fabs(V[0] - lx) + fabs(V[1] - ly) + fabs(V[2] - lz) < same_eps)
-                            decision = 1;
-                        else if (bk == s && fabs(V[0] - vx) + fabs(V[1] - vy) + fabs(V[2] - vz) < same_eps)
-                            decision = 2;
+                    int s1 = -1, s2 = 0;
+                    if (sizeof(TS) > sizeof(TC)) {
+                        s1 = same_filter<TC, TS>(Vc, __shfl_sync(0xffffffffu, cx, n - 1),
+                                                 __shfl_sync(0xffffffffu, cy, n - 1),
+                                                 __shfl_sync(0xffffffffu, cz, n - 1), same_eps);
+                        if (bk == s && s1 == 0)
+                            s2 = same_filter<TC, TS>(Vc, __shfl_sync(0xffffffffu, cx, 0),
+                                                     __shfl_sync(0xffffffffu, cy, 0),
+                                                     __shfl_sync(0xffffffffu, cz, 0), same_eps);
                     }
-                    decision = __shfl_sync(0xffffffffu, decision, 0);
+                    if (s1 == 1) {
+                        decision = 1;
+                    } else if (s1 == 0 && s2 != -1) {
+                        decision = s2 == 1 ? 2 : 0;
+                    } else {
+                        const TS lx = __shfl_sync(0xffffffffu, vx, n - 1);
+                        const TS ly = __shfl_sync(0xffffffffu, vy, n - 1);
+                        const TS lz = __shfl_sync(0xffffffffu, vz, n - 1);
+                        if (lane == 0) { // in the solve precision, on one lane
+                            if (fabs(V[0] - lx) + fabs(V[1] - ly) + fabs(V[2] - lz) < same_eps)
+                                decision = 1;
+                            else if (bk == s && fabs(V[0] - vx) + fabs(V[1] - vy) + fabs(V[2] - vz) < same_eps)
+                                decision = 2;
+                        }
+                        decision = __shfl_sync(0xffffffffu, decision, 0);
+                    }
                 }
                 if (decision == 1 && lane == n - 1) ve = bk; // the edge on e has zero length
                 const bool appended = (decision == 0);
@@ -328,6 +366,9 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                         vx = V[0];
                         vy = V[1];
                         vz = V[2];
+                        cx = Vc[0];
+                        cy = Vc[1];
+                        cz = Vc[2];
                         ve = bk;
                     }
                     n++;

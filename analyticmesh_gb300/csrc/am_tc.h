@@ -10,24 +10,29 @@
 namespace am {
 
 // A weight pre-split into three bf16 terms (w = hi + mid + lo, 24 bits),
-// zero-padded to Mp (multiple of 128) rows x Kp (multiple of 64) columns,
-// row-major; the three planes are contiguous starting at `hi`.
+// zero-padded to Mp (multiple of 128) rows x Kp (multiple of 64) columns and
+// stored as the shared-memory image of its 128 x 64 blocks: block (mt, kb)
+// at (mt * Kp / 64 + kb) * kWBlockBytes holds the three terms 16 KB apart,
+// each K-major with the 128-byte swizzle, so one bulk copy stages it.
+constexpr int kWBlockBytes = 3 * 128 * 128;
+
 struct TcMat {
-    const __nv_bfloat16 *hi;
+    const uint8_t *blocks;
     int Mp, Kp;
 };
 
 struct TcNet {
     TcMat lin[kMaxLayers];              // linear i, 1 <= i <= n_lin - 2 (hidden outputs)
     TcMat skip[kMaxLayers][kMaxSkips];  // transforms from hidden layers into linear i
-    int ncols;                          // UMMA N = 4 x regions per CTA (multiple of 16, <= 256)
+    int ncols_max;                      // widest UMMA N = 4 x regions per CTA (multiple of 16, <= 256)
     int kp_max;                         // largest padded K of any operand
-    int tmem_cols;                      // TMEM columns per CTA (power of two)
+    int mtiles_max;                     // largest number of 128-row tiles of any layer
+    int nstage;                         // weight blocks in flight (1 or 2)
 };
 
-size_t tc_smem_bytes(const TcNet &tc, int W);
+size_t tc_smem_bytes(const TcNet &tc, int ncols, int W);
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,
                        int *d_err, cudaStream_t st);
-void launch_split_weights(const float *src, int M, int K, int Mp, int Kp, void *dst, cudaStream_t st);
+void launch_pack_weights(const float *src, int M, int K, int Mp, int Kp, void *dst, cudaStream_t st);
 
 } // namespace am
