@@ -31,6 +31,7 @@ class AmStats(C.Structure):
 AM_OPT_CHUNK = 1
 AM_OPT_PHASE_TIMING = 2
 AM_OPT_WELD = 3
+AM_OPT_GRAPH = 4
 
 
 class AmError(RuntimeError):

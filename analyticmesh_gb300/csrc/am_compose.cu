@@ -85,110 +85,115 @@ __global__ void __launch_bounds__(kThreads) compose_kernel(NetDev net, RegionsDe
     const int tid = threadIdx.x;
     const int r = tid & (kR - 1);
     const int g = tid >> 4;
-    const long long rl0 = (long long)blockIdx.x * kR;
-    const int nreg = (int)min((long long)kR, (long long)ch.count - rl0);
-    if (nreg <= 0) return;
+    long long head;
+    int count;
+    chunk_range(ch, head, count);
     const size_t rstride = (size_t)net.ALLP * 4;
-    T *cons = (T *)ch.cons + (size_t)rl0 * rstride;
-    const uint32_t *keys = reg.keys + (size_t)(ch.head + rl0) * net.W;
+    // tiles of kR regions, strided over the grid (the graph-driven loop
+    // launches a fixed grid; the host-driven one a tile per CTA)
+    for (long long rl0 = (long long)blockIdx.x * kR; rl0 < count; rl0 += (long long)gridDim.x * kR) {
+        const int nreg = (int)min((long long)kR, (long long)count - rl0);
+        T *cons = (T *)ch.cons + (size_t)rl0 * rstride;
+        const uint32_t *keys = reg.keys + (size_t)(head + rl0) * net.W;
 
-    // hidden layer 1 = linear 0 rows, sign-flipped; extra constraints as given
-    {
-        const T *W0 = (const T *)net.W0;
-        const T *b0 = (const T *)net.bias[0];
-        const int n1 = net.nodes[1];
-        for (int q = tid; q < nreg * n1; q += kThreads) {
-            const int rr = q / n1, m = q % n1;
-            const T sg = key_bit(keys + (size_t)rr * net.W, m) ? T(-1) : T(1);
-            vec4_t<T> c;
-            c.x = sg * W0[3 * m + 0];
-            c.y = sg * W0[3 * m + 1];
-            c.z = sg * W0[3 * m + 2];
-            c.w = sg * b0[m];
-            st4<T>(cons + (size_t)rr * rstride + (size_t)m * 4, c);
-        }
-        const T *we = (const T *)net.w_extra;
-        const T *be = (const T *)net.b_extra;
-        for (int q = tid; q < nreg * net.E; q += kThreads) {
-            const int rr = q / net.E, e = q % net.E;
-            vec4_t<T> c;
-            c.x = we[3 * e + 0];
-            c.y = we[3 * e + 1];
-            c.z = we[3 * e + 2];
-            c.w = be[e];
-            st4<T>(cons + (size_t)rr * rstride + (size_t)(net.N + e) * 4, c);
-        }
-    }
-
-    for (int i = 1; i < net.n_lin; ++i) {
-        const int M = net.nodes[i + 1];
-        const int K = net.nodes[i];
-        const bool last = (i == net.n_lin - 1);
-        const T *bias = (const T *)net.bias[i];
-        for (int mb = 0; mb < M; mb += kRowsPerPass) {
-            const int m0 = mb + 4 * g;
-            Acc<T> acc;
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc.v[j][c] = T(0);
-            accumulate<T>(X, cons, rstride, keys, net.W, nreg, net.hoff[i], K, (const T *)net.Wt[i], net.Mp[i], m0, acc);
-            for (int s = 0; s < net.nskip[i]; ++s) {
-                const SkipDev &sk = net.skip[i][s];
-                if (sk.kind == 1 && sk.from >= 1)
-                    accumulate<T>(X, cons, rstride, keys, net.W, nreg, net.hoff[sk.from], net.nodes[sk.from],
-                                  (const T *)sk.tmt, sk.Mp, m0, acc);
+        // hidden layer 1 = linear 0 rows, sign-flipped; extra constraints as given
+        {
+            const T *W0 = (const T *)net.W0;
+            const T *b0 = (const T *)net.bias[0];
+            const int n1 = net.nodes[1];
+            for (int q = tid; q < nreg * n1; q += kThreads) {
+                const int rr = q / n1, m = q % n1;
+                const T sg = key_bit(keys + (size_t)rr * net.W, m) ? T(-1) : T(1);
+                vec4_t<T> c;
+                c.x = sg * W0[3 * m + 0];
+                c.y = sg * W0[3 * m + 1];
+                c.z = sg * W0[3 * m + 2];
+                c.w = sg * b0[m];
+                st4<T>(cons + (size_t)rr * rstride + (size_t)m * 4, c);
             }
-            if (r < nreg) {
-                const uint32_t *key = keys + (size_t)r * net.W;
-                T *cr = cons + (size_t)r * rstride;
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    const int m = m0 + j;
-                    if (m >= M) continue;
-                    T v[4] = {acc.v[j][0], acc.v[j][1], acc.v[j][2], acc.v[j][3] + bias[m]};
-                    for (int s = 0; s < net.nskip[i]; ++s) {
-                        const SkipDev &sk = net.skip[i][s];
-                        if (sk.kind == 0) {
-                            if (sk.from == 0) {
-                                if (m < 3) v[m] += T(1);
-                            } else {
-                                const int row = net.hoff[sk.from] + m;
-                                if (key_bit(key, row)) {
-                                    const vec4_t<T> c = ld4<T>(cr + (size_t)row * 4);
-                                    v[0] -= c.x;
-                                    v[1] -= c.y;
-                                    v[2] -= c.z;
-                                    v[3] -= c.w;
+            const T *we = (const T *)net.w_extra;
+            const T *be = (const T *)net.b_extra;
+            for (int q = tid; q < nreg * net.E; q += kThreads) {
+                const int rr = q / net.E, e = q % net.E;
+                vec4_t<T> c;
+                c.x = we[3 * e + 0];
+                c.y = we[3 * e + 1];
+                c.z = we[3 * e + 2];
+                c.w = be[e];
+                st4<T>(cons + (size_t)rr * rstride + (size_t)(net.N + e) * 4, c);
+            }
+        }
+
+        for (int i = 1; i < net.n_lin; ++i) {
+            const int M = net.nodes[i + 1];
+            const int K = net.nodes[i];
+            const bool last = (i == net.n_lin - 1);
+            const T *bias = (const T *)net.bias[i];
+            for (int mb = 0; mb < M; mb += kRowsPerPass) {
+                const int m0 = mb + 4 * g;
+                Acc<T> acc;
+    #pragma unroll
+                for (int j = 0; j < 4; ++j)
+    #pragma unroll
+                    for (int c = 0; c < 4; ++c) acc.v[j][c] = T(0);
+                accumulate<T>(X, cons, rstride, keys, net.W, nreg, net.hoff[i], K, (const T *)net.Wt[i], net.Mp[i], m0, acc);
+                for (int s = 0; s < net.nskip[i]; ++s) {
+                    const SkipDev &sk = net.skip[i][s];
+                    if (sk.kind == 1 && sk.from >= 1)
+                        accumulate<T>(X, cons, rstride, keys, net.W, nreg, net.hoff[sk.from], net.nodes[sk.from],
+                                      (const T *)sk.tmt, sk.Mp, m0, acc);
+                }
+                if (r < nreg) {
+                    const uint32_t *key = keys + (size_t)r * net.W;
+                    T *cr = cons + (size_t)r * rstride;
+    #pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const int m = m0 + j;
+                        if (m >= M) continue;
+                        T v[4] = {acc.v[j][0], acc.v[j][1], acc.v[j][2], acc.v[j][3] + bias[m]};
+                        for (int s = 0; s < net.nskip[i]; ++s) {
+                            const SkipDev &sk = net.skip[i][s];
+                            if (sk.kind == 0) {
+                                if (sk.from == 0) {
+                                    if (m < 3) v[m] += T(1);
+                                } else {
+                                    const int row = net.hoff[sk.from] + m;
+                                    if (key_bit(key, row)) {
+                                        const vec4_t<T> c = ld4<T>(cr + (size_t)row * 4);
+                                        v[0] -= c.x;
+                                        v[1] -= c.y;
+                                        v[2] -= c.z;
+                                        v[3] -= c.w;
+                                    }
                                 }
+                            } else if (sk.from == 0) {
+                                const T *tt = (const T *)sk.tmt; // [3][Mp]
+                                v[0] += tt[m];
+                                v[1] += tt[(size_t)sk.Mp + m];
+                                v[2] += tt[2 * (size_t)sk.Mp + m];
                             }
-                        } else if (sk.from == 0) {
-                            const T *tt = (const T *)sk.tmt; // [3][Mp]
-                            v[0] += tt[m];
-                            v[1] += tt[(size_t)sk.Mp + m];
-                            v[2] += tt[2 * (size_t)sk.Mp + m];
                         }
-                    }
-                    vec4_t<T> o;
-                    if (!last) {
-                        const int row = net.hoff[i + 1] + m;
-                        const T sg = key_bit(key, row) ? T(-1) : T(1);
-                        o.x = sg * v[0];
-                        o.y = sg * v[1];
-                        o.z = sg * v[2];
-                        o.w = sg * v[3];
-                        st4<T>(cr + (size_t)row * 4, o);
-                    } else {
-                        o.x = v[0];
-                        o.y = v[1];
-                        o.z = v[2];
-                        o.w = v[3] - iso;
-                        st4<T>((T *)ch.eq + (size_t)(rl0 + r) * 4, o);
+                        vec4_t<T> o;
+                        if (!last) {
+                            const int row = net.hoff[i + 1] + m;
+                            const T sg = key_bit(key, row) ? T(-1) : T(1);
+                            o.x = sg * v[0];
+                            o.y = sg * v[1];
+                            o.z = sg * v[2];
+                            o.w = sg * v[3];
+                            st4<T>(cr + (size_t)row * 4, o);
+                        } else {
+                            o.x = v[0];
+                            o.y = v[1];
+                            o.z = v[2];
+                            o.w = v[3] - iso;
+                            st4<T>((T *)ch.eq + (size_t)(rl0 + r) * 4, o);
+                        }
                     }
                 }
             }
+            __syncthreads(); // layer i+1 rows written by this CTA become the next operand
         }
-        __syncthreads(); // layer i+1 rows written by this CTA become the next operand
     }
 }
 
@@ -207,8 +212,8 @@ __global__ void prepare_weights_kernel(const T *src, int M, int K, int Mp, T *ds
 
 void launch_compose(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, double iso, cudaStream_t st)
 {
-    if (ch.count <= 0) return;
-    const int grid = (ch.count + kR - 1) / kR;
+    if (!ch.ctl && ch.count <= 0) return;
+    const int grid = ch.ctl ? device_sms() * 4 : (ch.count + kR - 1) / kR;
     if (prec == kFloat64)
         compose_kernel<double><<<grid, kThreads, 0, st>>>(net, reg, ch, iso);
     else

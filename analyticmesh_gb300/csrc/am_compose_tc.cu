@@ -121,12 +121,14 @@ __device__ int total_blocks(const NetDev &net, const TcNet &tc)
 // Weight-block pipeline, driven by thread 0: stage h % nstage receives block
 // h once block h - nstage's products have completed (done barrier); block
 // h's products wait for its bytes (full barrier).  Phase parity of either
-// barrier for block h is (h / nstage) & 1.
+// barrier for block h is (h / nstage) & 1.  h counts on across the CTA's
+// tiles, so the next tile's first blocks load during this tile's last layer.
 struct WPipe {
     uint64_t *full, *done;
     uint8_t *ws;
     int nstage, total, issued;
     int *err;
+    int per_tile; // blocks one tile consumes; the sequence repeats per tile
 };
 
 __device__ __forceinline__ void wp_wait(WPipe &p, uint64_t *bar, uint32_t parity)
@@ -142,7 +144,8 @@ __device__ void wp_issue(WPipe &p, const NetDev &net, const TcNet &tc)
     const int h = p.issued, s = h % p.nstage;
     if (h >= p.nstage) wp_wait(p, p.done + s, (uint32_t)((h - p.nstage) / p.nstage) & 1u);
     umma::mbar_expect_tx(p.full + s, (uint32_t)kWBlockBytes);
-    umma::bulk_g2s(p.ws + (size_t)s * kWBlockBytes, block_ptr(net, tc, h), (uint32_t)kWBlockBytes, p.full + s);
+    umma::bulk_g2s(p.ws + (size_t)s * kWBlockBytes, block_ptr(net, tc, h % p.per_tile), (uint32_t)kWBlockBytes,
+                   p.full + s);
     p.issued = h + 1;
 }
 
@@ -207,21 +210,35 @@ __device__ __forceinline__ void gemm_observe(const WPipe &p, int last)
     umma::fence_after();
 }
 
+// tile width for a wave of `count` regions: one tile per SM while the wave
+// is small, the widest tile otherwise
+__host__ __device__ __forceinline__ int tile_cols(int count, int sms, int ncols_max)
+{
+    const int per = (count + sms - 1) / sms;
+    const int ncols = (4 * per + 15) / 16 * 16;
+    return ncols < 16 ? 16 : (ncols > ncols_max ? ncols_max : ncols);
+}
+
 __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcNet tc, RegionsDev reg, ChunkDev ch,
-                                                                  float iso, int ncols, int tmem_cols, int *err)
+                                                                  float iso, int sms, int *err)
 {
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint64_t bars[4];
     __shared__ uint32_t tslot;
     __shared__ int s_last;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    long long head;
+    int count;
+    chunk_range(ch, head, count);
+    if (count <= 0) return;
+    const int ncols = tile_cols(count, sms, tc.ncols_max);
     const int R = ncols / 4;
-    const long long rl0 = (long long)blockIdx.x * R;
-    const int nreg = (int)min((long long)R, (long long)ch.count - rl0);
-    if (nreg <= 0) return;
+    const int ntiles = (count + R - 1) / R;
+    const int mytiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (mytiles == 0) return;
+    int tmem_cols = 32;
+    while (tmem_cols < 2 * tc.mtiles_max * ncols) tmem_cols <<= 1;
     const size_t rstride = (size_t)net.ALLP * 4;
-    float *cons = (float *)ch.cons + (size_t)rl0 * rstride;
-    const uint32_t *gkeys = reg.keys + (size_t)(ch.head + rl0) * net.W;
 
     uint8_t *base = smem_raw + ((1024u - (umma::smem_addr(smem_raw) & 1023u)) & 1023u);
     const size_t xbytes = (size_t)ncols * tc.kp_max * 2; // one bf16 term of the operand
@@ -229,209 +246,218 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     uint8_t *ws = base + 3 * xbytes;                     // nstage weight blocks
     uint32_t *keys = reinterpret_cast<uint32_t *>(ws + (size_t)tc.nstage * kWBlockBytes); // the tile's bits
 
-    WPipe pp{bars, bars + 2, ws, tc.nstage, 0, 0, err};
+    WPipe pp{bars, bars + 2, ws, tc.nstage, 0, 0, err, 1};
     if (tid == 0) {
         for (int b = 0; b < 4; ++b) umma::mbar_init(bars + b, 1);
         umma::fence_mbar_init();
-        pp.total = total_blocks(net, tc);
+        pp.per_tile = total_blocks(net, tc);
+        pp.total = pp.per_tile * mytiles;
         // the first weight blocks do not depend on the tile: start them now
         while (pp.issued < pp.total && pp.issued < pp.nstage) wp_issue(pp, net, tc);
     }
     if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tmem_cols);
-    for (int q = tid; q < R * net.W; q += kThreads) keys[q] = q < nreg * net.W ? gkeys[q] : 0u;
-    __syncthreads(); // every thread reads every region's bits below
-
-    // hidden layer 1 = linear 0 rows (sign-flipped) and the extra constraints
-    {
-        const float *W0 = (const float *)net.W0;
-        const float *b0 = (const float *)net.bias[0];
-        const int n1 = net.nodes[1];
-        for (int q = tid; q < nreg * n1; q += kThreads) {
-            const int rr = q / n1, m = q % n1;
-            const float sg = key_bit(keys + (size_t)rr * net.W, m) ? -1.f : 1.f;
-            st4<float>(cons + (size_t)rr * rstride + (size_t)m * 4,
-                       make_float4(sg * W0[3 * m], sg * W0[3 * m + 1], sg * W0[3 * m + 2], sg * b0[m]));
-        }
-        const float *we = (const float *)net.w_extra;
-        const float *be = (const float *)net.b_extra;
-        for (int q = tid; q < nreg * net.E; q += kThreads) {
-            const int rr = q / net.E, e = q % net.E;
-            st4<float>(cons + (size_t)rr * rstride + (size_t)(net.N + e) * 4,
-                       make_float4(we[3 * e], we[3 * e + 1], we[3 * e + 2], be[e]));
-        }
-        // X_1 = diag(s_1) [W0 | b0]
-        const int Kp = (n1 + 63) / 64 * 64;
-        for (int q = tid; q < R * Kp; q += kThreads) {
-            const int r = q / Kp, k = q % Kp;
-            float x[4] = {0.f, 0.f, 0.f, 0.f};
-            if (r < nreg && k < n1 && key_bit(keys + (size_t)r * net.W, k)) {
-                x[0] = W0[3 * k];
-                x[1] = W0[3 * k + 1];
-                x[2] = W0[3 * k + 2];
-                x[3] = b0[k];
-            }
-#pragma unroll
-            for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), x[c]);
-        }
-    }
-    umma::fence_proxy_async();
-    umma::fence_before();
-    __syncthreads();
-    umma::fence_after();
-    const uint32_t tmem = tslot;
     int g = 0; // next weight block (thread 0)
     const int q4 = warp & 3, half = warp >> 2;
 
-    for (int i = 1; i <= net.n_lin - 2; ++i) {
-        const int M = net.nodes[i + 1];
-        const int mtiles = (M + 127) / 128;
-        if (tid == 0) gemm_issue(pp, net, tc, tc.lin[i], mtiles, xs, xbytes, ncols, tmem, true, g);
-        for (int s = 0; s < net.nskip[i]; ++s) {
-            const SkipDev &sk = net.skip[i][s];
-            if (tc_skip(sk)) {
-                // the operand is about to be overwritten: the products so far must be done
-                if (tid == 0) gemm_finish(pp, net, tc, g);
-                __syncthreads();
-                stage_x_from_rows(xs, xbytes, ncols, cons, rstride, keys, net.W, nreg, net.hoff[sk.from],
-                                  net.nodes[sk.from], tc.skip[i][s].Kp);
-                umma::fence_proxy_async();
-                __syncthreads();
-                if (tid == 0) gemm_issue(pp, net, tc, tc.skip[i][s], mtiles, xs, xbytes, ncols, tmem, false, g);
+    for (int j = 0; j < mytiles; ++j) {
+        const long long rl0 = (long long)(blockIdx.x + (long long)j * gridDim.x) * R;
+        const int nreg = (int)min((long long)R, (long long)count - rl0);
+        float *cons = (float *)ch.cons + (size_t)rl0 * rstride;
+        const uint32_t *gkeys = reg.keys + (size_t)(head + rl0) * net.W;
+        __syncthreads(); // the previous tile is done with the keys and the operand
+        for (int q = tid; q < R * net.W; q += kThreads) keys[q] = q < nreg * net.W ? gkeys[q] : 0u;
+        __syncthreads(); // every thread reads every region's bits below
+
+        // hidden layer 1 = linear 0 rows (sign-flipped) and the extra constraints
+        {
+            const float *W0 = (const float *)net.W0;
+            const float *b0 = (const float *)net.bias[0];
+            const int n1 = net.nodes[1];
+            for (int q = tid; q < nreg * n1; q += kThreads) {
+                const int rr = q / n1, m = q % n1;
+                const float sg = key_bit(keys + (size_t)rr * net.W, m) ? -1.f : 1.f;
+                st4<float>(cons + (size_t)rr * rstride + (size_t)m * 4,
+                           make_float4(sg * W0[3 * m], sg * W0[3 * m + 1], sg * W0[3 * m + 2], sg * b0[m]));
             }
-        }
-        if (tid == 0) {
-            gemm_finish(pp, net, tc, g);
-            s_last = g - 1;
-        }
-        __syncwarp();
-        __syncthreads();
-        gemm_observe(pp, s_last);
-        // epilogue: accumulators -> constraint rows (HBM) and the next operand (smem)
-        const float *bias = (const float *)net.bias[i];
-        const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
-        for (int q = tid; q < R * (Kn - M); q += kThreads) {
-            const int r = q / (Kn - M), k = M + q % (Kn - M);
-#pragma unroll
-            for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), 0.f);
-        }
-        for (int mt = 0; mt < mtiles; ++mt) {
-            const int m = mt * 128 + q4 * 32 + lane;
-            const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
-            const float bm = m < M ? bias[m] : 0.f;
-            const int row = net.hoff[i + 1] + m;
-            // byte offset of (n, k = m) for n = 0 (the swizzle adds n & 7)
-            const uint32_t kofs = (uint32_t)((m >> 6) * ncols * 128 + ((m & 7) << 1));
-            const int kchunk = (m & 63) >> 3;
-            for (int cb = half; cb < ncols / 16; cb += 2) {
-                float v[16], vc[16];
-                umma::tmem_ld16(lane_base + (uint32_t)(mt * ncols + cb * 16), v);
-                umma::tmem_ld16(lane_base + (uint32_t)((mtiles + mt) * ncols + cb * 16), vc);
-                if (m >= M) continue;
-#pragma unroll
-                for (int qq = 0; qq < 4; ++qq) {
-                    const int r = cb * 4 + qq;
-                    float x[4] = {0.f, 0.f, 0.f, 0.f};
-                    if (r < nreg) {
-                        const uint32_t *key = keys + (size_t)r * net.W;
-                        float *cr = cons + (size_t)r * rstride;
-                        float o[4] = {v[4 * qq] + vc[4 * qq], v[4 * qq + 1] + vc[4 * qq + 1],
-                                      v[4 * qq + 2] + vc[4 * qq + 2], v[4 * qq + 3] + vc[4 * qq + 3] + bm};
-                        for (int s = 0; s < net.nskip[i]; ++s) {
-                            const SkipDev &sk = net.skip[i][s];
-                            if (sk.kind == 0) {
-                                if (sk.from == 0) {
-                                    if (m < 3) o[m] += 1.f;
-                                } else {
-                                    const int srow = net.hoff[sk.from] + m;
-                                    if (key_bit(key, srow)) {
-                                        const float4 c = ld4<float>(cr + (size_t)srow * 4);
-                                        o[0] -= c.x;
-                                        o[1] -= c.y;
-                                        o[2] -= c.z;
-                                        o[3] -= c.w;
-                                    }
-                                }
-                            } else if (sk.from == 0) {
-                                const float *tt = (const float *)sk.tmt;
-                                o[0] += tt[m];
-                                o[1] += tt[(size_t)sk.Mp + m];
-                                o[2] += tt[2 * (size_t)sk.Mp + m];
-                            }
-                        }
-                        const bool act = key_bit(key, row);
-                        const float sg = act ? -1.f : 1.f;
-                        st4<float>(cr + (size_t)row * 4, make_float4(sg * o[0], sg * o[1], sg * o[2], sg * o[3]));
-                        if (act) {
-                            x[0] = o[0];
-                            x[1] = o[1];
-                            x[2] = o[2];
-                            x[3] = o[3];
-                        }
-                    }
-                    if (Kn > 0) {
-#pragma unroll
-                        for (int c = 0; c < 4; ++c) {
-                            const int n = 4 * r + c;
-                            put_split(xs, xbytes, kofs + (uint32_t)(n * 128) + (uint32_t)(((kchunk ^ (n & 7)) & 7) << 4),
-                                      x[c]);
-                        }
-                    }
+            const float *we = (const float *)net.w_extra;
+            const float *be = (const float *)net.b_extra;
+            for (int q = tid; q < nreg * net.E; q += kThreads) {
+                const int rr = q / net.E, e = q % net.E;
+                st4<float>(cons + (size_t)rr * rstride + (size_t)(net.N + e) * 4,
+                           make_float4(we[3 * e], we[3 * e + 1], we[3 * e + 2], be[e]));
+            }
+            // X_1 = diag(s_1) [W0 | b0]
+            const int Kp = (n1 + 63) / 64 * 64;
+            for (int q = tid; q < R * Kp; q += kThreads) {
+                const int r = q / Kp, k = q % Kp;
+                float x[4] = {0.f, 0.f, 0.f, 0.f};
+                if (r < nreg && k < n1 && key_bit(keys + (size_t)r * net.W, k)) {
+                    x[0] = W0[3 * k];
+                    x[1] = W0[3 * k + 1];
+                    x[2] = W0[3 * k + 2];
+                    x[3] = b0[k];
                 }
+    #pragma unroll
+                for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), x[c]);
             }
         }
         umma::fence_proxy_async();
         umma::fence_before();
         __syncthreads();
         umma::fence_after();
-    }
+        const uint32_t tmem = tslot;
 
-    // face plane: w_eq = W_L . X_L (+ b_L, + connections into the output layer)
-    // in fp32, one warp per region, from the operand in shared memory
-    // (hi + mid + lo is exact)
-    {
-        const int i = net.n_lin - 1;
-        const int K = net.nodes[i];
-        const float *wl = (const float *)net.Wt[i]; // [K][Mp], column 0
-        const int Mp = net.Mp[i];
-        const float bl = ((const float *)net.bias[i])[0];
-        for (int r = warp; r < nreg; r += kThreads / 32) {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
-            for (int k = lane; k < K; k += 32) {
-                const float w = __ldg(wl + (size_t)k * Mp);
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, get_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols)), acc[c]);
+        for (int i = 1; i <= net.n_lin - 2; ++i) {
+            const int M = net.nodes[i + 1];
+            const int mtiles = (M + 127) / 128;
+            if (tid == 0) gemm_issue(pp, net, tc, tc.lin[i], mtiles, xs, xbytes, ncols, tmem, true, g);
+            for (int s = 0; s < net.nskip[i]; ++s) {
+                const SkipDev &sk = net.skip[i][s];
+                if (tc_skip(sk)) {
+                    // the operand is about to be overwritten: the products so far must be done
+                    if (tid == 0) gemm_finish(pp, net, tc, g);
+                    __syncthreads();
+                    stage_x_from_rows(xs, xbytes, ncols, cons, rstride, keys, net.W, nreg, net.hoff[sk.from],
+                                      net.nodes[sk.from], tc.skip[i][s].Kp);
+                    umma::fence_proxy_async();
+                    __syncthreads();
+                    if (tid == 0) gemm_issue(pp, net, tc, tc.skip[i][s], mtiles, xs, xbytes, ncols, tmem, false, g);
+                }
             }
-#pragma unroll
-            for (int c = 0; c < 4; ++c)
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-            if (lane < 4) {
-                const int c = lane;
-                float a = c == 0 ? acc[0] : (c == 1 ? acc[1] : (c == 2 ? acc[2] : acc[3]));
-                const uint32_t *key = keys + (size_t)r * net.W;
-                const float *cr = cons + (size_t)r * rstride;
-                for (int s = 0; s < net.nskip[i]; ++s) {
-                    const SkipDev &sk = net.skip[i][s];
-                    if (sk.kind == 0) {
-                        if (sk.from >= 1 && net.nodes[sk.from] == 1 && key_bit(key, net.hoff[sk.from]))
-                            a -= cr[(size_t)net.hoff[sk.from] * 4 + c];
-                    } else if (sk.from == 0) {
-                        if (c < 3) a += ((const float *)sk.tmt)[(size_t)c * sk.Mp];
-                    } else {
-                        const float *tt = (const float *)sk.tmt; // [dec][Mp]
-                        const int hs = net.hoff[sk.from];
-                        for (int k = 0; k < net.nodes[sk.from]; ++k)
-                            if (key_bit(key, hs + k)) a -= tt[(size_t)k * sk.Mp] * cr[(size_t)(hs + k) * 4 + c];
+            if (tid == 0) {
+                gemm_finish(pp, net, tc, g);
+                s_last = g - 1;
+            }
+            __syncwarp();
+            __syncthreads();
+            gemm_observe(pp, s_last);
+            // epilogue: accumulators -> constraint rows (HBM) and the next operand (smem)
+            const float *bias = (const float *)net.bias[i];
+            const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
+            for (int q = tid; q < R * (Kn - M); q += kThreads) {
+                const int r = q / (Kn - M), k = M + q % (Kn - M);
+    #pragma unroll
+                for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), 0.f);
+            }
+            for (int mt = 0; mt < mtiles; ++mt) {
+                const int m = mt * 128 + q4 * 32 + lane;
+                const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
+                const float bm = m < M ? bias[m] : 0.f;
+                const int row = net.hoff[i + 1] + m;
+                // byte offset of (n, k = m) for n = 0 (the swizzle adds n & 7)
+                const uint32_t kofs = (uint32_t)((m >> 6) * ncols * 128 + ((m & 7) << 1));
+                const int kchunk = (m & 63) >> 3;
+                for (int cb = half; cb < ncols / 16; cb += 2) {
+                    float v[16], vc[16];
+                    umma::tmem_ld16(lane_base + (uint32_t)(mt * ncols + cb * 16), v);
+                    umma::tmem_ld16(lane_base + (uint32_t)((mtiles + mt) * ncols + cb * 16), vc);
+                    if (m >= M) continue;
+    #pragma unroll
+                    for (int qq = 0; qq < 4; ++qq) {
+                        const int r = cb * 4 + qq;
+                        float x[4] = {0.f, 0.f, 0.f, 0.f};
+                        if (r < nreg) {
+                            const uint32_t *key = keys + (size_t)r * net.W;
+                            float *cr = cons + (size_t)r * rstride;
+                            float o[4] = {v[4 * qq] + vc[4 * qq], v[4 * qq + 1] + vc[4 * qq + 1],
+                                          v[4 * qq + 2] + vc[4 * qq + 2], v[4 * qq + 3] + vc[4 * qq + 3] + bm};
+                            for (int s = 0; s < net.nskip[i]; ++s) {
+                                const SkipDev &sk = net.skip[i][s];
+                                if (sk.kind == 0) {
+                                    if (sk.from == 0) {
+                                        if (m < 3) o[m] += 1.f;
+                                    } else {
+                                        const int srow = net.hoff[sk.from] + m;
+                                        if (key_bit(key, srow)) {
+                                            const float4 c = ld4<float>(cr + (size_t)srow * 4);
+                                            o[0] -= c.x;
+                                            o[1] -= c.y;
+                                            o[2] -= c.z;
+                                            o[3] -= c.w;
+                                        }
+                                    }
+                                } else if (sk.from == 0) {
+                                    const float *tt = (const float *)sk.tmt;
+                                    o[0] += tt[m];
+                                    o[1] += tt[(size_t)sk.Mp + m];
+                                    o[2] += tt[2 * (size_t)sk.Mp + m];
+                                }
+                            }
+                            const bool act = key_bit(key, row);
+                            const float sg = act ? -1.f : 1.f;
+                            st4<float>(cr + (size_t)row * 4, make_float4(sg * o[0], sg * o[1], sg * o[2], sg * o[3]));
+                            if (act) {
+                                x[0] = o[0];
+                                x[1] = o[1];
+                                x[2] = o[2];
+                                x[3] = o[3];
+                            }
+                        }
+                        if (Kn > 0) {
+    #pragma unroll
+                            for (int c = 0; c < 4; ++c) {
+                                const int n = 4 * r + c;
+                                put_split(xs, xbytes, kofs + (uint32_t)(n * 128) + (uint32_t)(((kchunk ^ (n & 7)) & 7) << 4),
+                                          x[c]);
+                            }
+                        }
                     }
                 }
-                if (c == 3) a += bl - iso;
-                ((float *)ch.eq)[(size_t)(rl0 + r) * 4 + c] = a;
+            }
+            umma::fence_proxy_async();
+            umma::fence_before();
+            __syncthreads();
+            umma::fence_after();
+        }
+
+        // face plane: w_eq = W_L . X_L (+ b_L, + connections into the output layer)
+        // in fp32, one warp per region, from the operand in shared memory
+        // (hi + mid + lo is exact)
+        {
+            const int i = net.n_lin - 1;
+            const int K = net.nodes[i];
+            const float *wl = (const float *)net.Wt[i]; // [K][Mp], column 0
+            const int Mp = net.Mp[i];
+            const float bl = ((const float *)net.bias[i])[0];
+            for (int r = warp; r < nreg; r += kThreads / 32) {
+                float acc[4] = {0.f, 0.f, 0.f, 0.f};
+                for (int k = lane; k < K; k += 32) {
+                    const float w = __ldg(wl + (size_t)k * Mp);
+    #pragma unroll
+                    for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, get_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols)), acc[c]);
+                }
+    #pragma unroll
+                for (int c = 0; c < 4; ++c)
+    #pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+                if (lane < 4) {
+                    const int c = lane;
+                    float a = c == 0 ? acc[0] : (c == 1 ? acc[1] : (c == 2 ? acc[2] : acc[3]));
+                    const uint32_t *key = keys + (size_t)r * net.W;
+                    const float *cr = cons + (size_t)r * rstride;
+                    for (int s = 0; s < net.nskip[i]; ++s) {
+                        const SkipDev &sk = net.skip[i][s];
+                        if (sk.kind == 0) {
+                            if (sk.from >= 1 && net.nodes[sk.from] == 1 && key_bit(key, net.hoff[sk.from]))
+                                a -= cr[(size_t)net.hoff[sk.from] * 4 + c];
+                        } else if (sk.from == 0) {
+                            if (c < 3) a += ((const float *)sk.tmt)[(size_t)c * sk.Mp];
+                        } else {
+                            const float *tt = (const float *)sk.tmt; // [dec][Mp]
+                            const int hs = net.hoff[sk.from];
+                            for (int k = 0; k < net.nodes[sk.from]; ++k)
+                                if (key_bit(key, hs + k)) a -= tt[(size_t)k * sk.Mp] * cr[(size_t)(hs + k) * 4 + c];
+                        }
+                    }
+                    if (c == 3) a += bl - iso;
+                    ((float *)ch.eq)[(size_t)(rl0 + r) * 4 + c] = a;
+                }
             }
         }
-    }
+    } // tiles
     umma::fence_before();
     __syncthreads();
-    if (warp == 0) umma::tmem_dealloc(tmem, (uint32_t)tmem_cols);
+    if (warp == 0) umma::tmem_dealloc(tslot, (uint32_t)tmem_cols);
 }
 
 // src (M x K fp32, row-major) -> three bf16 terms as the shared-memory image
@@ -456,7 +482,9 @@ __global__ void pack_weights_kernel(const float *src, int M, int K, int Mp, int 
     }
 }
 
-int sm_count()
+} // namespace
+
+int device_sms()
 {
     static int sms[64] = {};
     int dev = 0;
@@ -470,8 +498,6 @@ int sm_count()
     return sms[dev];
 }
 
-} // namespace
-
 size_t tc_smem_bytes(const TcNet &tc, int ncols, int W)
 {
     return 1024 + 3 * (size_t)ncols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(ncols / 4) * W * 4;
@@ -480,20 +506,19 @@ size_t tc_smem_bytes(const TcNet &tc, int ncols, int W)
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,
                        int *d_err, cudaStream_t st)
 {
-    if (ch.count <= 0) return;
-    // one tile per SM when the chunk is small, the widest tile otherwise
-    const int sms = sm_count();
-    const int per = (ch.count + sms - 1) / sms;
-    int ncols = (4 * per + 15) / 16 * 16;
-    ncols = std::max(16, std::min(ncols, tc.ncols_max));
-    int tcols = 32;
-    while (tcols < 2 * tc.mtiles_max * ncols) tcols <<= 1;
+    if (!ch.ctl && ch.count <= 0) return;
+    const int sms = device_sms();
+    const size_t smem_max = tc_smem_bytes(tc, tc.ncols_max, net.W);
+    cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+    if (ch.ctl) { // wave size known on the device only: a CTA per SM, tiles strided
+        compose_tc_kernel<<<sms, kThreads, smem_max, st>>>(net, tc, reg, ch, (float)iso, sms, d_err);
+        return;
+    }
+    const int ncols = tile_cols(ch.count, sms, tc.ncols_max);
     const int R = ncols / 4;
     const int grid = (ch.count + R - 1) / R;
-    const size_t smem = tc_smem_bytes(tc, ncols, net.W);
-    cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)tc_smem_bytes(tc, tc.ncols_max, net.W));
-    compose_tc_kernel<<<grid, kThreads, smem, st>>>(net, tc, reg, ch, (float)iso, ncols, tcols, d_err);
+    compose_tc_kernel<<<grid, kThreads, tc_smem_bytes(tc, ncols, net.W), st>>>(net, tc, reg, ch, (float)iso, sms,
+                                                                              d_err);
 }
 
 void launch_pack_weights(const float *src, int M, int K, int Mp, int Kp, void *dst, cudaStream_t st)

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -148,7 +149,15 @@ struct am_engine {
     // seeds
     DevBuf s_states, s_keys, s_hash, s_pts, s_rec;
     // counters
-    DevBuf d_tail, d_err;
+    // wave control block (region tail, error bits, the graph-driven loop's
+    // queue state), read back with one copy into pinned host memory
+    DevBuf d_tail; // the WaveCtl; tail at offset 0
+    struct {
+        void *p = nullptr;
+        template <typename T> T *as() const { return (T *)p; }
+    } d_err;
+    WaveCtl *h_ctl = nullptr;
+    bool use_graph = true;
     // results
     bool has_am = false, has_mesh = false;
     long long num_regions = 0;
@@ -163,6 +172,7 @@ struct am_engine {
     ~am_engine()
     {
         if (own) cudaStreamDestroy(own);
+        if (h_ctl) cudaFreeHost(h_ctl);
     }
 
     RegionsDev regions() const
@@ -233,22 +243,77 @@ struct am_engine {
         return (int)c;
     }
 
-    long long read_tail()
+    // one copy of (tail, error bits) after the work queued so far; throws on errors
+    long long poll(size_t bytes = 16)
     {
-        long long t = 0;
-        AM_CUDA(cudaMemcpyAsync(&t, d_tail.p, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaMemcpyAsync(h_ctl, d_tail.p, bytes, cudaMemcpyDeviceToHost, st));
         AM_CUDA(cudaStreamSynchronize(st));
-        return t;
-    }
-
-    void check_err()
-    {
-        int e = 0;
-        AM_CUDA(cudaMemcpyAsync(&e, d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-        AM_CUDA(cudaStreamSynchronize(st));
+        const int e = h_ctl->err;
         if (e & kErrTableFull) throw Failure{AM_ERR_TABLE_FULL, "hash probe bound reached"};
         if (e & kErrCapacity) throw Failure{AM_ERR_CAPACITY, "region store capacity exceeded"};
+        return h_ctl->tail;
     }
+    WaveCtl *ctl() const { return (WaveCtl *)d_tail.p; }
+
+    // Capture one wave -- composition, polygons, append, step -- as the body
+    // of a conditional while node and run the graph once on the stream.  The
+    // kernels read the wave's range from the control block, so the captured
+    // launches serve every wave.
+    void run_wave_graph(int prec, const NetDev &net, double iso, const Tolerances &tol, int chunk)
+    {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        auto cleanup = [&] {
+            if (exec) cudaGraphExecDestroy(exec);
+            if (graph) cudaGraphDestroy(graph);
+        };
+        try {
+            AM_CUDA(cudaGraphCreate(&graph, 0));
+            cudaGraphConditionalHandle cond;
+            AM_CUDA(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
+            cudaGraphNodeParams np = {};
+            np.type = cudaGraphNodeTypeConditional;
+            np.conditional.handle = cond;
+            np.conditional.type = cudaGraphCondTypeWhile;
+            np.conditional.size = 1;
+            cudaGraphNode_t node;
+            AM_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np));
+            cudaGraph_t body = np.conditional.phGraph_out[0];
+            AM_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+            ChunkDev ch;
+            ch.head = 0;
+            ch.count = chunk;
+            ch.cons = cons.p;
+            ch.eq = eq.p;
+            ch.rec = rec.as<int32_t>();
+            ch.ctl = ctl();
+            const RegionsDev reg = regions();
+            const HashDev hs = hashdev();
+            if (prec == kMixed)
+                launch_compose_tc(net, tcnet, reg, ch, iso, d_err.as<int>(), st);
+            else
+                launch_compose(prec, net, reg, ch, iso, st);
+            launch_polygon(prec, net, reg, ch, hs, tol, d_err.as<int>(), st);
+            launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, chunk * kVMax, d_tail.as<long long>(),
+                          blocksum.as<int>(), (int)(blocksum.bytes / sizeof(int)), d_err.as<int>(), st);
+            launch_wave_step(ctl(), cond, st);
+            cudaGraph_t captured = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(st, &captured);
+            AM_CUDA(ce);
+            AM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+            AM_CUDA(cudaGraphLaunch(exec, st));
+        } catch (...) {
+            cudaStreamCaptureStatus cs;
+            if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+                cudaGraph_t g2 = nullptr;
+                cudaStreamEndCapture(st, &g2);
+            }
+            cleanup();
+            throw;
+        }
+        cleanup(); // destroying a launched exec is stream-ordered-safe
+    }
+    void check_err() { poll(); }
 };
 
 namespace {
@@ -340,8 +405,11 @@ int am_init(am_engine **out, const char *float_type, const int32_t *nodesnum, in
                  "too many constraint rows for one face (sum of hidden widths + extra constraints)");
         AM_CUDA(cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking));
         e->st = e->own;
-        AM_CUDA(e->d_tail.alloc(sizeof(long long)));
-        AM_CUDA(e->d_err.alloc(sizeof(int)));
+        AM_CUDA(e->d_tail.alloc(sizeof(WaveCtl)));
+        AM_CUDA(cudaMemset(e->d_tail.p, 0, sizeof(WaveCtl)));
+        e->d_err.p = &((WaveCtl *)e->d_tail.p)->err;
+        AM_CUDA(cudaHostAlloc((void **)&e->h_ctl, sizeof(WaveCtl), cudaHostAllocDefault));
+        memset(e->h_ctl, 0, sizeof(WaveCtl));
     });
     if (rc == AM_OK) *out = e.release();
     return rc;
@@ -362,6 +430,10 @@ int am_set_option(am_engine *e, int option, int64_t value)
     if (option == AM_OPT_WELD) {
         if (value != 0 && value != 1) return AM_ERR_INVALID_ARGUMENT;
         e->weld_mode = (int)value;
+        return AM_OK;
+    }
+    if (option == AM_OPT_GRAPH) {
+        e->use_graph = value != 0;
         return AM_OK;
     }
     return AM_ERR_INVALID_ARGUMENT;
@@ -572,8 +644,7 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
         }
         launches += 5;
         AM_CUDA(cudaGetLastError());
-        long long tail = e->read_tail();
-        e->check_err();
+        long long tail = e->poll();
         e->num_regions = tail;
         e->stats.num_seeds = tail;
 
@@ -581,6 +652,35 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
         long long head = 0;
         int chunks = 0;
         double t_comp = 0, t_poly = 0, t_front = 0;
+        if (e->use_graph && !e->phase_timing) {
+            // graph-driven loop: one graph launch runs every wave until the
+            // queue is empty; it stops early only when the next wave's
+            // children might not fit, and then resumes after the host grows
+            // the region store and the table
+            e->ensure_chunk(chunk);
+            while (head < tail) {
+                const int count = (int)std::min<long long>(tail - head, chunk);
+                e->ensure_regions(tail + (long long)count * kVMax);
+                e->ensure_table(std::max<long long>(tail + (long long)count * kVMax, e->cap), true);
+                WaveCtl *h = e->h_ctl;
+                h->head = head;
+                h->count = count;
+                h->waves = 0;
+                h->limit = std::min<long long>(e->cap, (long long)(e->hcap / 2));
+                h->chunk_cap = chunk;
+                h->work = 0u;
+                // tail and err stay as the device has them
+                AM_CUDA(cudaMemcpyAsync((char *)e->d_tail.p + offsetof(WaveCtl, head), (char *)h + offsetof(WaveCtl, head),
+                                        sizeof(WaveCtl) - offsetof(WaveCtl, head), cudaMemcpyHostToDevice, st));
+                e->run_wave_graph(prec, net, iso, tol, chunk);
+                tail = e->poll(sizeof(WaveCtl));
+                chunks += h->waves;
+                launches += 6ll * h->waves;
+                head = h->head;
+                e->num_regions = tail;
+                AM_CHECK(h->waves < kMaxWaves, "wave bound reached");
+            }
+        }
         while (head < tail) {
             const int count = (int)std::min<long long>(tail - head, chunk);
             e->ensure_chunk(count);
@@ -626,10 +726,9 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             launches += 5;
             AM_CUDA(cudaGetLastError());
             head += count;
-            tail = e->read_tail();
+            tail = e->poll();
             e->num_regions = tail;
             chunks++;
-            e->check_err();
         }
         AM_CUDA(cudaEventRecord(ev1, st));
         AM_CUDA(cudaEventSynchronize(ev1));

@@ -10,6 +10,7 @@
 // New regions are appended in candidate order: winners of the insert are
 // flagged, counted per block, scanned, and written at tail + prefix, so the
 // region ids of a run do not depend on thread scheduling.
+#include <algorithm>
 #include <cuda/atomic>
 #include <cuda_runtime.h>
 
@@ -127,9 +128,29 @@ struct AppendArgs {
     int *err;
 };
 
-__device__ __forceinline__ int is_winner(const AppendArgs &a, int q)
+// items of this append: head of the chunk and the number of candidates, from
+// the launch or (graph-driven loop) from the wave control block
+__device__ __forceinline__ void append_range(const AppendArgs &a, long long &head, int &n)
 {
-    if (q >= a.n_items) return 0;
+    if (a.ch.ctl) {
+        head = *(volatile const long long *)&a.ch.ctl->head;
+        n = *(volatile const int *)&a.ch.ctl->count * kVMax;
+    } else {
+        head = a.ch.head;
+        n = a.n_items;
+    }
+}
+
+// block b scans items [b * span, (b + 1) * span) in tiles of kScanBlock
+__device__ __forceinline__ int block_span(int n)
+{
+    const int tiles = (n + kScanBlock - 1) / kScanBlock;
+    return (tiles + (int)gridDim.x - 1) / (int)gridDim.x * kScanBlock;
+}
+
+__device__ __forceinline__ int is_winner(const AppendArgs &a, int q, long long head, int n)
+{
+    if (q >= n) return 0;
     const int rec = a.ch.rec[q];
     if (rec < 0) return 0;
     uint32_t myid;
@@ -138,7 +159,7 @@ __device__ __forceinline__ int is_winner(const AppendArgs &a, int q)
     } else {
         const long long rl = q / kVMax;
         const int i = q % kVMax;
-        const int k = a.reg.edges[(size_t)(a.ch.head + rl) * kVMax + i];
+        const int k = a.reg.edges[(size_t)(head + rl) * kVMax + i];
         myid = (uint32_t)(rl * a.net.ALL + k);
     }
     const unsigned long long cur = load_slot(a.hs.slots + rec);
@@ -147,11 +168,18 @@ __device__ __forceinline__ int is_winner(const AppendArgs &a, int q)
 
 __global__ void __launch_bounds__(kScanBlock) append_count_kernel(AppendArgs a)
 {
-    const int q = blockIdx.x * kScanBlock + threadIdx.x;
-    int total;
-    const int f = is_winner(a, q);
-    block_exclusive_scan(f, &total);
-    if (threadIdx.x == 0) a.blockoff[blockIdx.x] = total;
+    long long head;
+    int n;
+    append_range(a, head, n);
+    const int span = block_span(n);
+    const int q1 = min(n, (int)blockIdx.x * span + span);
+    int sum = 0;
+    for (int q0 = (int)blockIdx.x * span; q0 < q1; q0 += kScanBlock) {
+        int total;
+        block_exclusive_scan(is_winner(a, q0 + (int)threadIdx.x, head, n), &total);
+        sum += total;
+    }
+    if (threadIdx.x == 0) a.blockoff[blockIdx.x] = sum;
 }
 
 __global__ void __launch_bounds__(kScanBlock) append_offsets_kernel(AppendArgs a, int nblocks)
@@ -173,14 +201,8 @@ __global__ void __launch_bounds__(kScanBlock) append_offsets_kernel(AppendArgs a
 }
 
 template <typename TS>
-__global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
+__device__ void append_one(const AppendArgs &a, int q, long long rid, long long head)
 {
-    const int q = blockIdx.x * kScanBlock + threadIdx.x;
-    int total;
-    const int f = is_winner(a, q);
-    const int pre = block_exclusive_scan(f, &total);
-    if (!f) return;
-    const long long rid = (long long)a.blockoff[blockIdx.x] + pre;
     if (rid >= a.reg.cap) {
         atomicOr(a.err, kErrCapacity);
         return;
@@ -200,7 +222,7 @@ __global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
         mid[3] = TS(0);
         a.reg.start[rid] = -1;
     } else {
-        const long long parent = a.ch.head + q / kVMax;
+        const long long parent = head + q / kVMax;
         const int i = q % kVMax;
         const int k = a.reg.edges[(size_t)parent * kVMax + i];
         const uint32_t *pk = a.reg.keys + (size_t)parent * W;
@@ -220,6 +242,40 @@ __global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
     a.reg.nv[rid] = 0;
     a.reg.status[rid] = 0;
     a.hs.slots[a.ch.rec[q]] = slot_value(fp_of(h), 0, (uint32_t)rid);
+}
+
+template <typename TS>
+__global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
+{
+    long long head;
+    int n;
+    append_range(a, head, n);
+    const int span = block_span(n);
+    const int q1 = min(n, (int)blockIdx.x * span + span);
+    long long base = a.blockoff[blockIdx.x];
+    for (int q0 = (int)blockIdx.x * span; q0 < q1; q0 += kScanBlock) {
+        const int q = q0 + (int)threadIdx.x;
+        int total;
+        const int f = is_winner(a, q, head, n);
+        const int pre = block_exclusive_scan(f, &total);
+        if (f) append_one<TS>(a, q, base + pre, head);
+        base += total;
+    }
+}
+
+// graph-driven loop: retire the wave, take the next one from the queue and
+// go on while it is non-empty, no fatal error is set and its children fit
+__global__ void wave_step_kernel(WaveCtl *ctl, cudaGraphConditionalHandle cond)
+{
+    WaveCtl &c = *ctl;
+    if (c.count > 0) c.waves++;
+    c.head += c.count;
+    const long long rem = c.tail - c.head;
+    c.count = (int)(rem < (long long)c.chunk_cap ? (rem > 0 ? rem : 0) : (long long)c.chunk_cap);
+    c.work = 0u;
+    const bool go = c.count > 0 && (c.err & (kErrTableFull | kErrCapacity)) == 0 &&
+                    c.tail + (long long)c.count * kVMax <= c.limit && c.waves < kMaxWaves;
+    cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 
 __global__ void rehash_kernel(RegionsDev reg, long long n, HashDev hs, int *err)
@@ -265,11 +321,12 @@ void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg,
     a.seed_keys = seed_keys;
     a.seed_hash = seed_hash;
     a.seed_points = seed_points;
-    a.n_items = n_items;
+    a.n_items = n_items; // graph-driven loop: the largest wave's candidates
     a.tail = d_tail;
     a.blockoff = d_blocksum;
     a.err = d_err;
-    const int nb = (n_items + kScanBlock - 1) / kScanBlock;
+    int nb = (n_items + kScanBlock - 1) / kScanBlock;
+    if (ch.ctl) nb = std::min(nb, 2 * device_sms()); // several tiles per block
     if (nb > nblocks_cap) { // the host sizes d_blocksum for the largest chunk
         int e = kErrCapacity;
         cudaMemcpyAsync(d_err, &e, sizeof(int), cudaMemcpyHostToDevice, st);
@@ -281,6 +338,11 @@ void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg,
         append_write_kernel<float><<<nb, kScanBlock, 0, st>>>(a);
     else
         append_write_kernel<double><<<nb, kScanBlock, 0, st>>>(a);
+}
+
+void launch_wave_step(WaveCtl *ctl, cudaGraphConditionalHandle cond, cudaStream_t st)
+{
+    wave_step_kernel<<<1, 1, 0, st>>>(ctl, cond);
 }
 
 void launch_rehash(const RegionsDev &reg, long long n, const HashDev &hs, int *d_err, cudaStream_t st)

@@ -14,6 +14,7 @@ constexpr int kWalkSteps = 96;   // bound on walk iterations (vertices + merges)
 constexpr int kTopK = 64;        // seed start search: pairs x <= 812 use the 57 nearest planes
 constexpr int kMaxProbes = 4096; // hash probe bound
 constexpr uint64_t kEmpty = ~0ull;
+constexpr int kMaxWaves = 1 << 20; // bound on the waves of one graph launch
 
 enum Precision : int { kFloat32 = 0, kFloat64 = 1, kMixed = 2 };
 
@@ -64,13 +65,44 @@ struct HashDev {
     unsigned long long mask;
 };
 
+// Wave control block in device memory.  The host-driven loop reads tail and
+// err after every wave; the graph-driven loop keeps head and count here too,
+// so the kernels of a captured wave read their range from the device and a
+// one-thread step kernel advances the queue and decides whether to go on.
+struct WaveCtl {
+    long long tail;     // regions in the store (appends advance it)
+    int err;            // device error bits
+    int pad0;
+    long long head;     // first region of the current wave (graph-driven loop)
+    int count;          // regions in the current wave
+    int waves;          // waves completed
+    long long limit;    // go on only while tail + count * kVMax <= limit
+    int chunk_cap;      // largest wave
+    unsigned int work;  // next region of the wave for the polygon warps
+};
+
 struct ChunkDev {
     long long head;     // first rid of the chunk
     int count;          // regions in the chunk
     void *cons;         // [count][ALLP][4] TC constraint rows
     void *eq;           // [count][4] TC face plane (b already offset by iso)
     int32_t *rec;       // [count * kVMax] hash slot claimed by each child, -1 none
+    WaveCtl *ctl = nullptr; // set: head and count come from the device (graph-driven loop)
 };
+
+#ifdef __CUDACC__
+// the wave's range, from the launch or from the device
+__device__ __forceinline__ void chunk_range(const ChunkDev &ch, long long &head, int &count)
+{
+    if (ch.ctl) {
+        head = *(volatile const long long *)&ch.ctl->head;
+        count = *(volatile const int *)&ch.ctl->count;
+    } else {
+        head = ch.head;
+        count = ch.count;
+    }
+}
+#endif
 
 struct Tolerances {
     double eps;         // feasibility (geometric distance), reference FP_EPS
@@ -91,6 +123,9 @@ void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg,
                    const HashDev &hs, const uint32_t *seed_keys, const uint64_t *seed_hash, const void *seed_points,
                    int n_items, long long *d_tail, int *d_blocksum, int nblocks_cap, int *d_err, cudaStream_t st);
 void launch_rehash(const RegionsDev &reg, long long n, const HashDev &hs, int *d_err, cudaStream_t st);
+// graph-driven loop: advance ctl to the next wave and set the loop condition
+void launch_wave_step(WaveCtl *ctl, cudaGraphConditionalHandle cond, cudaStream_t st);
+int device_sms();
 void launch_prepare_weights(int prec, const void *src, int M, int K, int Mp, void *dst, cudaStream_t st);
 
 // mesh weld (CombineMesh)

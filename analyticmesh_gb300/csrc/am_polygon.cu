@@ -121,6 +121,13 @@ __device__ __forceinline__ int same_filter(const TC *Vc, TC px, TC py, TC pz, TS
     return -1;
 }
 
+__device__ __forceinline__ long long next_work(WaveCtl *ctl, int lane)
+{
+    unsigned int v = 0;
+    if (lane == 0) v = atomicAdd(&ctl->work, 1u);
+    return (long long)__shfl_sync(0xffffffffu, v, 0);
+}
+
 __device__ __forceinline__ unsigned long long load_slot(const unsigned long long *p)
 {
     cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> a(*const_cast<unsigned long long *>(p));
@@ -174,14 +181,20 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
     const TC eps = (TC)tol.eps, par_eps = (TC)tol.par_eps;
     const TS same_eps = (TS)tol.same_eps;
 
-    for (long long rl = (long long)blockIdx.x * wpb + wib; rl < ch.count; rl += (long long)gridDim.x * wpb) {
-        const long long rid = ch.head + rl;
+    long long head;
+    int count;
+    chunk_range(ch, head, count);
+    // a region per warp: by launch position, or (fixed grid of the
+    // graph-driven loop) from the wave's work counter
+    for (long long rl = ch.ctl ? next_work(ch.ctl, lane) : (long long)blockIdx.x * wpb + wib; rl < count;
+         rl = ch.ctl ? next_work(ch.ctl, lane) : rl + (long long)gridDim.x * wpb) {
+        const long long rid = head + rl;
         const vec4_t<TC> *grows = reinterpret_cast<const vec4_t<TC> *>((const TC *)ch.cons + (size_t)rl * net.ALLP * 4);
         for (int q = lane; q < ALL; q += 32) {
             vec4_t<TC> v = grows[q];
             const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
             if (n2 > TC(0)) {
-                const TC inv = TC(1) / sqrt(n2);
+                const TC inv = rsqrt(n2); // as the reference's distance normalisation
                 v.x *= inv;
                 v.y *= inv;
                 v.z *= inv;
@@ -291,19 +304,34 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                 const TC c0 = curc[0], c1 = curc[1], c2 = curc[2];
                 // first hit along the edge line: min over crossing planes of
                 // t = max(0, -g) / a, compared as fractions
-                TC bnum = TC(1), bden = TC(0);
-                int bk = 0x7fffffff;
-                for (int k = lane; k < ALL; k += 32) {
+                // (two interleaved candidates per lane halve the compare chain)
+                TC bnum = TC(1), bden = TC(0), bnum1 = TC(1), bden1 = TC(0);
+                int bk = 0x7fffffff, bk1 = 0x7fffffff;
+                auto consider = [&](int k, TC &bn, TC &bd, int &bi) {
                     const vec4_t<TC> r = rows[k];
                     const TC a = r.x * d0 + r.y * d1 + r.z * d2;
-                    if (!(a > thr) || k == e || k == prev) continue;
+                    if (!(a > thr) || k == e || k == prev) return;
                     TC num = -(r.x * c0 + r.y * c1 + r.z * c2 + r.w);
                     num = num > TC(0) ? num : TC(0);
-                    const TC lhs = num * bden, rhs = bnum * a;
-                    if (lhs < rhs || (lhs == rhs && k < bk)) {
-                        bnum = num;
-                        bden = a;
-                        bk = k;
+                    const TC lhs = num * bd, rhs = bn * a;
+                    if (lhs < rhs || (lhs == rhs && k < bi)) {
+                        bn = num;
+                        bd = a;
+                        bi = k;
+                    }
+                };
+                int k = lane;
+                for (; k + 32 < ALL; k += 64) {
+                    consider(k, bnum, bden, bk);
+                    consider(k + 32, bnum1, bden1, bk1);
+                }
+                if (k < ALL) consider(k, bnum, bden, bk);
+                {
+                    const TC lhs = bnum1 * bden, rhs = bnum * bden1;
+                    if (bk1 != 0x7fffffff && (lhs < rhs || (lhs == rhs && bk1 < bk))) {
+                        bnum = bnum1;
+                        bden = bden1;
+                        bk = bk1;
                     }
                 }
                 TC bt = bk == 0x7fffffff ? TC(INFINITY) : bnum / bden;
@@ -425,7 +453,7 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
                     }
                     cur = old;
                 }
-                if ((uint32_t)(cur >> 32) == fp && key_matches(cur, reg, ch.head, ALL, W, pkey, k)) {
+                if ((uint32_t)(cur >> 32) == fp && key_matches(cur, reg, head, ALL, W, pkey, k)) {
                     if ((cur >> 31) & 1ull) {
                         atomicMin(hs.slots + slot, mine);
                         rec = (int)slot;
@@ -443,31 +471,38 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
 
 } // namespace
 
+template <typename TC, typename TS>
+void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs, const Tolerances &tol,
+                int *d_err, int wpb, size_t smem, cudaStream_t st)
+{
+    auto k = polygon_kernel<TC, TS>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    const int sms = device_sms();
+    int grid;
+    if (ch.ctl) { // wave size on the device: as many blocks as stay resident
+        int per_sm = 1;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32 * wpb, smem);
+        grid = sms * std::max(per_sm, 1);
+    } else {
+        const long long need = (ch.count + wpb - 1) / wpb;
+        grid = (int)std::min<long long>(need, (long long)sms * 16);
+    }
+    k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err);
+}
+
 void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs,
                     const Tolerances &tol, int *d_err, cudaStream_t st)
 {
-    if (ch.count <= 0) return;
+    if (!ch.ctl && ch.count <= 0) return;
     const size_t row_bytes = (prec == kFloat64 ? sizeof(double4) : sizeof(float4)) * (size_t)net.ALLP;
     const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96u * 1024u) / std::max<size_t>(row_bytes, 1)));
     const size_t smem = row_bytes * wpb; // the host rejects networks whose rows do not fit (am_init)
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    const long long need = (ch.count + wpb - 1) / wpb;
-    const int grid = (int)std::min<long long>(need, (long long)sms * 16);
-    if (prec == kFloat64) {
-        auto k = polygon_kernel<double, double>;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err);
-    } else if (prec == kMixed) {
-        auto k = polygon_kernel<float, double>;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err);
-    } else {
-        auto k = polygon_kernel<float, float>;
-        if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err);
-    }
+    if (prec == kFloat64)
+        launch_one<double, double>(net, reg, ch, hs, tol, d_err, wpb, smem, st);
+    else if (prec == kMixed)
+        launch_one<float, double>(net, reg, ch, hs, tol, d_err, wpb, smem, st);
+    else
+        launch_one<float, float>(net, reg, ch, hs, tol, d_err, wpb, smem, st);
 }
 
 } // namespace am

@@ -117,10 +117,14 @@ int am_region_rows(am_engine *engine, int64_t first, int count, double *rows, do
 typedef enum {
     AM_OPT_CHUNK = 1,         /* regions per chunk (default: sized to ~1 GiB of constraint rows) */
     AM_OPT_PHASE_TIMING = 2,  /* 1: time compose / polygon / frontier separately */
-    AM_OPT_WELD = 3           /* CombineMesh vertex weld: 0 = topological (default: a vertex is named by
+    AM_OPT_WELD = 3,          /* CombineMesh vertex weld: 0 = topological (default: a vertex is named by
                                  its two edge planes and the region key without those bits, which is
                                  watertight by construction), 1 = quantised coordinates as the
                                  reference (int(v*1e6) fp32 / int(v*1e9) fp64, backend/inc/polymesh.h:192) */
+    AM_OPT_GRAPH = 4          /* 1 (default): the wave loop runs on the device as one CUDA graph with a
+                                 conditional while node, no host round trip per wave; 0: host-driven loop.
+                                 Phase timing always uses the host-driven loop.  Both give the same regions
+                                 in the same order. */
 } am_option;
 int am_set_option(am_engine *engine, int option, int64_t value);
 
