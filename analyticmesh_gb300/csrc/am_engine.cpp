@@ -47,6 +47,13 @@ struct DevBuf {
         else p = nullptr;
         return e;
     }
+    // at least n bytes, reusing the allocation when it is large enough
+    // (contents not kept)
+    cudaError_t reserve(size_t n)
+    {
+        if (p && n <= bytes) return cudaSuccess;
+        return alloc(n);
+    }
     // grow keeping the first `keep` bytes
     cudaError_t grow(size_t n, size_t keep, cudaStream_t st)
     {
@@ -107,7 +114,7 @@ bool is_device_ptr(const void *p)
 // copy n bytes from a host or device pointer to a device buffer
 void upload(DevBuf &dst, const void *src, size_t n, cudaStream_t st)
 {
-    AM_CUDA(dst.alloc(n));
+    AM_CUDA(dst.reserve(n));
     if (n) AM_CUDA(cudaMemcpyAsync(dst.p, src, n, is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st));
 }
 
@@ -158,6 +165,10 @@ struct am_engine {
     } d_err;
     WaveCtl *h_ctl = nullptr;
     bool use_graph = true;
+    // the instantiated wave-loop graph and the launch parameters it captured
+    cudaGraph_t wgraph = nullptr;
+    cudaGraphExec_t wexec = nullptr;
+    std::vector<unsigned char> wsig;
     // results
     bool has_am = false, has_mesh = false;
     long long num_regions = 0;
@@ -173,6 +184,7 @@ struct am_engine {
     {
         if (own) cudaStreamDestroy(own);
         if (h_ctl) cudaFreeHost(h_ctl);
+        drop_graph();
     }
 
     RegionsDev regions() const
@@ -214,7 +226,7 @@ struct am_engine {
         while (need < (unsigned long long)std::max<long long>(entries, 1) * 2ull) need <<= 1;
         need = std::max<unsigned long long>(need, 1ull << 16);
         if (need <= hcap) return;
-        AM_CUDA(table.alloc(sizeof(unsigned long long) * need));
+        AM_CUDA(table.reserve(sizeof(unsigned long long) * need));
         hcap = need;
         AM_CUDA(cudaMemsetAsync(table.p, 0xff, sizeof(unsigned long long) * need, st));
         if (rehash && num_regions > 0) {
@@ -255,63 +267,85 @@ struct am_engine {
     }
     WaveCtl *ctl() const { return (WaveCtl *)d_tail.p; }
 
-    // Capture one wave -- composition, polygons, append, step -- as the body
-    // of a conditional while node and run the graph once on the stream.  The
-    // kernels read the wave's range from the control block, so the captured
-    // launches serve every wave.
+    void drop_graph()
+    {
+        if (wexec) cudaGraphExecDestroy(wexec);
+        if (wgraph) cudaGraphDestroy(wgraph);
+        wexec = nullptr;
+        wgraph = nullptr;
+        wsig.clear();
+    }
+
+    // Run every remaining wave with one graph launch: one wave --
+    // composition, polygons, append, step -- is captured as the body of a
+    // conditional while node.  The kernels read the wave's range from the
+    // control block, so the captured launches serve every wave, and the
+    // instantiated graph is reused by later calls while the parameters it
+    // captured (buffers, network layout, iso) are unchanged.
     void run_wave_graph(int prec, const NetDev &net, double iso, const Tolerances &tol, int chunk)
     {
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        auto cleanup = [&] {
-            if (exec) cudaGraphExecDestroy(exec);
-            if (graph) cudaGraphDestroy(graph);
+        const RegionsDev reg = regions();
+        const HashDev hs = hashdev();
+        std::vector<unsigned char> sig;
+        auto add = [&](const void *p, size_t n) {
+            sig.insert(sig.end(), (const unsigned char *)p, (const unsigned char *)p + n);
         };
-        try {
-            AM_CUDA(cudaGraphCreate(&graph, 0));
-            cudaGraphConditionalHandle cond;
-            AM_CUDA(cudaGraphConditionalHandleCreate(&cond, graph, 1, cudaGraphCondAssignDefault));
-            cudaGraphNodeParams np = {};
-            np.type = cudaGraphNodeTypeConditional;
-            np.conditional.handle = cond;
-            np.conditional.type = cudaGraphCondTypeWhile;
-            np.conditional.size = 1;
-            cudaGraphNode_t node;
-            AM_CUDA(cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np));
-            cudaGraph_t body = np.conditional.phGraph_out[0];
-            AM_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-            ChunkDev ch;
-            ch.head = 0;
-            ch.count = chunk;
-            ch.cons = cons.p;
-            ch.eq = eq.p;
-            ch.rec = rec.as<int32_t>();
-            ch.ctl = ctl();
-            const RegionsDev reg = regions();
-            const HashDev hs = hashdev();
-            if (prec == kMixed)
-                launch_compose_tc(net, tcnet, reg, ch, iso, d_err.as<int>(), st);
-            else
-                launch_compose(prec, net, reg, ch, iso, st);
-            launch_polygon(prec, net, reg, ch, hs, tol, d_err.as<int>(), st);
-            launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, chunk * kVMax, d_tail.as<long long>(),
-                          blocksum.as<int>(), (int)(blocksum.bytes / sizeof(int)), d_err.as<int>(), st);
-            launch_wave_step(ctl(), cond, st);
-            cudaGraph_t captured = nullptr;
-            const cudaError_t ce = cudaStreamEndCapture(st, &captured);
-            AM_CUDA(ce);
-            AM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-            AM_CUDA(cudaGraphLaunch(exec, st));
-        } catch (...) {
-            cudaStreamCaptureStatus cs;
-            if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
-                cudaGraph_t g2 = nullptr;
-                cudaStreamEndCapture(st, &g2);
+        const void *bufs[6] = {cons.p, eq.p, rec.p, blocksum.p, d_tail.p, (const void *)blocksum.bytes};
+        add(&prec, sizeof(prec));
+        add(&chunk, sizeof(chunk));
+        add(&iso, sizeof(iso));
+        add(&tol, sizeof(tol));
+        add(&net, sizeof(net));
+        if (prec == kMixed) add(&tcnet, sizeof(tcnet));
+        add(&reg, sizeof(reg));
+        add(&hs, sizeof(hs));
+        add(bufs, sizeof(bufs));
+        if (!wexec || sig != wsig) {
+            drop_graph();
+            try {
+                AM_CUDA(cudaGraphCreate(&wgraph, 0));
+                cudaGraphConditionalHandle cond;
+                AM_CUDA(cudaGraphConditionalHandleCreate(&cond, wgraph, 1, cudaGraphCondAssignDefault));
+                cudaGraphNodeParams np = {};
+                np.type = cudaGraphNodeTypeConditional;
+                np.conditional.handle = cond;
+                np.conditional.type = cudaGraphCondTypeWhile;
+                np.conditional.size = 1;
+                cudaGraphNode_t node;
+                AM_CUDA(cudaGraphAddNode(&node, wgraph, nullptr, nullptr, 0, &np));
+                cudaGraph_t body = np.conditional.phGraph_out[0];
+                AM_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+                ChunkDev ch;
+                ch.head = 0;
+                ch.count = chunk;
+                ch.cons = cons.p;
+                ch.eq = eq.p;
+                ch.rec = rec.as<int32_t>();
+                ch.ctl = ctl();
+                if (prec == kMixed)
+                    launch_compose_tc(net, tcnet, reg, ch, iso, d_err.as<int>(), st);
+                else
+                    launch_compose(prec, net, reg, ch, iso, st);
+                launch_polygon(prec, net, reg, ch, hs, tol, d_err.as<int>(), st);
+                launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, chunk * kVMax,
+                              d_tail.as<long long>(), blocksum.as<int>(), (int)(blocksum.bytes / sizeof(int)),
+                              d_err.as<int>(), st);
+                launch_wave_step(ctl(), cond, st);
+                cudaGraph_t captured = nullptr;
+                AM_CUDA(cudaStreamEndCapture(st, &captured));
+                AM_CUDA(cudaGraphInstantiate(&wexec, wgraph, 0));
+            } catch (...) {
+                cudaStreamCaptureStatus cs;
+                if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
+                    cudaGraph_t g2 = nullptr;
+                    cudaStreamEndCapture(st, &g2);
+                }
+                drop_graph();
+                throw;
             }
-            cleanup();
-            throw;
+            wsig.swap(sig);
         }
-        cleanup(); // destroying a launched exec is stream-ordered-safe
+        AM_CUDA(cudaGraphLaunch(wexec, st));
     }
     void check_err() { poll(); }
 };
@@ -510,7 +544,7 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             } else {
                 const int Mp = (M + 3) / 4 * 4;
                 upload(e->scratch, weights[i], tc * (size_t)M * K, st);
-                AM_CUDA(e->wt[i].alloc(tc * (size_t)K * Mp));
+                AM_CUDA(e->wt[i].reserve(tc * (size_t)K * Mp));
                 launch_prepare_weights(prec == kFloat64 ? kFloat64 : kFloat32, e->scratch.p, M, K, Mp, e->wt[i].p, st);
                 net.Wt[i] = e->wt[i].p;
                 net.Mp[i] = Mp;
@@ -533,7 +567,7 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
                     AM_CHECK(ntm < 64, "too many transform matrices");
                     const int Mp = (h + 3) / 4 * 4;
                     upload(e->scratch, arc_tm[t], tc * (size_t)h * w, st);
-                    AM_CUDA(e->tmt[ntm].alloc(tc * (size_t)w * Mp));
+                    AM_CUDA(e->tmt[ntm].reserve(tc * (size_t)w * Mp));
                     launch_prepare_weights(prec == kFloat64 ? kFloat64 : kFloat32, e->scratch.p, h, w, Mp,
                                            e->tmt[ntm].p, st);
                     sk.kind = 1;
@@ -557,9 +591,8 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             auto split = [&](DevBuf &buf, const void *src_fp32, int M, int K, TcMat &m) {
                 const int Mp = (M + 127) / 128 * 128, Kp = (K + 63) / 64 * 64;
                 upload(e->scratch, src_fp32, sizeof(float) * (size_t)M * K, st);
-                AM_CUDA(buf.alloc((size_t)(Mp / 128) * (Kp / 64) * kWBlockBytes));
+                AM_CUDA(buf.reserve((size_t)(Mp / 128) * (Kp / 64) * kWBlockBytes));
                 launch_pack_weights(e->scratch.as<float>(), M, K, Mp, Kp, buf.p, st);
-                AM_CUDA(cudaStreamSynchronize(st));
                 m.blocks = (const uint8_t *)buf.p;
                 m.Mp = Mp;
                 m.Kp = Kp;
@@ -614,9 +647,9 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             }
             AM_CUDA(cudaStreamSynchronize(st));
         }
-        AM_CUDA(e->s_keys.alloc(sizeof(uint32_t) * (size_t)S * e->W));
-        AM_CUDA(e->s_hash.alloc(sizeof(uint64_t) * (size_t)S));
-        AM_CUDA(e->s_rec.alloc(sizeof(int32_t) * (size_t)S));
+        AM_CUDA(e->s_keys.reserve(sizeof(uint32_t) * (size_t)S * e->W));
+        AM_CUDA(e->s_hash.reserve(sizeof(uint64_t) * (size_t)S));
+        AM_CUDA(e->s_rec.reserve(sizeof(int32_t) * (size_t)S));
 
         e->num_regions = 0;
         e->hcap = 0;
@@ -787,19 +820,19 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
         const long long ns = std::max<long long>(R * kVMax, 1);
         unsigned long long tcap = 1;
         while (tcap < (unsigned long long)ns * 2ull) tcap <<= 1;
-        AM_CUDA(e->w_table.alloc(sizeof(unsigned long long) * tcap));
-        AM_CUDA(e->w_rep.alloc(sizeof(long long) * ns));
-        AM_CUDA(e->w_flag.alloc(sizeof(int) * ns));
-        AM_CUDA(e->w_vidx.alloc(sizeof(int) * ns));
-        AM_CUDA(e->w_bsum.alloc(sizeof(int) * (ns / 1024 + 2)));
-        AM_CUDA(e->w_fflag.alloc(sizeof(int) * (R + 1)));
-        AM_CUDA(e->w_fsize.alloc(sizeof(int) * (R + 1)));
-        AM_CUDA(e->w_fid.alloc(sizeof(int) * (R + 1)));
-        AM_CUDA(e->w_foff.alloc(sizeof(int) * (R + 1)));
-        AM_CUDA(e->w_verts.alloc(e->ts * 3 * ns));
-        AM_CUDA(e->w_fs.alloc(sizeof(int) * (R + 1)));
-        AM_CUDA(e->w_fi.alloc(sizeof(int) * ns));
-        AM_CUDA(e->w_counts.alloc(sizeof(long long) * 3));
+        AM_CUDA(e->w_table.reserve(sizeof(unsigned long long) * tcap));
+        AM_CUDA(e->w_rep.reserve(sizeof(long long) * ns));
+        AM_CUDA(e->w_flag.reserve(sizeof(int) * ns));
+        AM_CUDA(e->w_vidx.reserve(sizeof(int) * ns));
+        AM_CUDA(e->w_bsum.reserve(sizeof(int) * (ns / 1024 + 2)));
+        AM_CUDA(e->w_fflag.reserve(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_fsize.reserve(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_fid.reserve(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_foff.reserve(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_verts.reserve(e->ts * 3 * ns));
+        AM_CUDA(e->w_fs.reserve(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_fi.reserve(sizeof(int) * ns));
+        AM_CUDA(e->w_counts.reserve(sizeof(long long) * 3));
         WeldBuffers wb;
         wb.table = e->w_table.as<unsigned long long>();
         wb.mask = tcap - 1;
