@@ -41,33 +41,118 @@ namespace am {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 512;
 constexpr int kWaitIters = 1 << 22;
 
-// x = hi + mid + lo in bf16 at byte offset `off` of each term (terms `xbytes` apart)
-__device__ __forceinline__ void put_split(uint8_t *xs, size_t xbytes, uint32_t off, float v)
+// x = hi + mid + lo in bf16 for two values at once (round to nearest each)
+__device__ __forceinline__ void split2(float a, float b, uint32_t &h, uint32_t &m, uint32_t &l)
 {
-    const __nv_bfloat16 h = __float2bfloat16_rn(v);
-    const float r1 = v - __bfloat162float(h);
-    const __nv_bfloat16 m = __float2bfloat16_rn(r1);
-    const __nv_bfloat16 l = __float2bfloat16_rn(r1 - __bfloat162float(m));
-    *reinterpret_cast<__nv_bfloat16 *>(xs + off) = h;
-    *reinterpret_cast<__nv_bfloat16 *>(xs + xbytes + off) = m;
-    *reinterpret_cast<__nv_bfloat16 *>(xs + 2 * xbytes + off) = l;
+    const __nv_bfloat162 hb = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(hb);
+    const float ra = a - hf.x, rb = b - hf.y;
+    const __nv_bfloat162 mb = __floats2bfloat162_rn(ra, rb);
+    const float2 mf = __bfloat1622float2(mb);
+    const __nv_bfloat162 lb = __floats2bfloat162_rn(ra - mf.x, rb - mf.y);
+    h = *reinterpret_cast<const uint32_t *>(&hb);
+    m = *reinterpret_cast<const uint32_t *>(&mb);
+    l = *reinterpret_cast<const uint32_t *>(&lb);
 }
 
-__device__ __forceinline__ float get_split(const uint8_t *xs, size_t xbytes, uint32_t off)
-{
-    return __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + off)) +
-           __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + xbytes + off)) +
-           __bfloat162float(*reinterpret_cast<const __nv_bfloat16 *>(xs + 2 * xbytes + off));
-}
+// The masked operand X (ncols x Kp, three bf16 terms `xbytes` apart) in
+// shared memory, in one of two layouts.  MN-major (64-column atoms): the
+// thread that owns one K row writes 8 consecutive columns with one 16-byte
+// store per term.  K-major (any multiple of 16 columns, 2-byte stores): used
+// when a 64-column atom of the widest K does not fit beside the weights.
+struct XOp {
+    uint8_t *xs;
+    size_t xbytes;
+    int ncols, natoms;
+    bool mn;
+
+    __device__ __forceinline__ uint32_t off(int n, int k) const
+    {
+        return mn ? umma::mn_sw128_offset(n, k, natoms) : umma::sw128_offset(n, k, ncols);
+    }
+    // columns n0 .. n0 + 2w - 1 of row k (n0 a multiple of 2w, w = 2 or 4)
+    template <int w>
+    __device__ __forceinline__ void put(int n0, int k, const float *v) const
+    {
+        uint32_t h[w], m[w], l[w];
+#pragma unroll
+        for (int i = 0; i < w; ++i) split2(v[2 * i], v[2 * i + 1], h[i], m[i], l[i]);
+        if (mn) {
+            const uint32_t o = off(n0, k);
+            if (w == 4) {
+                *reinterpret_cast<uint4 *>(xs + o) = make_uint4(h[0], h[1], h[2 % w], h[3 % w]);
+                *reinterpret_cast<uint4 *>(xs + xbytes + o) = make_uint4(m[0], m[1], m[2 % w], m[3 % w]);
+                *reinterpret_cast<uint4 *>(xs + 2 * xbytes + o) = make_uint4(l[0], l[1], l[2 % w], l[3 % w]);
+            } else {
+                *reinterpret_cast<uint2 *>(xs + o) = make_uint2(h[0], h[1]);
+                *reinterpret_cast<uint2 *>(xs + xbytes + o) = make_uint2(m[0], m[1]);
+                *reinterpret_cast<uint2 *>(xs + 2 * xbytes + o) = make_uint2(l[0], l[1]);
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 2 * w; ++i) {
+                const uint32_t o = off(n0 + i, k);
+                const int sh = (i & 1) * 16;
+                *reinterpret_cast<uint16_t *>(xs + o) = (uint16_t)(h[i >> 1] >> sh);
+                *reinterpret_cast<uint16_t *>(xs + xbytes + o) = (uint16_t)(m[i >> 1] >> sh);
+                *reinterpret_cast<uint16_t *>(xs + 2 * xbytes + o) = (uint16_t)(l[i >> 1] >> sh);
+            }
+        }
+    }
+    // hi + mid + lo of columns n0 .. n0 + 3 (n0 a multiple of 4) of row k
+    __device__ __forceinline__ void get4(int n0, int k, float *v) const
+    {
+        uint32_t hw[2], mw[2], lw[2];
+        if (mn) {
+            const uint32_t o = off(n0, k);
+            const uint2 h = *reinterpret_cast<const uint2 *>(xs + o);
+            const uint2 m = *reinterpret_cast<const uint2 *>(xs + xbytes + o);
+            const uint2 l = *reinterpret_cast<const uint2 *>(xs + 2 * xbytes + o);
+            hw[0] = h.x, hw[1] = h.y, mw[0] = m.x, mw[1] = m.y, lw[0] = l.x, lw[1] = l.y;
+        } else {
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const uint32_t o0 = off(n0 + 2 * i, k), o1 = off(n0 + 2 * i + 1, k);
+                auto pair = [&](size_t t) {
+                    return (uint32_t)*reinterpret_cast<const uint16_t *>(xs + t + o0) |
+                           ((uint32_t)*reinterpret_cast<const uint16_t *>(xs + t + o1) << 16);
+                };
+                hw[i] = pair(0), mw[i] = pair(xbytes), lw[i] = pair(2 * xbytes);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&hw[i]));
+            const float2 b = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&mw[i]));
+            const float2 c = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&lw[i]));
+            v[2 * i] = a.x + b.x + c.x;
+            v[2 * i + 1] = a.y + b.y + c.y;
+        }
+    }
+    // descriptor of term u for K block kb, K step j (16 deep) of the block
+    __device__ __forceinline__ uint64_t desc(int u, int kb, int j) const
+    {
+        const uint32_t base = umma::smem_addr(xs) + (uint32_t)(u * xbytes);
+        if (mn) {
+            const uint32_t kgroup = (uint32_t)natoms * 1024u;
+            return umma::desc_sw128_mn(base + (uint32_t)(kb * 8 + 2 * j) * kgroup, 1024u, kgroup);
+        }
+        return umma::desc_sw128(base + (uint32_t)(kb * ncols * 128 + j * 32));
+    }
+    __device__ __forceinline__ uint32_t idesc() const
+    {
+        return mn ? umma::idesc_bf16_bmn(128, ncols) : umma::idesc_bf16(128, ncols);
+    }
+};
 
 // X[n = 4r + c][k] = s_k(r) ? -C[r][src + k][c] : 0 for k < K, 0 up to Kp
-__device__ void stage_x_from_rows(uint8_t *xs, size_t xbytes, int ncols, const float *cons, size_t rstride,
-                                  const uint32_t *keys, int W, int nreg, int src, int K, int Kp)
+__device__ void stage_x_from_rows(const XOp &X, const float *cons, size_t rstride, const uint32_t *keys, int W, int nreg,
+                                  int src, int K, int Kp)
 {
-    const int R = ncols / 4;
+    const int R = X.ncols / 4;
     for (int q = threadIdx.x; q < R * Kp; q += kThreads) {
         const int r = q / Kp, k = q % Kp;
         float x[4] = {0.f, 0.f, 0.f, 0.f};
@@ -81,8 +166,7 @@ __device__ void stage_x_from_rows(uint8_t *xs, size_t xbytes, int ncols, const f
                 x[3] = -c.w;
             }
         }
-#pragma unroll
-        for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), x[c]);
+        X.put<2>(4 * r, k, x);
     }
 }
 
@@ -151,10 +235,11 @@ __device__ void wp_issue(WPipe &p, const NetDev &net, const TcNet &tc)
 
 // (thread 0) D[mt] (+)= M . X over all K blocks of the operand in shared
 // memory: six products per K step (terms t, u of weight 2^-8(t+u), t + u <= 2)
-__device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const TcMat &m, int mtiles, uint8_t *xs,
-                           size_t xbytes, int ncols, uint32_t tmem, bool first, int &g)
+__device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const TcMat &m, int mtiles, const XOp &X,
+                           uint32_t tmem, bool first, int &g)
 {
-    const uint32_t idesc = umma::idesc_bf16(128, ncols);
+    const int ncols = X.ncols;
+    const uint32_t idesc = X.idesc();
     const int kblocks = m.Kp / 64;
     for (int mt = 0; mt < mtiles; ++mt) {
         for (int kb = 0; kb < kblocks; ++kb) {
@@ -163,23 +248,20 @@ __device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const T
             wp_wait(p, p.full + s, (uint32_t)(g / p.nstage) & 1u);
             umma::fence_after();
             const uint32_t a0 = umma::smem_addr(p.ws + (size_t)s * kWBlockBytes);
-            const uint32_t b0 = umma::smem_addr(xs) + (uint32_t)(kb * ncols * 128);
             const uint32_t d_main = tmem + (uint32_t)(mt * ncols);            // hh
             const uint32_t d_corr = tmem + (uint32_t)((mtiles + mt) * ncols); // the rest
             const bool fresh = first && kb == 0;
-#pragma unroll
+            #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const uint32_t o = (uint32_t)(j * 32);
-                umma::mma_bf16(d_main, umma::desc_sw128(a0 + o), umma::desc_sw128(b0 + o), idesc,
-                               (fresh && j == 0) ? 0u : 1u);
+                const uint32_t o = (uint32_t)(j * 32); // A: 16 K columns = 32 bytes of each row
+                umma::mma_bf16(d_main, umma::desc_sw128(a0 + o), X.desc(0, kb, j), idesc, (fresh && j == 0) ? 0u : 1u);
                 int q = 0;
-#pragma unroll
+                #pragma unroll
                 for (int t = 0; t < 3; ++t)
-#pragma unroll
+                    #pragma unroll
                     for (int u = 0; u + t < 3; ++u) {
                         if (t == 0 && u == 0) continue;
-                        umma::mma_bf16(d_corr, umma::desc_sw128(a0 + t * 16384u + o),
-                                       umma::desc_sw128(b0 + (uint32_t)(u * xbytes) + o), idesc,
+                        umma::mma_bf16(d_corr, umma::desc_sw128(a0 + t * 16384u + o), X.desc(u, kb, j), idesc,
                                        (fresh && j == 0 && q == 0) ? 0u : 1u);
                         ++q;
                     }
@@ -210,17 +292,17 @@ __device__ __forceinline__ void gemm_observe(const WPipe &p, int last)
     umma::fence_after();
 }
 
-// tile width for a wave of `count` regions: one tile per SM while the wave
-// is small, the widest tile otherwise
-__host__ __device__ __forceinline__ int tile_cols(int count, int sms, int ncols_max)
+// tile width for a wave of `count` regions: one tile per resident slot
+// while the wave is small, the widest tile otherwise
+__host__ __device__ __forceinline__ int tile_cols(int count, int slots, int ncols_max)
 {
-    const int per = (count + sms - 1) / sms;
+    const int per = (count + slots - 1) / slots;
     const int ncols = (4 * per + 15) / 16 * 16;
     return ncols < 16 ? 16 : (ncols > ncols_max ? ncols_max : ncols);
 }
 
 __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcNet tc, RegionsDev reg, ChunkDev ch,
-                                                                  float iso, int sms, int *err)
+                                                                  float iso, int slots, int *err)
 {
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint64_t bars[4];
@@ -231,7 +313,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     int count;
     chunk_range(ch, head, count);
     if (count <= 0) return;
-    const int ncols = tile_cols(count, sms, tc.ncols_max);
+    const int ncols = tile_cols(count, slots, tc.ncols_max);
     const int R = ncols / 4;
     const int ntiles = (count + R - 1) / R;
     const int mytiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
@@ -241,10 +323,18 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     const size_t rstride = (size_t)net.ALLP * 4;
 
     uint8_t *base = smem_raw + ((1024u - (umma::smem_addr(smem_raw) & 1023u)) & 1023u);
-    const size_t xbytes = (size_t)ncols * tc.kp_max * 2; // one bf16 term of the operand
-    uint8_t *xs = base;                                  // hi, mid, lo: 3 x xbytes
-    uint8_t *ws = base + 3 * xbytes;                     // nstage weight blocks
+    XOp X;
+    X.mn = tc.mn != 0;
+    X.ncols = ncols;
+    X.natoms = (ncols + 63) / 64;
+    X.xbytes = (size_t)(X.mn ? X.natoms * 64 : ncols) * tc.kp_max * 2; // one bf16 term of the operand
+    X.xs = base;                                                     // hi, mid, lo
+    uint8_t *ws = base + 3 * X.xbytes;                               // nstage weight blocks
     uint32_t *keys = reinterpret_cast<uint32_t *>(ws + (size_t)tc.nstage * kWBlockBytes); // the tile's bits
+    // per CTA, for every tile: linear 0 as (w0, w1, w2, b) per unit and the
+    // face-plane weights (the output linear's only row)
+    float4 *w0s = reinterpret_cast<float4 *>(keys + (size_t)(tc.ncols_max / 4) * net.W);
+    float *wls = reinterpret_cast<float *>(w0s + net.nodes[1]);
 
     WPipe pp{bars, bars + 2, ws, tc.nstage, 0, 0, err, 1};
     if (tid == 0) {
@@ -256,8 +346,18 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         while (pp.issued < pp.total && pp.issued < pp.nstage) wp_issue(pp, net, tc);
     }
     if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tmem_cols);
+    {
+        const float *W0 = (const float *)net.W0;
+        const float *b0 = (const float *)net.bias[0];
+        for (int m = tid; m < net.nodes[1]; m += kThreads)
+            w0s[m] = make_float4(W0[3 * m], W0[3 * m + 1], W0[3 * m + 2], b0[m]);
+        const int il = net.n_lin - 1;
+        const float *wl = (const float *)net.Wt[il]; // [K][Mp], column 0
+        for (int k = tid; k < net.nodes[il]; k += kThreads) wls[k] = wl[(size_t)k * net.Mp[il]];
+    }
     int g = 0; // next weight block (thread 0)
-    const int q4 = warp & 3, half = warp >> 2;
+    // epilogue: warp w reads TMEM lanes 32 (w % 4).. and every (kThreads / 128)-th column block
+    const int q4 = warp & 3, cgrp = warp >> 2, ngrp = kThreads / 128;
 
     for (int j = 0; j < mytiles; ++j) {
         const long long rl0 = (long long)(blockIdx.x + (long long)j * gridDim.x) * R;
@@ -270,14 +370,12 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
 
         // hidden layer 1 = linear 0 rows (sign-flipped) and the extra constraints
         {
-            const float *W0 = (const float *)net.W0;
-            const float *b0 = (const float *)net.bias[0];
             const int n1 = net.nodes[1];
             for (int q = tid; q < nreg * n1; q += kThreads) {
                 const int rr = q / n1, m = q % n1;
                 const float sg = key_bit(keys + (size_t)rr * net.W, m) ? -1.f : 1.f;
-                st4<float>(cons + (size_t)rr * rstride + (size_t)m * 4,
-                           make_float4(sg * W0[3 * m], sg * W0[3 * m + 1], sg * W0[3 * m + 2], sg * b0[m]));
+                const float4 w = w0s[m];
+                st4<float>(cons + (size_t)rr * rstride + (size_t)m * 4, make_float4(sg * w.x, sg * w.y, sg * w.z, sg * w.w));
             }
             const float *we = (const float *)net.w_extra;
             const float *be = (const float *)net.b_extra;
@@ -292,13 +390,13 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                 const int r = q / Kp, k = q % Kp;
                 float x[4] = {0.f, 0.f, 0.f, 0.f};
                 if (r < nreg && k < n1 && key_bit(keys + (size_t)r * net.W, k)) {
-                    x[0] = W0[3 * k];
-                    x[1] = W0[3 * k + 1];
-                    x[2] = W0[3 * k + 2];
-                    x[3] = b0[k];
+                    const float4 w = w0s[k];
+                    x[0] = w.x;
+                    x[1] = w.y;
+                    x[2] = w.z;
+                    x[3] = w.w;
                 }
-    #pragma unroll
-                for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), x[c]);
+                    X.put<2>(4 * r, k, x);
             }
         }
         umma::fence_proxy_async();
@@ -310,18 +408,18 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         for (int i = 1; i <= net.n_lin - 2; ++i) {
             const int M = net.nodes[i + 1];
             const int mtiles = (M + 127) / 128;
-            if (tid == 0) gemm_issue(pp, net, tc, tc.lin[i], mtiles, xs, xbytes, ncols, tmem, true, g);
+            if (tid == 0) gemm_issue(pp, net, tc, tc.lin[i], mtiles, X, tmem, true, g);
             for (int s = 0; s < net.nskip[i]; ++s) {
                 const SkipDev &sk = net.skip[i][s];
                 if (tc_skip(sk)) {
                     // the operand is about to be overwritten: the products so far must be done
                     if (tid == 0) gemm_finish(pp, net, tc, g);
                     __syncthreads();
-                    stage_x_from_rows(xs, xbytes, ncols, cons, rstride, keys, net.W, nreg, net.hoff[sk.from],
+                    stage_x_from_rows(X, cons, rstride, keys, net.W, nreg, net.hoff[sk.from],
                                       net.nodes[sk.from], tc.skip[i][s].Kp);
                     umma::fence_proxy_async();
                     __syncthreads();
-                    if (tid == 0) gemm_issue(pp, net, tc, tc.skip[i][s], mtiles, xs, xbytes, ncols, tmem, false, g);
+                    if (tid == 0) gemm_issue(pp, net, tc, tc.skip[i][s], mtiles, X, tmem, false, g);
                 }
             }
             if (tid == 0) {
@@ -336,26 +434,24 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
             for (int q = tid; q < R * (Kn - M); q += kThreads) {
                 const int r = q / (Kn - M), k = M + q % (Kn - M);
-    #pragma unroll
-                for (int c = 0; c < 4; ++c) put_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols), 0.f);
+                const float z[4] = {0.f, 0.f, 0.f, 0.f};
+                X.put<2>(4 * r, k, z);
             }
             for (int mt = 0; mt < mtiles; ++mt) {
                 const int m = mt * 128 + q4 * 32 + lane;
                 const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
                 const float bm = m < M ? bias[m] : 0.f;
                 const int row = net.hoff[i + 1] + m;
-                // byte offset of (n, k = m) for n = 0 (the swizzle adds n & 7)
-                const uint32_t kofs = (uint32_t)((m >> 6) * ncols * 128 + ((m & 7) << 1));
-                const int kchunk = (m & 63) >> 3;
-                for (int cb = half; cb < ncols / 16; cb += 2) {
+                for (int cb = cgrp; cb < ncols / 16; cb += ngrp) {
                     float v[16], vc[16];
-                    umma::tmem_ld16(lane_base + (uint32_t)(mt * ncols + cb * 16), v);
-                    umma::tmem_ld16(lane_base + (uint32_t)((mtiles + mt) * ncols + cb * 16), vc);
+                    umma::tmem_ld16x2(lane_base + (uint32_t)(mt * ncols + cb * 16),
+                                      lane_base + (uint32_t)((mtiles + mt) * ncols + cb * 16), v, vc);
                     if (m >= M) continue;
-    #pragma unroll
+                    float x[16]; // next operand, columns cb * 16 .. + 15 of row k = m
+                    #pragma unroll
                     for (int qq = 0; qq < 4; ++qq) {
                         const int r = cb * 4 + qq;
-                        float x[4] = {0.f, 0.f, 0.f, 0.f};
+                        x[4 * qq] = x[4 * qq + 1] = x[4 * qq + 2] = x[4 * qq + 3] = 0.f;
                         if (r < nreg) {
                             const uint32_t *key = keys + (size_t)r * net.W;
                             float *cr = cons + (size_t)r * rstride;
@@ -387,21 +483,15 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                             const float sg = act ? -1.f : 1.f;
                             st4<float>(cr + (size_t)row * 4, make_float4(sg * o[0], sg * o[1], sg * o[2], sg * o[3]));
                             if (act) {
-                                x[0] = o[0];
-                                x[1] = o[1];
-                                x[2] = o[2];
-                                x[3] = o[3];
-                            }
-                        }
-                        if (Kn > 0) {
-    #pragma unroll
-                            for (int c = 0; c < 4; ++c) {
-                                const int n = 4 * r + c;
-                                put_split(xs, xbytes, kofs + (uint32_t)(n * 128) + (uint32_t)(((kchunk ^ (n & 7)) & 7) << 4),
-                                          x[c]);
+                                x[4 * qq] = o[0];
+                                x[4 * qq + 1] = o[1];
+                                x[4 * qq + 2] = o[2];
+                                x[4 * qq + 3] = o[3];
                             }
                         }
                     }
+                    X.put<4>(cb * 16, m, x);
+                    X.put<4>(cb * 16 + 8, m, x + 8);
                 }
             }
             umma::fence_proxy_async();
@@ -416,19 +506,19 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         {
             const int i = net.n_lin - 1;
             const int K = net.nodes[i];
-            const float *wl = (const float *)net.Wt[i]; // [K][Mp], column 0
-            const int Mp = net.Mp[i];
             const float bl = ((const float *)net.bias[i])[0];
             for (int r = warp; r < nreg; r += kThreads / 32) {
                 float acc[4] = {0.f, 0.f, 0.f, 0.f};
                 for (int k = lane; k < K; k += 32) {
-                    const float w = __ldg(wl + (size_t)k * Mp);
-    #pragma unroll
-                    for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, get_split(xs, xbytes, umma::sw128_offset(4 * r + c, k, ncols)), acc[c]);
+                    const float w = wls[k];
+                    float x[4];
+                    X.get4(4 * r, k, x);
+                    #pragma unroll
+                    for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, x[c], acc[c]);
                 }
-    #pragma unroll
+                #pragma unroll
                 for (int c = 0; c < 4; ++c)
-    #pragma unroll
+                    #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
                 if (lane < 4) {
                     const int c = lane;
@@ -500,7 +590,9 @@ int device_sms()
 
 size_t tc_smem_bytes(const TcNet &tc, int ncols, int W)
 {
-    return 1024 + 3 * (size_t)ncols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(ncols / 4) * W * 4;
+    const size_t cols = tc.mn ? (size_t)(ncols + 63) / 64 * 64 : (size_t)ncols;
+    return 1024 + 3 * cols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * W * 4 +
+           16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last;
 }
 
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,
@@ -510,14 +602,15 @@ void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg
     const int sms = device_sms();
     const size_t smem_max = tc_smem_bytes(tc, tc.ncols_max, net.W);
     cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-    if (ch.ctl) { // wave size known on the device only: a CTA per SM, tiles strided
-        compose_tc_kernel<<<sms, kThreads, smem_max, st>>>(net, tc, reg, ch, (float)iso, sms, d_err);
+    const int slots = sms; // one resident tile per SM
+    if (ch.ctl) { // wave size known on the device only: every resident tile slot, tiles strided
+        compose_tc_kernel<<<slots, kThreads, smem_max, st>>>(net, tc, reg, ch, (float)iso, slots, d_err);
         return;
     }
-    const int ncols = tile_cols(ch.count, sms, tc.ncols_max);
+    const int ncols = tile_cols(ch.count, slots, tc.ncols_max);
     const int R = ncols / 4;
     const int grid = (ch.count + R - 1) / R;
-    compose_tc_kernel<<<grid, kThreads, tc_smem_bytes(tc, ncols, net.W), st>>>(net, tc, reg, ch, (float)iso, sms,
+    compose_tc_kernel<<<grid, kThreads, tc_smem_bytes(tc, ncols, net.W), st>>>(net, tc, reg, ch, (float)iso, slots,
                                                                               d_err);
 }
 

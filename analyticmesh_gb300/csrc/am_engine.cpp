@@ -615,13 +615,23 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             // beside two weight blocks in flight (one if that leaves no room),
             // two accumulators (main + correction) per M tile in 512 TMEM columns
             const size_t smem_cap = 227u * 1024u;
-            for (tc.nstage = 2; tc.nstage >= 1; --tc.nstage) {
-                const long long room = (long long)smem_cap - 1024 - (long long)tc.nstage * kWBlockBytes - 64ll * e->W * 4;
-                int ncols = (int)std::min<long long>(256, std::max<long long>(0, room) / (6ll * tc.kp_max));
-                ncols = std::min(ncols, 256 / tc.mtiles_max) / 16 * 16;
-                tc.ncols_max = ncols;
-                if (ncols >= 16) break;
-            }
+            // preference: MN-major operand (whole 64-column atoms), two weight
+            // stages, then one; then the K-major operand (any 16 columns)
+            tc.ncols_max = 0;
+            tc.n1 = e->nodes[1];
+            tc.k_last = e->nodes[e->n_lin - 1];
+            for (int mn = 1; mn >= 0 && tc.ncols_max < 16; --mn)
+                for (tc.nstage = 2; tc.nstage >= 1; --tc.nstage) {
+                    const long long room = (long long)smem_cap - 1024 - (long long)tc.nstage * kWBlockBytes -
+                                           64ll * e->W * 4 - 16ll * tc.n1 - 4ll * tc.k_last;
+                    long long c = std::max<long long>(0, room) / (6ll * tc.kp_max);
+                    if (mn) c = c / 64 * 64;
+                    int ncols = (int)std::min<long long>(c, 256);
+                    ncols = std::min(ncols, 256 / tc.mtiles_max) / 16 * 16;
+                    tc.ncols_max = ncols;
+                    tc.mn = mn;
+                    if (ncols >= 16) break;
+                }
             AM_CHECK(tc.nstage >= 1 && tc.ncols_max >= 16, "layer widths too large for the tensor-core composition tile");
             AM_CHECK(tc_smem_bytes(tc, tc.ncols_max, e->W) <= smem_cap,
                      "tensor-core composition tile exceeds shared memory");

@@ -11,7 +11,7 @@ namespace am {
 namespace {
 
 __global__ void __launch_bounds__(128) umma_selftest_kernel(const __nv_bfloat16 *A, const __nv_bfloat16 *B, float *D,
-                                                             int N, int K, uint32_t ncols, int *status)
+                                                             int N, int K, uint32_t ncols, int bmn, int *status)
 {
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint64_t mbar;
@@ -24,9 +24,11 @@ __global__ void __launch_bounds__(128) umma_selftest_kernel(const __nv_bfloat16 
         const int r = q / K, k = q % K;
         *reinterpret_cast<__nv_bfloat16 *>(sA + umma::sw128_offset(r, k, 128)) = A[q];
     }
+    const int natoms = (N + 63) / 64;
     for (int q = tid; q < N * K; q += 128) {
         const int r = q / K, k = q % K;
-        *reinterpret_cast<__nv_bfloat16 *>(sB + umma::sw128_offset(r, k, N)) = B[q];
+        const uint32_t off = bmn ? umma::mn_sw128_offset(r, k, natoms) : umma::sw128_offset(r, k, N);
+        *reinterpret_cast<__nv_bfloat16 *>(sB + off) = B[q];
     }
     umma::fence_proxy_async();
     if (tid == 0) umma::mbar_init(&mbar, 1);
@@ -36,11 +38,14 @@ __global__ void __launch_bounds__(128) umma_selftest_kernel(const __nv_bfloat16 
     umma::fence_after();
     const uint32_t tmem = tslot;
     if (tid == 0) {
-        const uint32_t idesc = umma::idesc_bf16(128, N);
+        const uint32_t idesc = bmn ? umma::idesc_bf16_bmn(128, N) : umma::idesc_bf16(128, N);
         for (int j = 0; j < K / 16; ++j) {
             const uint32_t off = (uint32_t)((j & 3) * 32);
             const uint64_t ad = umma::desc_sw128(umma::smem_addr(sA) + (j >> 2) * 128 * 128 + off);
-            const uint64_t bd = umma::desc_sw128(umma::smem_addr(sB) + (j >> 2) * N * 128 + off);
+            // MN-major: one K step of 16 is two 8-row groups
+            const uint64_t bd = bmn ? umma::desc_sw128_mn(umma::smem_addr(sB) + (uint32_t)(2 * j * natoms * 1024), 1024u,
+                                                          (uint32_t)(natoms * 1024))
+                                    : umma::desc_sw128(umma::smem_addr(sB) + (j >> 2) * N * 128 + off);
             umma::mma_bf16(tmem, ad, bd, idesc, j > 0 ? 1u : 0u);
         }
         umma::commit(umma::smem_addr(&mbar));
@@ -66,7 +71,8 @@ __global__ void __launch_bounds__(128) umma_selftest_kernel(const __nv_bfloat16 
 } // namespace
 } // namespace am
 
-extern "C" int am_selftest_umma(const void *A, const void *B, void *D, int N, int K)
+namespace {
+int selftest(const void *A, const void *B, void *D, int N, int K, int bmn)
 {
     if (N < 16 || N > 256 || N % 16 || K < 64 || K % 64) return AM_ERR_INVALID_ARGUMENT;
     uint32_t ncols = 32;
@@ -74,14 +80,28 @@ extern "C" int am_selftest_umma(const void *A, const void *B, void *D, int N, in
     int *status = nullptr;
     if (cudaMalloc(&status, sizeof(int)) != cudaSuccess) return AM_ERR_OUT_OF_MEMORY;
     cudaMemset(status, 0, sizeof(int));
-    const size_t smem = 1024 + (size_t)(128 + N) * K * 2;
+    // B region: N x K (K-major) or 64-wide atoms (MN-major), doubled so that
+    // every descriptor reading of it stays inside the allocation
+    const size_t bbytes = (size_t)(bmn ? (N + 63) / 64 * 64 : N) * K * 2;
+    const size_t smem = 1024 + (size_t)128 * K * 2 + 2 * bbytes;
     cudaFuncSetAttribute(am::umma_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     am::umma_selftest_kernel<<<1, 128, smem>>>((const __nv_bfloat16 *)A, (const __nv_bfloat16 *)B, (float *)D, N, K, ncols,
-                                               status);
+                                               bmn, status);
     cudaError_t e = cudaDeviceSynchronize();
     int h = 0;
     cudaMemcpy(&h, status, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(status);
     if (e != cudaSuccess) return AM_ERR_CUDA;
     return h ? AM_ERR_CUDA : AM_OK;
+}
+} // namespace
+
+extern "C" int am_selftest_umma(const void *A, const void *B, void *D, int N, int K)
+{
+    return selftest(A, B, D, N, K, 0);
+}
+
+extern "C" int am_selftest_umma_bmn(const void *A, const void *B, void *D, int N, int K)
+{
+    return selftest(A, B, D, N, K, 1);
 }

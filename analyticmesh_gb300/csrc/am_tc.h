@@ -28,6 +28,8 @@ struct TcNet {
     int kp_max;                         // largest padded K of any operand
     int mtiles_max;                     // largest number of 128-row tiles of any layer
     int nstage;                         // weight blocks in flight (1 or 2)
+    int mn;                             // operand layout: 1 MN-major (64-column atoms), 0 K-major
+    int n1, k_last;                     // widths of hidden layer 1 and of the last hidden layer
 };
 
 size_t tc_smem_bytes(const TcNet &tc, int ncols, int W);

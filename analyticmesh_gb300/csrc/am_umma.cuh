@@ -40,11 +40,37 @@ __device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr)
     return d;
 }
 
+// byte offset of element (n, k) in an MN-major SW128 operand whose MN extent
+// is natoms x 64: groups of eight K rows, each group natoms 1024-byte atoms
+// (8 rows x 128 bytes, 64 consecutive n per row, 16-byte chunks XOR-permuted
+// by k % 8)
+__device__ __forceinline__ uint32_t mn_sw128_offset(int n, int k, int natoms)
+{
+    return (uint32_t)((((k >> 3) * natoms + (n >> 6)) << 10) + ((k & 7) << 7) +
+                      (((((n & 63) >> 3) ^ (k & 7)) & 7) << 4) + ((n & 7) << 1));
+}
+
+// descriptor of an MN-major SW128 operand: leading byte offset = stride
+// between 64-wide MN atoms, stride byte offset = stride between 8-row K groups
+__device__ __forceinline__ uint64_t desc_sw128_mn(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
 // instruction descriptor, kind::f16: D fp32, A and B bf16, both K-major
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+
+// the same with B MN-major (transpose-B bit)
+__host__ __device__ constexpr uint32_t idesc_bf16_bmn(int M, int N) { return idesc_bf16(M, N) | (1u << 16); }
 
 __device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc)
 {
@@ -135,6 +161,29 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// two 16-column loads (e.g. the two accumulators of one column block) under
+// one wait
+__device__ __forceinline__ void tmem_ld16x2(uint32_t a, uint32_t b, float *v, float *w)
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, "
+        "[%33];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(a), "r"(b)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        v[i] = __uint_as_float(r[i]);
+        w[i] = __uint_as_float(r[16 + i]);
+    }
 }
 
 } // namespace umma

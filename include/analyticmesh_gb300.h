@@ -133,6 +133,10 @@ int am_set_option(am_engine *engine, int option, int64_t value);
  * A (128 x K, bf16, row-major) . B (N x K, bf16, row-major)^T on one CTA,
  * 16 <= N <= 256, N % 16 == 0, K % 64 == 0; device pointers. */
 int am_selftest_umma(const void *A, const void *B, void *D, int N, int K);
+/* The same tile with B staged MN-major (64-wide 128B-swizzled atoms), the
+ * operand layout of the mixed composition (no counterpart in the reference);
+ * the inputs and D are as for am_selftest_umma. */
+int am_selftest_umma_bmn(const void *A, const void *B, void *D, int N, int K);
 
 /* ---- region composition that allocates nothing (no counterpart in the
  * reference).  For callers that cannot let a library call cudaMalloc: code

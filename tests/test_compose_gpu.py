@@ -64,7 +64,8 @@ def rel_err(rows, ref):
     lambda: wl.geometric([20, 50, 20, 80, 20], 13, skips=[[0], [1, 1, 0], [1, 1, 1], [0], [0]], tm_shapes=[[0, 0], [80, 20]]),
     lambda: wl.geometric([256, 256, 256], 14, perturb=0.02),
     lambda: wl.geometric([64] * 5, 15, perturb=0.01, skips=[[0], [0], [1, 0, 0], [0], [0]], tm_shapes=[[64, 3]]),
-], ids=["sphere", "odd_widths", "wide256", "input_skip"])
+    lambda: wl.geometric([512] * 3, 16, perturb=0.01),
+], ids=["sphere", "odd_widths", "wide256", "input_skip", "wide512_kmajor"])
 def test_tensor_core_rows_match_fp32_accuracy(factory):
     m = factory()
     net = wl.net_arrays(m)

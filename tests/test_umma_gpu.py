@@ -46,3 +46,18 @@ def test_umma_accumulation_bits():
     bits = max(survived) if survived else 0
     print("tcgen05 bf16 accumulation keeps 1 + 2^-k up to k =", bits)
     assert bits >= 8
+
+
+@pytest.mark.parametrize("N,K", [(256, 128), (64, 192), (16, 64), (128, 256), (48, 64), (160, 128)])
+def test_umma_tile_mn_major_b_matches_torch(N, K):
+    """B staged MN-major (the composition's operand layout), including MN
+    extents that fill only part of the last 64-wide atom."""
+    from analyticmesh_gb300 import _lib
+    L = _lib.lib()
+    L.am_selftest_umma_bmn.argtypes = [C.c_void_p] * 3 + [C.c_int, C.c_int]
+    g = torch.Generator(device="cuda").manual_seed(N * 1000 + K + 7)
+    A = torch.randn(128, K, device="cuda", generator=g).to(torch.bfloat16)
+    B = torch.randn(N, K, device="cuda", generator=g).to(torch.bfloat16)
+    D = torch.empty(128, N, device="cuda", dtype=torch.float32)
+    assert L.am_selftest_umma_bmn(A.data_ptr(), B.data_ptr(), D.data_ptr(), N, K) == 0
+    torch.testing.assert_close(D, A.float() @ B.float().t(), rtol=1e-5, atol=1e-4)
