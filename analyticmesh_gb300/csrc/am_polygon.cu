@@ -162,6 +162,261 @@ __device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long 
     return true;
 }
 
+// One face walk: from the start plane s, ray shooting along each edge line
+// in the scan precision TC, vertices solved in TS.  Lane i ends with vertex
+// i (vx, vy, vz) and the plane of the edge leaving it (ve); lane j records
+// step j's hit plane (sbk) and merge decision (sdec, 0 append, 1 merge with
+// the previous vertex, 2 merge with the first), nsteps the steps taken.
+template <typename TC, typename TS>
+__device__ void walk(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TS *eqv, const TS *p, int s, TC par_eps,
+                     TS same_eps, int lane, TS &vx, TS &vy, TS &vz, int &ve, int &n, bool &closed, int8_t &status,
+                     int &sbk, int &sdec, int &nsteps)
+{
+    TC cx = 0, cy = 0, cz = 0; // the vertex rounded to the scan precision
+    vx = vy = vz = TS(0);
+    ve = -1;
+    n = 0;
+    closed = false;
+    sbk = -1;
+    sdec = 0;
+    nsteps = 0;
+    int e = s, prev = -1;
+    TC curc[3] = {(TC)p[0], (TC)p[1], (TC)p[2]}; // current point, scan precision
+    for (int step = 0; step < kWalkSteps; ++step) {
+        nsteps = step + 1;
+        // direction of the edge line: w_eq x w_e (counter-clockwise about w_eq)
+        const vec4_t<TC> ref_ = rows[e];
+        const TC d0 = eqc.y * ref_.z - eqc.z * ref_.y;
+        const TC d1 = eqc.z * ref_.x - eqc.x * ref_.z;
+        const TC d2 = eqc.x * ref_.y - eqc.y * ref_.x;
+        const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        const TC c0 = curc[0], c1 = curc[1], c2 = curc[2];
+        // first hit along the edge line: min over crossing planes of
+        // t = max(0, -g) / a, compared as fractions
+        // (two interleaved candidates per lane halve the compare chain)
+        TC bnum = TC(1), bden = TC(0), bnum1 = TC(1), bden1 = TC(0);
+        int bk = 0x7fffffff, bk1 = 0x7fffffff;
+        auto consider = [&](int k, TC &bn, TC &bd, int &bi) {
+            const vec4_t<TC> r = rows[k];
+            const TC a = r.x * d0 + r.y * d1 + r.z * d2;
+            if (!(a > thr) || k == e || k == prev) return;
+            TC num = -(r.x * c0 + r.y * c1 + r.z * c2 + r.w);
+            num = num > TC(0) ? num : TC(0);
+            const TC lhs = num * bd, rhs = bn * a;
+            if (lhs < rhs || (lhs == rhs && k < bi)) {
+                bn = num;
+                bd = a;
+                bi = k;
+            }
+        };
+        int k = lane;
+        for (; k + 32 < ALL; k += 64) {
+            consider(k, bnum, bden, bk);
+            consider(k + 32, bnum1, bden1, bk1);
+        }
+        if (k < ALL) consider(k, bnum, bden, bk);
+        {
+            const TC lhs = bnum1 * bden, rhs = bnum * bden1;
+            if (bk1 != 0x7fffffff && (lhs < rhs || (lhs == rhs && bk1 < bk))) {
+                bnum = bnum1;
+                bden = bden1;
+                bk = bk1;
+            }
+        }
+        TC bt = bk == 0x7fffffff ? TC(INFINITY) : bnum / bden;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const TC ot = __shfl_xor_sync(0xffffffffu, bt, o);
+            const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+            if (ot < bt || (ot == bt && ok < bk)) {
+                bt = ot;
+                bk = ok;
+            }
+        }
+        if (bk == 0x7fffffff) { // the edge line never leaves the region
+            status = kOpen;
+            break;
+        }
+        // vertex = 3x3 solve of (edge plane, hit plane, face plane)
+        TS V[3];
+        TC Vc[3];
+        if (!warp_solve<TC, TS>(rows, e, bk, eqv, V, Vc, lane)) {
+            status = kSingular;
+            break;
+        }
+        // 0 append, 1 zero-length edge on e (merge), 2 zero-length closing edge;
+        // decided in the solve precision (on the scan-precision copies
+        // where the rounding margin settles it)
+        int decision = 0;
+        if (n > 0) {
+            int s1 = -1, s2 = 0;
+            if (sizeof(TS) > sizeof(TC)) {
+                s1 = same_filter<TC, TS>(Vc, __shfl_sync(0xffffffffu, cx, n - 1),
+                                         __shfl_sync(0xffffffffu, cy, n - 1),
+                                         __shfl_sync(0xffffffffu, cz, n - 1), same_eps);
+                if (bk == s && s1 == 0)
+                    s2 = same_filter<TC, TS>(Vc, __shfl_sync(0xffffffffu, cx, 0),
+                                             __shfl_sync(0xffffffffu, cy, 0),
+                                             __shfl_sync(0xffffffffu, cz, 0), same_eps);
+            }
+            if (s1 == 1) {
+                decision = 1;
+            } else if (s1 == 0 && s2 != -1) {
+                decision = s2 == 1 ? 2 : 0;
+            } else {
+                const TS lx = __shfl_sync(0xffffffffu, vx, n - 1);
+                const TS ly = __shfl_sync(0xffffffffu, vy, n - 1);
+                const TS lz = __shfl_sync(0xffffffffu, vz, n - 1);
+                if (lane == 0) { // in the solve precision, on one lane
+                    if (fabs(V[0] - lx) + fabs(V[1] - ly) + fabs(V[2] - lz) < same_eps)
+                        decision = 1;
+                    else if (bk == s && fabs(V[0] - vx) + fabs(V[1] - vy) + fabs(V[2] - vz) < same_eps)
+                        decision = 2;
+                }
+                decision = __shfl_sync(0xffffffffu, decision, 0);
+            }
+        }
+        if (lane == step) {
+            sbk = bk;
+            sdec = decision;
+        }
+        if (decision == 1 && lane == n - 1) ve = bk; // the edge on e has zero length
+        const bool appended = (decision == 0);
+        if (appended) {
+            if (lane == n) {
+                vx = V[0];
+                vy = V[1];
+                vz = V[2];
+                cx = Vc[0];
+                cy = Vc[1];
+                cz = Vc[2];
+                ve = bk;
+            }
+            n++;
+        }
+        if (bk == s) {
+            closed = true;
+            break;
+        }
+        if (n >= kVMax) {
+            status = kTruncated;
+            break;
+        }
+        prev = e;
+        e = bk;
+        curc[0] = Vc[0];
+        curc[1] = Vc[1];
+        curc[2] = Vc[2];
+    }
+    if (!closed && status == kOk) status = kTruncated;
+}
+
+// Mixed form: the walk runs in the scan precision TC (solves included, as the
+// plain form does), then every vertex is solved again in TS -- four lanes per
+// vertex (the four Cramer determinants), eight vertices per warp instruction
+// -- and every merge decision is taken again on the TS vertices.  When all
+// decisions agree, the face is the TS walk's face: the same hit planes, the
+// same TS vertices.  Returns false, and the caller walks again with a TS
+// solve at every step, when the TC walk did not close normally, took more
+// than 32 steps, met a vertex that is not finite in TS, or a decision comes
+// out differently in TS.
+template <typename TC, typename TS>
+__device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TS *eqv, const TS *p, int s,
+                             TC par_eps, TS same_eps, int lane, TS &vx, TS &vy, TS &vz, int &ve, int &n, bool &closed,
+                             int8_t &status)
+{
+    const unsigned full = 0xffffffffu;
+    const TC eqf[4] = {eqc.x, eqc.y, eqc.z, eqc.w};
+    const TC pf[3] = {(TC)p[0], (TC)p[1], (TC)p[2]};
+    TC fx, fy, fz;
+    int fve, fn, sbk, sdec, nsteps;
+    bool fclosed;
+    int8_t fst = kOk;
+    walk<TC, TC>(rows, ALL, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz, fve, fn, fclosed, fst, sbk, sdec,
+                 nsteps);
+    if (fst != kOk || !fclosed || nsteps < 1 || nsteps > 32) return false;
+
+    // step j's vertex in TS, into lane j
+    const int G = lane >> 2, L = lane & 3, gbase = lane & ~3;
+    TS rx = 0, ry = 0, rz = 0;
+    bool planes_ok = true;
+    for (int r0 = 0; r0 < nsteps; r0 += 8) {
+        const int j = min(r0 + G, nsteps - 1);            // the step this lane group solves
+        const int pb = __shfl_sync(full, sbk, j);          // its hit plane
+        const int pj = __shfl_sync(full, sbk, max(j - 1, 0));
+        const int pa = j == 0 ? s : pj;                    // and the edge plane it walked on
+        const bool in = (unsigned)pa < (unsigned)ALL && (unsigned)pb < (unsigned)ALL;
+        planes_ok = planes_ok && in;
+        const TC *ra = reinterpret_cast<const TC *>(rows + (in ? pa : 0));
+        const TC *rb = reinterpret_cast<const TC *>(rows + (in ? pb : 0));
+        // lane t of the group converts components 2t, 2t + 1 of [row a | row b]
+        const TS c0 = (TS)(L < 2 ? ra[2 * L] : rb[2 * L - 4]);
+        const TS c1 = (TS)(L < 2 ? ra[2 * L + 1] : rb[2 * L - 3]);
+        TS m[8];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            m[2 * t] = __shfl_sync(full, c0, gbase | t);
+            m[2 * t + 1] = __shfl_sync(full, c1, gbase | t);
+        }
+        const TS a00 = L == 1 ? -m[3] : m[0], a01 = L == 2 ? -m[3] : m[1], a02 = L == 3 ? -m[3] : m[2];
+        const TS a10 = L == 1 ? -m[7] : m[4], a11 = L == 2 ? -m[7] : m[5], a12 = L == 3 ? -m[7] : m[6];
+        const TS a20 = L == 1 ? -eqv[3] : eqv[0], a21 = L == 2 ? -eqv[3] : eqv[1], a22 = L == 3 ? -eqv[3] : eqv[2];
+        const TS d = det3<TS>(a00, a01, a02, a10, a11, a12, a20, a21, a22);
+        const TS x = d / __shfl_sync(full, d, gbase);
+        const int src = ((lane - r0) & 7) * 4 + 1;
+        const TS v0 = __shfl_sync(full, x, src), v1 = __shfl_sync(full, x, src + 1), v2 = __shfl_sync(full, x, src + 2);
+        if (lane >= r0 && lane < r0 + 8) {
+            rx = v0;
+            ry = v1;
+            rz = v2;
+        }
+    }
+    const bool mine = lane < nsteps;
+    if (!__all_sync(full, planes_ok && (!mine || (finite_bits(rx) && finite_bits(ry) && finite_bits(rz))))) return false;
+
+    // the decisions again, on the TS vertices: step j against the last
+    // vertex appended before it and, on the closing step, the first vertex
+    const unsigned amask = __ballot_sync(full, mine && sdec == 0);
+    const unsigned before = lane > 0 ? (amask & ((1u << lane) - 1u)) : 0u;
+    const int la = before ? 31 - __clz(before) : 0;
+    const TC Vc[3] = {(TC)rx, (TC)ry, (TC)rz};
+    const TC lx = __shfl_sync(full, Vc[0], la), ly = __shfl_sync(full, Vc[1], la), lz = __shfl_sync(full, Vc[2], la);
+    const TC f0 = __shfl_sync(full, Vc[0], 0), f1 = __shfl_sync(full, Vc[1], 0), f2 = __shfl_sync(full, Vc[2], 0);
+    const bool check = mine && lane > 0;
+    int s1 = same_filter<TC, TS>(Vc, lx, ly, lz, same_eps);
+    int s2 = sbk == s ? same_filter<TC, TS>(Vc, f0, f1, f2, same_eps) : 0;
+    if (__any_sync(full, check && (s1 < 0 || (s1 == 0 && s2 < 0)))) {
+        const TS Lx = __shfl_sync(full, rx, la), Ly = __shfl_sync(full, ry, la), Lz = __shfl_sync(full, rz, la);
+        const TS Fx = __shfl_sync(full, rx, 0), Fy = __shfl_sync(full, ry, 0), Fz = __shfl_sync(full, rz, 0);
+        if (check && s1 < 0) s1 = (fabs(rx - Lx) + fabs(ry - Ly) + fabs(rz - Lz) < same_eps) ? 1 : 0;
+        if (check && s2 < 0) s2 = (fabs(rx - Fx) + fabs(ry - Fy) + fabs(rz - Fz) < same_eps) ? 1 : 0;
+    }
+    const int dec = s1 == 1 ? 1 : (sbk == s && s2 == 1 ? 2 : 0);
+    if (!__all_sync(full, !check || dec == sdec)) return false;
+
+    // vertex o is the o-th appended step; its edge is the hit plane of the
+    // last step before the next append, a closing merge excepted
+    n = __popc(amask);
+    const int so = lane < n ? (int)__fns(amask, 0, lane + 1) : 0;
+    const int snext = lane + 1 < n ? (int)__fns(amask, 0, lane + 2) : nsteps;
+    int kl = (snext - 1) & 31;
+    if (__shfl_sync(full, sdec, kl) == 2) kl = (kl - 1) & 31;
+    const int e_out = __shfl_sync(full, sbk, kl);
+    const TS ox = __shfl_sync(full, rx, so), oy = __shfl_sync(full, ry, so), oz = __shfl_sync(full, rz, so);
+    if (lane < n) {
+        vx = ox;
+        vy = oy;
+        vz = oz;
+        ve = e_out;
+    } else {
+        vx = vy = vz = TS(0);
+        ve = -1;
+    }
+    closed = true;
+    status = kOk;
+    return true;
+}
+
 // Rows are staged normalised (|w| = 1, zero rows become 0.x + sign(b) inf):
 // signed geometric distances are then plain dot products, the same quantity
 // the reference's feasibility test computes as (w.x + b) * rsqrt(|w|^2)
@@ -262,8 +517,10 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
             for (int x = 0; x <= x_max; ++x) {
                 int i, j;
                 get_i_j(x, ALL, i, j);
-                const int ri = i < 32 ? __shfl_sync(0xffffffffu, top0, i) : __shfl_sync(0xffffffffu, top1, i - 32);
-                const int rj = j < 32 ? __shfl_sync(0xffffffffu, top0, j) : __shfl_sync(0xffffffffu, top1, j - 32);
+                const int ri0 = __shfl_sync(0xffffffffu, top0, i & 31), ri1 = __shfl_sync(0xffffffffu, top1, i & 31);
+                const int rj0 = __shfl_sync(0xffffffffu, top0, j & 31), rj1 = __shfl_sync(0xffffffffu, top1, j & 31);
+                const int ri = i < 32 ? ri0 : ri1;
+                const int rj = j < 32 ? rj0 : rj1;
                 TS v[3];
                 TC vc[3];
                 warp_solve<TC, TS>(rows, ri, rj, eqv, v, vc, lane);
@@ -287,135 +544,19 @@ __global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg
         // ---------------------------------------------------- walk
         // lane i holds vertex i and the plane of the edge leaving it
         TS vx = 0, vy = 0, vz = 0;
-        TC cx = 0, cy = 0, cz = 0; // the vertex rounded to the scan precision
         int ve = -1;
         int n = 0;
         bool closed = false;
         if (s >= 0) {
-            int e = s, prev = -1;
-            TC curc[3] = {(TC)p[0], (TC)p[1], (TC)p[2]}; // current point, scan precision
-            for (int step = 0; step < kWalkSteps; ++step) {
-                // direction of the edge line: w_eq x w_e (counter-clockwise about w_eq)
-                const vec4_t<TC> ref_ = rows[e];
-                const TC d0 = eqc.y * ref_.z - eqc.z * ref_.y;
-                const TC d1 = eqc.z * ref_.x - eqc.x * ref_.z;
-                const TC d2 = eqc.x * ref_.y - eqc.y * ref_.x;
-                const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-                const TC c0 = curc[0], c1 = curc[1], c2 = curc[2];
-                // first hit along the edge line: min over crossing planes of
-                // t = max(0, -g) / a, compared as fractions
-                // (two interleaved candidates per lane halve the compare chain)
-                TC bnum = TC(1), bden = TC(0), bnum1 = TC(1), bden1 = TC(0);
-                int bk = 0x7fffffff, bk1 = 0x7fffffff;
-                auto consider = [&](int k, TC &bn, TC &bd, int &bi) {
-                    const vec4_t<TC> r = rows[k];
-                    const TC a = r.x * d0 + r.y * d1 + r.z * d2;
-                    if (!(a > thr) || k == e || k == prev) return;
-                    TC num = -(r.x * c0 + r.y * c1 + r.z * c2 + r.w);
-                    num = num > TC(0) ? num : TC(0);
-                    const TC lhs = num * bd, rhs = bn * a;
-                    if (lhs < rhs || (lhs == rhs && k < bi)) {
-                        bn = num;
-                        bd = a;
-                        bi = k;
-                    }
-                };
-                int k = lane;
-                for (; k + 32 < ALL; k += 64) {
-                    consider(k, bnum, bden, bk);
-                    consider(k + 32, bnum1, bden1, bk1);
-                }
-                if (k < ALL) consider(k, bnum, bden, bk);
-                {
-                    const TC lhs = bnum1 * bden, rhs = bnum * bden1;
-                    if (bk1 != 0x7fffffff && (lhs < rhs || (lhs == rhs && bk1 < bk))) {
-                        bnum = bnum1;
-                        bden = bden1;
-                        bk = bk1;
-                    }
-                }
-                TC bt = bk == 0x7fffffff ? TC(INFINITY) : bnum / bden;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    const TC ot = __shfl_xor_sync(0xffffffffu, bt, o);
-                    const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
-                    if (ot < bt || (ot == bt && ok < bk)) {
-                        bt = ot;
-                        bk = ok;
-                    }
-                }
-                if (bk == 0x7fffffff) { // the edge line never leaves the region
-                    status = kOpen;
-                    break;
-                }
-                // vertex = 3x3 solve of (edge plane, hit plane, face plane)
-                TS V[3];
-                TC Vc[3];
-                if (!warp_solve<TC, TS>(rows, e, bk, eqv, V, Vc, lane)) {
-                    status = kSingular;
-                    break;
-                }
-                // 0 append, 1 zero-length edge on e (merge), 2 zero-length closing edge;
-                // decided in the solve precision (on the scan-precision copies
-                // where the rounding margin settles it)
-                int decision = 0;
-                if (n > 0) {
-                    int s1 = -1, s2 = 0;
-                    if (sizeof(TS) > sizeof(TC)) {
-                        s1 = same_filter<TC, TS>(Vc, __shfl_sync(0xffffffffu, cx, n - 1),
-                                                 __shfl_sync(0xffffffffu, cy, n - 1),
-                                                 __shfl_sync(0xffffffffu, cz, n - 1), same_eps);
-                        if (bk == s && s1 == 0)
-                            s2 = same_filter<TC, TS>(Vc, __shfl_sync(0xffffffffu, cx, 0),
-                                                     __shfl_sync(0xffffffffu, cy, 0),
-                                                     __shfl_sync(0xffffffffu, cz, 0), same_eps);
-                    }
-                    if (s1 == 1) {
-                        decision = 1;
-                    } else if (s1 == 0 && s2 != -1) {
-                        decision = s2 == 1 ? 2 : 0;
-                    } else {
-                        const TS lx = __shfl_sync(0xffffffffu, vx, n - 1);
-                        const TS ly = __shfl_sync(0xffffffffu, vy, n - 1);
-                        const TS lz = __shfl_sync(0xffffffffu, vz, n - 1);
-                        if (lane == 0) { // in the solve precision, on one lane
-                            if (fabs(V[0] - lx) + fabs(V[1] - ly) + fabs(V[2] - lz) < same_eps)
-                                decision = 1;
-                            else if (bk == s && fabs(V[0] - vx) + fabs(V[1] - vy) + fabs(V[2] - vz) < same_eps)
-                                decision = 2;
-                        }
-                        decision = __shfl_sync(0xffffffffu, decision, 0);
-                    }
-                }
-                if (decision == 1 && lane == n - 1) ve = bk; // the edge on e has zero length
-                const bool appended = (decision == 0);
-                if (appended) {
-                    if (lane == n) {
-                        vx = V[0];
-                        vy = V[1];
-                        vz = V[2];
-                        cx = Vc[0];
-                        cy = Vc[1];
-                        cz = Vc[2];
-                        ve = bk;
-                    }
-                    n++;
-                }
-                if (bk == s) {
-                    closed = true;
-                    break;
-                }
-                if (n >= kVMax) {
-                    status = kTruncated;
-                    break;
-                }
-                prev = e;
-                e = bk;
-                curc[0] = Vc[0];
-                curc[1] = Vc[1];
-                curc[2] = Vc[2];
+            bool done = false;
+            if (sizeof(TS) > sizeof(TC)) // scan-precision walk, vertices refined in the solve precision
+                done = walk_refined<TC, TS>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n,
+                                            closed, status);
+            if (!done) {
+                int sbk, sdec, nsteps;
+                walk<TC, TS>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n, closed, status,
+                             sbk, sdec, nsteps);
             }
-            if (!closed && status == kOk) status = kTruncated;
         }
 
         // ---------------------------------------------------- outputs
