@@ -28,6 +28,15 @@ class AmStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class AmRunArgs(C.Structure):
+    """am_run_args: the arguments of am_analytic_marching for one network of a batch."""
+    _fields_ = [
+        ("weights", C.c_void_p), ("biases", C.c_void_p), ("states", C.c_void_p), ("points", C.c_void_p),
+        ("num_points", C.c_int), ("arc_tm", C.c_void_p), ("arc_tm_shapes", C.c_void_p), ("num_arc_tm", C.c_int),
+        ("w_extra", C.c_void_p), ("b_extra", C.c_void_p), ("iso", C.c_double), ("flip_insideout", C.c_int),
+    ]
+
+
 AM_OPT_CHUNK = 1
 AM_OPT_PHASE_TIMING = 2
 AM_OPT_WELD = 3
@@ -62,6 +71,7 @@ def lib():
     L.am_get_regions.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp]
     L.am_set_option.argtypes = [vp, C.c_int, C.c_int64]
     L.am_region_rows.argtypes = [vp, C.c_int64, C.c_int, vp, vp]
+    L.am_run_batch.argtypes = [vp, C.POINTER(AmRunArgs), C.c_int, C.POINTER(C.c_double)]
     L.am_compose_rows_noalloc.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, C.c_double, vp, vp, vp]
     _LIB = L
     return L

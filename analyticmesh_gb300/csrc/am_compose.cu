@@ -10,6 +10,7 @@
 // diag(s_l) A_l = -s_l * C_l staged in shared memory, and skip connections
 // accumulate into the same tile.  Connections into the output layer are
 // composed too (the reference's loop stops before them, process.h:42).
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "am_device.cuh"
@@ -213,7 +214,7 @@ __global__ void prepare_weights_kernel(const T *src, int M, int K, int Mp, T *ds
 void launch_compose(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, double iso, cudaStream_t st)
 {
     if (!ch.ctl && ch.count <= 0) return;
-    const int grid = ch.ctl ? device_sms() * 4 : (ch.count + kR - 1) / kR;
+    const int grid = ch.ctl ? std::max(1, device_sms() * 4 / std::max(ch.share, 1)) : (ch.count + kR - 1) / kR;
     if (prec == kFloat64)
         compose_kernel<double><<<grid, kThreads, 0, st>>>(net, reg, ch, iso);
     else

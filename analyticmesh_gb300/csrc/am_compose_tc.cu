@@ -602,7 +602,8 @@ void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg
     const int sms = device_sms();
     const size_t smem_max = tc_smem_bytes(tc, tc.ncols_max, net.W);
     cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-    const int slots = sms; // one resident tile per SM
+    // one resident tile per SM (per SM share when several networks march at once)
+    const int slots = std::max(1, sms / std::max(ch.share, 1));
     if (ch.ctl) { // wave size known on the device only: every resident tile slot, tiles strided
         compose_tc_kernel<<<slots, kThreads, smem_max, st>>>(net, tc, reg, ch, (float)iso, slots, d_err);
         return;

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/analyticmesh_gb300.h"
@@ -165,6 +166,25 @@ struct am_engine {
     } d_err;
     WaveCtl *h_ctl = nullptr;
     bool use_graph = true;
+    // the run in progress: am_analytic_marching, or one network of am_run_batch
+    struct Run {
+        int prec = 0;
+        double iso = 0;
+        Tolerances tol{};
+        int chunk = 0;
+        long long head = 0, tail = 0, launches = 0;
+        int chunks = 0;
+        double t_comp = 0, t_poly = 0, t_front = 0;
+        bool flip = false;
+    } run;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, pa = nullptr, pb = nullptr;
+    int share = 1; // networks marching side by side on the GPU (graph-driven grids are divided by it)
+    bool lean = false; // batch member: region store and table start small and grow on demand
+    void ensure_events()
+    {
+        for (cudaEvent_t *ev : {&ev0, &ev1, &pa, &pb})
+            if (!*ev) AM_CUDA(cudaEventCreate(ev));
+    }
     // the instantiated wave-loop graph and the launch parameters it captured
     cudaGraph_t wgraph = nullptr;
     cudaGraphExec_t wexec = nullptr;
@@ -184,6 +204,8 @@ struct am_engine {
     {
         if (own) cudaStreamDestroy(own);
         if (h_ctl) cudaFreeHost(h_ctl);
+        for (cudaEvent_t ev : {ev0, ev1, pa, pb})
+            if (ev) cudaEventDestroy(ev);
         drop_graph();
     }
 
@@ -293,6 +315,7 @@ struct am_engine {
         const void *bufs[6] = {cons.p, eq.p, rec.p, blocksum.p, d_tail.p, (const void *)blocksum.bytes};
         add(&prec, sizeof(prec));
         add(&chunk, sizeof(chunk));
+        add(&share, sizeof(share));
         add(&iso, sizeof(iso));
         add(&tol, sizeof(tol));
         add(&net, sizeof(net));
@@ -322,6 +345,7 @@ struct am_engine {
                 ch.eq = eq.p;
                 ch.rec = rec.as<int32_t>();
                 ch.ctl = ctl();
+                ch.share = share;
                 if (prec == kMixed)
                     launch_compose_tc(net, tcnet, reg, ch, iso, d_err.as<int>(), st);
                 else
@@ -370,6 +394,408 @@ int guarded(am_engine *e, F &&f)
 int size_of_prec(int prec) { return prec == kFloat64 ? 8 : 4; }
 
 } // namespace
+
+// A run in phases, so that am_run_batch can interleave networks: begin
+// (network upload, seed regions), the wave loop (graph-driven: launch, then
+// poll; or host-driven), end (statistics).
+struct RunArgs {
+    const void *const *weights, *const *biases;
+    const uint8_t *states;
+    const void *points;
+    int num_points;
+    const void *const *arc_tm;
+    const int32_t *arc_tm_shapes;
+    int num_arc_tm;
+    const void *w_extra, *b_extra;
+    double iso;
+    int flip_insideout;
+    void *stream;
+};
+
+void run_begin(am_engine *e, const RunArgs &a)
+{
+    const void *const *weights = a.weights;
+    const void *const *biases = a.biases;
+    const uint8_t *states = a.states;
+    const void *points = a.points;
+    const int num_points = a.num_points;
+    const void *const *arc_tm = a.arc_tm;
+    const int32_t *arc_tm_shapes = a.arc_tm_shapes;
+    const int num_arc_tm = a.num_arc_tm;
+    const void *w_extra = a.w_extra, *b_extra = a.b_extra;
+    const double iso = a.iso;
+    void *stream = a.stream;
+    e->ensure_events();
+    e->st = stream ? (cudaStream_t)stream : e->own;
+    cudaStream_t st = e->st;
+    const int prec = e->prec;
+    const size_t tc = e->tc, ts = e->ts;
+    AM_CHECK(weights && biases, "weights / biases are NULL");
+    AM_CHECK(states && points && num_points >= 1, "states / points are empty"); // cuam.cpp:142
+    AM_CHECK(e->E == 0 || (w_extra && b_extra), "extra constraints are NULL");
+    // arc_tm shapes, cuam.cpp:160-173
+    for (int i = 0; i + 1 < e->n_lin; ++i) {
+        const int *row = e->arc.data() + (size_t)i * e->arc_cols;
+        for (int c = 0; c < row[0]; ++c) {
+            const int from = row[1 + 2 * c], t = row[2 + 2 * c];
+            AM_CHECK(t >= 0 && t < num_arc_tm && arc_tm_shapes, "arc_table refers to a missing transform");
+            const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
+            if (h || w) {
+                AM_CHECK(h == e->nodes[i + 2], "transform rows must match the target width");
+                AM_CHECK(w == e->nodes[from], "transform columns must match the source width");
+            } else {
+                AM_CHECK(e->nodes[from] == e->nodes[i + 2], "identity connection between different widths");
+            }
+        }
+    }
+
+
+    // ---------------------------------------------------------- network
+    NetDev &net = e->net;
+    memset(&net, 0, sizeof(net));
+    net.n_lin = e->n_lin;
+    net.N = e->N;
+    net.E = e->E;
+    net.ALL = e->ALL;
+    net.ALLP = e->ALLP;
+    net.W = e->W;
+    for (int i = 0; i <= e->n_lin; ++i) net.nodes[i] = e->nodes[i];
+    net.hoff[1] = 0;
+    for (int h = 1; h < e->n_lin; ++h) net.hoff[h + 1] = net.hoff[h] + e->nodes[h];
+    for (int i = 0; i < e->n_lin; ++i) {
+        const int M = e->nodes[i + 1], K = e->nodes[i];
+        AM_CHECK(weights[i] && biases[i], "a weight / bias pointer is NULL");
+        upload(e->bias[i], biases[i], tc * M, st);
+        net.bias[i] = e->bias[i].p;
+        if (i == 0) {
+            upload(e->w0, weights[0], tc * (size_t)M * 3, st);
+            net.W0 = e->w0.p;
+        } else {
+            const int Mp = (M + 3) / 4 * 4;
+            upload(e->scratch, weights[i], tc * (size_t)M * K, st);
+            AM_CUDA(e->wt[i].reserve(tc * (size_t)K * Mp));
+            launch_prepare_weights(prec == kFloat64 ? kFloat64 : kFloat32, e->scratch.p, M, K, Mp, e->wt[i].p, st);
+            net.Wt[i] = e->wt[i].p;
+            net.Mp[i] = Mp;
+        }
+    }
+    int ntm = 0;
+    for (int i = 1; i < e->n_lin; ++i) {
+        const int *row = e->arc.data() + (size_t)(i - 1) * e->arc_cols;
+        net.nskip[i] = row[0];
+        for (int c = 0; c < row[0]; ++c) {
+            const int from = row[1 + 2 * c], t = row[2 + 2 * c];
+            SkipDev &sk = net.skip[i][c];
+            sk.from = from;
+            const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
+            if (h == 0 && w == 0) {
+                sk.kind = 0;
+                sk.tmt = nullptr;
+                sk.Mp = 0;
+            } else {
+                AM_CHECK(ntm < 64, "too many transform matrices");
+                const int Mp = (h + 3) / 4 * 4;
+                upload(e->scratch, arc_tm[t], tc * (size_t)h * w, st);
+                AM_CUDA(e->tmt[ntm].reserve(tc * (size_t)w * Mp));
+                launch_prepare_weights(prec == kFloat64 ? kFloat64 : kFloat32, e->scratch.p, h, w, Mp,
+                                       e->tmt[ntm].p, st);
+                sk.kind = 1;
+                sk.tmt = e->tmt[ntm].p;
+                sk.Mp = Mp;
+                ntm++;
+            }
+        }
+    }
+    if (e->E) {
+        upload(e->wext, w_extra, tc * 3 * (size_t)e->E, st);
+        upload(e->bext, b_extra, tc * (size_t)e->E, st);
+    }
+    net.w_extra = e->wext.p;
+    net.b_extra = e->bext.p;
+    if (prec == kMixed) {
+        // three bf16 terms per weight, stored as 128 x 64 shared-memory block images
+        TcNet &tc = e->tcnet;
+        memset(&tc, 0, sizeof(tc));
+        tc.mtiles_max = 1;
+        auto split = [&](DevBuf &buf, const void *src_fp32, int M, int K, TcMat &m) {
+            const int Mp = (M + 127) / 128 * 128, Kp = (K + 63) / 64 * 64;
+            upload(e->scratch, src_fp32, sizeof(float) * (size_t)M * K, st);
+            AM_CUDA(buf.reserve((size_t)(Mp / 128) * (Kp / 64) * kWBlockBytes));
+            launch_pack_weights(e->scratch.as<float>(), M, K, Mp, Kp, buf.p, st);
+            m.blocks = (const uint8_t *)buf.p;
+            m.Mp = Mp;
+            m.Kp = Kp;
+            tc.kp_max = std::max(tc.kp_max, Kp);
+            tc.mtiles_max = std::max(tc.mtiles_max, Mp / 128);
+        };
+        for (int i = 1; i <= e->n_lin - 2; ++i) {
+            split(e->tc_lin[i], weights[i], e->nodes[i + 1], e->nodes[i], tc.lin[i]);
+            const int *row = e->arc.data() + (size_t)(i - 1) * e->arc_cols;
+            for (int c = 0; c < row[0]; ++c) {
+                const int from = row[1 + 2 * c], t = row[2 + 2 * c];
+                const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
+                if ((h || w) && from >= 1) split(e->tc_skip[i][c], arc_tm[t], h, w, tc.skip[i][c]);
+            }
+        }
+        // the operand also holds hidden layer 1 and the last hidden layer
+        tc.kp_max = std::max(tc.kp_max, (e->nodes[1] + 63) / 64 * 64);
+        tc.kp_max = std::max(tc.kp_max, (e->nodes[e->n_lin - 1] + 63) / 64 * 64);
+        // widest tile: three operand terms (3 x ncols x kp_max x 2 bytes)
+        // beside two weight blocks in flight (one if that leaves no room),
+        // two accumulators (main + correction) per M tile in 512 TMEM columns
+        const size_t smem_cap = 227u * 1024u;
+        // preference: MN-major operand (whole 64-column atoms), two weight
+        // stages, then one; then the K-major operand (any 16 columns)
+        tc.ncols_max = 0;
+        tc.n1 = e->nodes[1];
+        tc.k_last = e->nodes[e->n_lin - 1];
+        for (int mn = 1; mn >= 0 && tc.ncols_max < 16; --mn)
+            for (tc.nstage = 2; tc.nstage >= 1; --tc.nstage) {
+                const long long room = (long long)smem_cap - 1024 - (long long)tc.nstage * kWBlockBytes -
+                                       64ll * e->W * 4 - 16ll * tc.n1 - 4ll * tc.k_last;
+                long long c = std::max<long long>(0, room) / (6ll * tc.kp_max);
+                if (mn) c = c / 64 * 64;
+                int ncols = (int)std::min<long long>(c, 256);
+                ncols = std::min(ncols, 256 / tc.mtiles_max) / 16 * 16;
+                tc.ncols_max = ncols;
+                tc.mn = mn;
+                if (ncols >= 16) break;
+            }
+        AM_CHECK(tc.nstage >= 1 && tc.ncols_max >= 16, "layer widths too large for the tensor-core composition tile");
+        AM_CHECK(tc_smem_bytes(tc, tc.ncols_max, e->W) <= smem_cap,
+                 "tensor-core composition tile exceeds shared memory");
+    }
+    AM_CUDA(cudaGetLastError());
+
+    // ---------------------------------------------------------- seeds
+    const int S = num_points;
+    upload(e->s_states, states, (size_t)S * e->N, st);
+    {
+        // seed points in the solve precision
+        std::vector<double> pd(3 * (size_t)S);
+        std::vector<unsigned char> raw(tc * 3 * (size_t)S);
+        to_host(raw.data(), points, raw.size(), st);
+        AM_CUDA(cudaStreamSynchronize(st));
+        for (size_t q = 0; q < 3 * (size_t)S; ++q)
+            pd[q] = tc == 8 ? ((const double *)raw.data())[q] : (double)((const float *)raw.data())[q];
+        if (ts == 8) {
+            upload(e->s_pts, pd.data(), sizeof(double) * pd.size(), st);
+        } else {
+            std::vector<float> pf(pd.begin(), pd.end());
+            upload(e->s_pts, pf.data(), sizeof(float) * pf.size(), st);
+        }
+        AM_CUDA(cudaStreamSynchronize(st));
+    }
+    AM_CUDA(e->s_keys.reserve(sizeof(uint32_t) * (size_t)S * e->W));
+    AM_CUDA(e->s_hash.reserve(sizeof(uint64_t) * (size_t)S));
+    AM_CUDA(e->s_rec.reserve(sizeof(int32_t) * (size_t)S));
+
+    e->num_regions = 0;
+    e->hcap = 0;
+    e->stats = am_stats{};
+    AM_CUDA(cudaMemsetAsync(e->d_tail.p, 0, sizeof(long long), st));
+    AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
+    const int chunk = e->default_chunk();
+    e->ensure_chunk(std::min(chunk, std::max(S, 1024)));
+    const long long first_wave = e->lean ? std::min<long long>(chunk, 4ll * S + 1024) : chunk;
+    e->ensure_regions(std::max<long long>(S, 1) + first_wave * kVMax);
+    e->ensure_table((long long)S + first_wave * kVMax, false);
+    AM_CUDA(e->blocksum.grow(sizeof(int) * ((size_t)S / 1024 + 2), 0, st));
+    AM_CUDA(cudaStreamSynchronize(st));
+
+    e->run.launches = 0;
+    AM_CUDA(cudaEventRecord(e->ev0, st));
+    launch_seed_pack(e->s_states.as<uint8_t>(), S, e->N, e->W, e->s_keys.as<uint32_t>(), e->s_hash.as<uint64_t>(), st);
+    launch_seed_insert(e->s_keys.as<uint32_t>(), e->s_hash.as<uint64_t>(), S, e->W, e->hashdev(),
+                       e->s_rec.as<int32_t>(), e->d_err.as<int>(), st);
+    {
+        ChunkDev sc{};
+        sc.rec = e->s_rec.as<int32_t>();
+        launch_append(1, prec, net, e->regions(), sc, e->hashdev(), e->s_keys.as<uint32_t>(),
+                      e->s_hash.as<uint64_t>(), e->s_pts.p, S, e->d_tail.as<long long>(), e->blocksum.as<int>(),
+                      (int)(e->blocksum.bytes / sizeof(int)), e->d_err.as<int>(), st);
+    }
+    e->run.launches += 5;
+    AM_CUDA(cudaGetLastError());
+    const long long tail = e->poll();
+    e->num_regions = tail;
+    e->stats.num_seeds = tail;
+
+    am_engine::Run &r = e->run;
+    r.prec = prec;
+    r.iso = iso;
+    r.tol = prec == kFloat64 ? Tolerances{1e-20, 3e-14, 1e-12} : Tolerances{1e-12, 3e-7, 1e-6};
+    r.chunk = chunk;
+    r.head = 0;
+    r.tail = tail;
+    r.chunks = 0;
+    r.t_comp = r.t_poly = r.t_front = 0;
+    r.flip = a.flip_insideout != 0;
+}
+
+// graph-driven loop: one graph launch runs up to max_waves waves, until the
+// queue is empty; it stops early when the next wave's children might not
+// fit, and then resumes after the host grows the region store and the
+// table.  The control block comes back to pinned memory behind the graph.
+void run_graph_launch(am_engine *e, int max_waves)
+{
+    am_engine::Run &r = e->run;
+    cudaStream_t st = e->st;
+    e->ensure_chunk(r.chunk);
+    const int count = (int)std::min<long long>(r.tail - r.head, r.chunk);
+    e->ensure_regions(r.tail + (long long)count * kVMax);
+    e->ensure_table(std::max<long long>(r.tail + (long long)count * kVMax, e->cap), true);
+    WaveCtl *h = e->h_ctl;
+    h->head = r.head;
+    h->count = count;
+    h->waves = 0;
+    h->limit = std::min<long long>(e->cap, (long long)(e->hcap / 2));
+    h->chunk_cap = r.chunk;
+    h->work = 0u;
+    h->max_waves = max_waves;
+    // tail and err stay as the device has them
+    AM_CUDA(cudaMemcpyAsync((char *)e->d_tail.p + offsetof(WaveCtl, head), (char *)h + offsetof(WaveCtl, head),
+                            sizeof(WaveCtl) - offsetof(WaveCtl, head), cudaMemcpyHostToDevice, st));
+    e->run_wave_graph(r.prec, e->net, r.iso, r.tol, r.chunk);
+    AM_CUDA(cudaMemcpyAsync(h, e->d_tail.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost, st));
+}
+
+// after the stream has reached the end of the launch: true while regions remain
+bool run_graph_done(am_engine *e)
+{
+    am_engine::Run &r = e->run;
+    const WaveCtl *h = e->h_ctl;
+    if (h->err & kErrTableFull) throw Failure{AM_ERR_TABLE_FULL, "hash probe bound reached"};
+    if (h->err & kErrCapacity) throw Failure{AM_ERR_CAPACITY, "region store capacity exceeded"};
+    AM_CHECK(h->waves < kMaxWaves, "wave bound reached");
+    r.tail = h->tail;
+    r.chunks += h->waves;
+    r.launches += 6ll * h->waves;
+    r.head = h->head;
+    e->num_regions = r.tail;
+    return r.head < r.tail;
+}
+
+// host-driven loop (phase timing, or AM_OPT_GRAPH = 0)
+void run_host_loop(am_engine *e)
+{
+    am_engine::Run &run = e->run;
+    cudaStream_t st = e->st;
+    const int prec = run.prec;
+    const NetDev &net = e->net;
+    const double iso = run.iso;
+    const Tolerances tol = run.tol;
+    const int chunk = run.chunk;
+    long long head = run.head, tail = run.tail, launches = run.launches;
+    int chunks = run.chunks;
+    double t_comp = 0, t_poly = 0, t_front = 0;
+    cudaEvent_t pa = e->pa, pb = e->pb;
+    while (head < tail) {
+        const int count = (int)std::min<long long>(tail - head, chunk);
+        e->ensure_chunk(count);
+        e->ensure_regions(tail + (long long)count * kVMax);
+        e->ensure_table(tail + (long long)count * kVMax, true);
+        ChunkDev ch;
+        ch.head = head;
+        ch.count = count;
+        ch.cons = e->cons.p;
+        ch.eq = e->eq.p;
+        ch.rec = e->rec.as<int32_t>();
+        const RegionsDev reg = e->regions();
+        const HashDev hs = e->hashdev();
+        float ms = 0;
+        if (e->phase_timing) AM_CUDA(cudaEventRecord(pa, st));
+        if (prec == kMixed)
+            launch_compose_tc(net, e->tcnet, reg, ch, iso, e->d_err.as<int>(), st);
+        else
+            launch_compose(prec, net, reg, ch, iso, st);
+        if (e->phase_timing) {
+            AM_CUDA(cudaEventRecord(pb, st));
+            AM_CUDA(cudaEventSynchronize(pb));
+            AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
+            t_comp += ms;
+            AM_CUDA(cudaEventRecord(pa, st));
+        }
+        launch_polygon(prec, net, reg, ch, hs, tol, e->d_err.as<int>(), st);
+        if (e->phase_timing) {
+            AM_CUDA(cudaEventRecord(pb, st));
+            AM_CUDA(cudaEventSynchronize(pb));
+            AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
+            t_poly += ms;
+            AM_CUDA(cudaEventRecord(pa, st));
+        }
+        launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, count * kVMax, e->d_tail.as<long long>(),
+                      e->blocksum.as<int>(), (int)(e->blocksum.bytes / sizeof(int)), e->d_err.as<int>(), st);
+        if (e->phase_timing) {
+            AM_CUDA(cudaEventRecord(pb, st));
+            AM_CUDA(cudaEventSynchronize(pb));
+            AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
+            t_front += ms;
+        }
+        launches += 5;
+        AM_CUDA(cudaGetLastError());
+        head += count;
+        tail = e->poll();
+        e->num_regions = tail;
+        chunks++;
+    }
+    run.head = head;
+    run.tail = tail;
+    run.launches = launches;
+    run.chunks = chunks;
+    run.t_comp = t_comp;
+    run.t_poly = t_poly;
+    run.t_front = t_front;
+}
+
+void run_end(am_engine *e)
+{
+    am_engine::Run &run = e->run;
+    cudaStream_t st = e->st;
+    const long long tail = run.tail;
+    const int chunks = run.chunks;
+    const long long launches = run.launches;
+    const double t_comp = run.t_comp, t_poly = run.t_poly, t_front = run.t_front;
+    const int flip_insideout = run.flip ? 1 : 0;
+    const double iso = run.iso;
+    cudaEvent_t ev0 = e->ev0, ev1 = e->ev1;
+    AM_CUDA(cudaEventRecord(ev1, st));
+    AM_CUDA(cudaEventSynchronize(ev1));
+    float total = 0;
+    AM_CUDA(cudaEventElapsedTime(&total, ev0, ev1));
+    e->check_err();
+
+    // statistics
+    am_stats &sx = e->stats;
+    sx.num_regions = tail;
+    sx.chunks = chunks;
+    sx.am_time_ms = total;
+    sx.compose_ms = t_comp;
+    sx.polygon_ms = t_poly;
+    sx.frontier_ms = t_front;
+    sx.kernel_launches = launches;
+    {
+        std::vector<int32_t> hn((size_t)tail);
+        std::vector<int8_t> hsx((size_t)tail);
+        AM_CUDA(cudaMemcpyAsync(hn.data(), e->nv.p, sizeof(int32_t) * tail, cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaMemcpyAsync(hsx.data(), e->status.p, sizeof(int8_t) * tail, cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        for (long long r = 0; r < tail; ++r) {
+            if (hn[r] >= 3) sx.num_faces++;
+            sx.max_polygon_verts = std::max(sx.max_polygon_verts, hn[r]);
+            switch (hsx[r]) {
+            case kNoStart: sx.num_nostart++; break;
+            case kOpen: sx.num_open++; break;
+            case kTruncated: sx.num_truncated++; break;
+            case kSingular: sx.num_singular++; break;
+            default: break;
+            }
+        }
+    }
+    e->flip = flip_insideout ? 1 : 0;
+    e->iso = iso;
+    e->has_am = true;
+}
 
 extern "C" {
 
@@ -481,335 +907,105 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
     if (!e) return AM_ERR_NOT_INITIALIZED;
     e->has_am = false;
     e->has_mesh = false;
+    e->share = 1;
+    const RunArgs a{weights, biases, states, points, num_points, arc_tm, arc_tm_shapes, num_arc_tm,
+                    w_extra, b_extra, iso, flip_insideout, stream};
     return guarded(e, [&] {
-        e->st = stream ? (cudaStream_t)stream : e->own;
-        cudaStream_t st = e->st;
-        const int prec = e->prec;
-        const size_t tc = e->tc, ts = e->ts;
-        AM_CHECK(weights && biases, "weights / biases are NULL");
-        AM_CHECK(states && points && num_points >= 1, "states / points are empty"); // cuam.cpp:142
-        AM_CHECK(e->E == 0 || (w_extra && b_extra), "extra constraints are NULL");
-        // arc_tm shapes, cuam.cpp:160-173
-        for (int i = 0; i + 1 < e->n_lin; ++i) {
-            const int *row = e->arc.data() + (size_t)i * e->arc_cols;
-            for (int c = 0; c < row[0]; ++c) {
-                const int from = row[1 + 2 * c], t = row[2 + 2 * c];
-                AM_CHECK(t >= 0 && t < num_arc_tm && arc_tm_shapes, "arc_table refers to a missing transform");
-                const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
-                if (h || w) {
-                    AM_CHECK(h == e->nodes[i + 2], "transform rows must match the target width");
-                    AM_CHECK(w == e->nodes[from], "transform columns must match the source width");
-                } else {
-                    AM_CHECK(e->nodes[from] == e->nodes[i + 2], "identity connection between different widths");
-                }
-            }
-        }
-
-        cudaEvent_t ev0, ev1, pa, pb;
-        AM_CUDA(cudaEventCreate(&ev0));
-        AM_CUDA(cudaEventCreate(&ev1));
-        AM_CUDA(cudaEventCreate(&pa));
-        AM_CUDA(cudaEventCreate(&pb));
-        struct EvGuard {
-            cudaEvent_t a, b, c, d;
-            ~EvGuard()
-            {
-                cudaEventDestroy(a);
-                cudaEventDestroy(b);
-                cudaEventDestroy(c);
-                cudaEventDestroy(d);
-            }
-        } evg{ev0, ev1, pa, pb};
-
-        // ---------------------------------------------------------- network
-        NetDev &net = e->net;
-        memset(&net, 0, sizeof(net));
-        net.n_lin = e->n_lin;
-        net.N = e->N;
-        net.E = e->E;
-        net.ALL = e->ALL;
-        net.ALLP = e->ALLP;
-        net.W = e->W;
-        for (int i = 0; i <= e->n_lin; ++i) net.nodes[i] = e->nodes[i];
-        net.hoff[1] = 0;
-        for (int h = 1; h < e->n_lin; ++h) net.hoff[h + 1] = net.hoff[h] + e->nodes[h];
-        for (int i = 0; i < e->n_lin; ++i) {
-            const int M = e->nodes[i + 1], K = e->nodes[i];
-            AM_CHECK(weights[i] && biases[i], "a weight / bias pointer is NULL");
-            upload(e->bias[i], biases[i], tc * M, st);
-            net.bias[i] = e->bias[i].p;
-            if (i == 0) {
-                upload(e->w0, weights[0], tc * (size_t)M * 3, st);
-                net.W0 = e->w0.p;
-            } else {
-                const int Mp = (M + 3) / 4 * 4;
-                upload(e->scratch, weights[i], tc * (size_t)M * K, st);
-                AM_CUDA(e->wt[i].reserve(tc * (size_t)K * Mp));
-                launch_prepare_weights(prec == kFloat64 ? kFloat64 : kFloat32, e->scratch.p, M, K, Mp, e->wt[i].p, st);
-                net.Wt[i] = e->wt[i].p;
-                net.Mp[i] = Mp;
-            }
-        }
-        int ntm = 0;
-        for (int i = 1; i < e->n_lin; ++i) {
-            const int *row = e->arc.data() + (size_t)(i - 1) * e->arc_cols;
-            net.nskip[i] = row[0];
-            for (int c = 0; c < row[0]; ++c) {
-                const int from = row[1 + 2 * c], t = row[2 + 2 * c];
-                SkipDev &sk = net.skip[i][c];
-                sk.from = from;
-                const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
-                if (h == 0 && w == 0) {
-                    sk.kind = 0;
-                    sk.tmt = nullptr;
-                    sk.Mp = 0;
-                } else {
-                    AM_CHECK(ntm < 64, "too many transform matrices");
-                    const int Mp = (h + 3) / 4 * 4;
-                    upload(e->scratch, arc_tm[t], tc * (size_t)h * w, st);
-                    AM_CUDA(e->tmt[ntm].reserve(tc * (size_t)w * Mp));
-                    launch_prepare_weights(prec == kFloat64 ? kFloat64 : kFloat32, e->scratch.p, h, w, Mp,
-                                           e->tmt[ntm].p, st);
-                    sk.kind = 1;
-                    sk.tmt = e->tmt[ntm].p;
-                    sk.Mp = Mp;
-                    ntm++;
-                }
-            }
-        }
-        if (e->E) {
-            upload(e->wext, w_extra, tc * 3 * (size_t)e->E, st);
-            upload(e->bext, b_extra, tc * (size_t)e->E, st);
-        }
-        net.w_extra = e->wext.p;
-        net.b_extra = e->bext.p;
-        if (prec == kMixed) {
-            // three bf16 terms per weight, stored as 128 x 64 shared-memory block images
-            TcNet &tc = e->tcnet;
-            memset(&tc, 0, sizeof(tc));
-            tc.mtiles_max = 1;
-            auto split = [&](DevBuf &buf, const void *src_fp32, int M, int K, TcMat &m) {
-                const int Mp = (M + 127) / 128 * 128, Kp = (K + 63) / 64 * 64;
-                upload(e->scratch, src_fp32, sizeof(float) * (size_t)M * K, st);
-                AM_CUDA(buf.reserve((size_t)(Mp / 128) * (Kp / 64) * kWBlockBytes));
-                launch_pack_weights(e->scratch.as<float>(), M, K, Mp, Kp, buf.p, st);
-                m.blocks = (const uint8_t *)buf.p;
-                m.Mp = Mp;
-                m.Kp = Kp;
-                tc.kp_max = std::max(tc.kp_max, Kp);
-                tc.mtiles_max = std::max(tc.mtiles_max, Mp / 128);
-            };
-            for (int i = 1; i <= e->n_lin - 2; ++i) {
-                split(e->tc_lin[i], weights[i], e->nodes[i + 1], e->nodes[i], tc.lin[i]);
-                const int *row = e->arc.data() + (size_t)(i - 1) * e->arc_cols;
-                for (int c = 0; c < row[0]; ++c) {
-                    const int from = row[1 + 2 * c], t = row[2 + 2 * c];
-                    const int h = arc_tm_shapes[2 * t], w = arc_tm_shapes[2 * t + 1];
-                    if ((h || w) && from >= 1) split(e->tc_skip[i][c], arc_tm[t], h, w, tc.skip[i][c]);
-                }
-            }
-            // the operand also holds hidden layer 1 and the last hidden layer
-            tc.kp_max = std::max(tc.kp_max, (e->nodes[1] + 63) / 64 * 64);
-            tc.kp_max = std::max(tc.kp_max, (e->nodes[e->n_lin - 1] + 63) / 64 * 64);
-            // widest tile: three operand terms (3 x ncols x kp_max x 2 bytes)
-            // beside two weight blocks in flight (one if that leaves no room),
-            // two accumulators (main + correction) per M tile in 512 TMEM columns
-            const size_t smem_cap = 227u * 1024u;
-            // preference: MN-major operand (whole 64-column atoms), two weight
-            // stages, then one; then the K-major operand (any 16 columns)
-            tc.ncols_max = 0;
-            tc.n1 = e->nodes[1];
-            tc.k_last = e->nodes[e->n_lin - 1];
-            for (int mn = 1; mn >= 0 && tc.ncols_max < 16; --mn)
-                for (tc.nstage = 2; tc.nstage >= 1; --tc.nstage) {
-                    const long long room = (long long)smem_cap - 1024 - (long long)tc.nstage * kWBlockBytes -
-                                           64ll * e->W * 4 - 16ll * tc.n1 - 4ll * tc.k_last;
-                    long long c = std::max<long long>(0, room) / (6ll * tc.kp_max);
-                    if (mn) c = c / 64 * 64;
-                    int ncols = (int)std::min<long long>(c, 256);
-                    ncols = std::min(ncols, 256 / tc.mtiles_max) / 16 * 16;
-                    tc.ncols_max = ncols;
-                    tc.mn = mn;
-                    if (ncols >= 16) break;
-                }
-            AM_CHECK(tc.nstage >= 1 && tc.ncols_max >= 16, "layer widths too large for the tensor-core composition tile");
-            AM_CHECK(tc_smem_bytes(tc, tc.ncols_max, e->W) <= smem_cap,
-                     "tensor-core composition tile exceeds shared memory");
-        }
-        AM_CUDA(cudaGetLastError());
-
-        // ---------------------------------------------------------- seeds
-        const int S = num_points;
-        upload(e->s_states, states, (size_t)S * e->N, st);
-        {
-            // seed points in the solve precision
-            std::vector<double> pd(3 * (size_t)S);
-            std::vector<unsigned char> raw(tc * 3 * (size_t)S);
-            to_host(raw.data(), points, raw.size(), st);
-            AM_CUDA(cudaStreamSynchronize(st));
-            for (size_t q = 0; q < 3 * (size_t)S; ++q)
-                pd[q] = tc == 8 ? ((const double *)raw.data())[q] : (double)((const float *)raw.data())[q];
-            if (ts == 8) {
-                upload(e->s_pts, pd.data(), sizeof(double) * pd.size(), st);
-            } else {
-                std::vector<float> pf(pd.begin(), pd.end());
-                upload(e->s_pts, pf.data(), sizeof(float) * pf.size(), st);
-            }
-            AM_CUDA(cudaStreamSynchronize(st));
-        }
-        AM_CUDA(e->s_keys.reserve(sizeof(uint32_t) * (size_t)S * e->W));
-        AM_CUDA(e->s_hash.reserve(sizeof(uint64_t) * (size_t)S));
-        AM_CUDA(e->s_rec.reserve(sizeof(int32_t) * (size_t)S));
-
-        e->num_regions = 0;
-        e->hcap = 0;
-        e->stats = am_stats{};
-        AM_CUDA(cudaMemsetAsync(e->d_tail.p, 0, sizeof(long long), st));
-        AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
-        const int chunk = e->default_chunk();
-        e->ensure_chunk(std::min(chunk, std::max(S, 1024)));
-        e->ensure_regions(std::max<long long>(S, 1) + (long long)chunk * kVMax);
-        e->ensure_table((long long)S + (long long)chunk * kVMax, false);
-        AM_CUDA(e->blocksum.grow(sizeof(int) * ((size_t)S / 1024 + 2), 0, st));
-        AM_CUDA(cudaStreamSynchronize(st));
-
-        long long launches = 0;
-        AM_CUDA(cudaEventRecord(ev0, st));
-        launch_seed_pack(e->s_states.as<uint8_t>(), S, e->N, e->W, e->s_keys.as<uint32_t>(), e->s_hash.as<uint64_t>(), st);
-        launch_seed_insert(e->s_keys.as<uint32_t>(), e->s_hash.as<uint64_t>(), S, e->W, e->hashdev(),
-                           e->s_rec.as<int32_t>(), e->d_err.as<int>(), st);
-        {
-            ChunkDev sc{};
-            sc.rec = e->s_rec.as<int32_t>();
-            launch_append(1, prec, net, e->regions(), sc, e->hashdev(), e->s_keys.as<uint32_t>(),
-                          e->s_hash.as<uint64_t>(), e->s_pts.p, S, e->d_tail.as<long long>(), e->blocksum.as<int>(),
-                          (int)(e->blocksum.bytes / sizeof(int)), e->d_err.as<int>(), st);
-        }
-        launches += 5;
-        AM_CUDA(cudaGetLastError());
-        long long tail = e->poll();
-        e->num_regions = tail;
-        e->stats.num_seeds = tail;
-
-        const Tolerances tol = prec == kFloat64 ? Tolerances{1e-20, 3e-14, 1e-12} : Tolerances{1e-12, 3e-7, 1e-6};
-        long long head = 0;
-        int chunks = 0;
-        double t_comp = 0, t_poly = 0, t_front = 0;
+        run_begin(e, a);
         if (e->use_graph && !e->phase_timing) {
-            // graph-driven loop: one graph launch runs every wave until the
-            // queue is empty; it stops early only when the next wave's
-            // children might not fit, and then resumes after the host grows
-            // the region store and the table
-            e->ensure_chunk(chunk);
-            while (head < tail) {
-                const int count = (int)std::min<long long>(tail - head, chunk);
-                e->ensure_regions(tail + (long long)count * kVMax);
-                e->ensure_table(std::max<long long>(tail + (long long)count * kVMax, e->cap), true);
-                WaveCtl *h = e->h_ctl;
-                h->head = head;
-                h->count = count;
-                h->waves = 0;
-                h->limit = std::min<long long>(e->cap, (long long)(e->hcap / 2));
-                h->chunk_cap = chunk;
-                h->work = 0u;
-                // tail and err stay as the device has them
-                AM_CUDA(cudaMemcpyAsync((char *)e->d_tail.p + offsetof(WaveCtl, head), (char *)h + offsetof(WaveCtl, head),
-                                        sizeof(WaveCtl) - offsetof(WaveCtl, head), cudaMemcpyHostToDevice, st));
-                e->run_wave_graph(prec, net, iso, tol, chunk);
-                tail = e->poll(sizeof(WaveCtl));
-                chunks += h->waves;
-                launches += 6ll * h->waves;
-                head = h->head;
-                e->num_regions = tail;
-                AM_CHECK(h->waves < kMaxWaves, "wave bound reached");
+            while (e->run.head < e->run.tail) {
+                run_graph_launch(e, kMaxWaves);
+                AM_CUDA(cudaStreamSynchronize(e->st));
+                run_graph_done(e);
             }
+        } else {
+            run_host_loop(e);
         }
-        while (head < tail) {
-            const int count = (int)std::min<long long>(tail - head, chunk);
-            e->ensure_chunk(count);
-            e->ensure_regions(tail + (long long)count * kVMax);
-            e->ensure_table(tail + (long long)count * kVMax, true);
-            ChunkDev ch;
-            ch.head = head;
-            ch.count = count;
-            ch.cons = e->cons.p;
-            ch.eq = e->eq.p;
-            ch.rec = e->rec.as<int32_t>();
-            const RegionsDev reg = e->regions();
-            const HashDev hs = e->hashdev();
-            float ms = 0;
-            if (e->phase_timing) AM_CUDA(cudaEventRecord(pa, st));
-            if (prec == kMixed)
-                launch_compose_tc(net, e->tcnet, reg, ch, iso, e->d_err.as<int>(), st);
-            else
-                launch_compose(prec, net, reg, ch, iso, st);
-            if (e->phase_timing) {
-                AM_CUDA(cudaEventRecord(pb, st));
-                AM_CUDA(cudaEventSynchronize(pb));
-                AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
-                t_comp += ms;
-                AM_CUDA(cudaEventRecord(pa, st));
-            }
-            launch_polygon(prec, net, reg, ch, hs, tol, e->d_err.as<int>(), st);
-            if (e->phase_timing) {
-                AM_CUDA(cudaEventRecord(pb, st));
-                AM_CUDA(cudaEventSynchronize(pb));
-                AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
-                t_poly += ms;
-                AM_CUDA(cudaEventRecord(pa, st));
-            }
-            launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, count * kVMax, e->d_tail.as<long long>(),
-                          e->blocksum.as<int>(), (int)(e->blocksum.bytes / sizeof(int)), e->d_err.as<int>(), st);
-            if (e->phase_timing) {
-                AM_CUDA(cudaEventRecord(pb, st));
-                AM_CUDA(cudaEventSynchronize(pb));
-                AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
-                t_front += ms;
-            }
-            launches += 5;
-            AM_CUDA(cudaGetLastError());
-            head += count;
-            tail = e->poll();
-            e->num_regions = tail;
-            chunks++;
-        }
-        AM_CUDA(cudaEventRecord(ev1, st));
-        AM_CUDA(cudaEventSynchronize(ev1));
-        float total = 0;
-        AM_CUDA(cudaEventElapsedTime(&total, ev0, ev1));
-        e->check_err();
-
-        // statistics
-        am_stats &sx = e->stats;
-        sx.num_regions = tail;
-        sx.chunks = chunks;
-        sx.am_time_ms = total;
-        sx.compose_ms = t_comp;
-        sx.polygon_ms = t_poly;
-        sx.frontier_ms = t_front;
-        sx.kernel_launches = launches;
-        {
-            std::vector<int32_t> hn((size_t)tail);
-            std::vector<int8_t> hsx((size_t)tail);
-            AM_CUDA(cudaMemcpyAsync(hn.data(), e->nv.p, sizeof(int32_t) * tail, cudaMemcpyDeviceToHost, st));
-            AM_CUDA(cudaMemcpyAsync(hsx.data(), e->status.p, sizeof(int8_t) * tail, cudaMemcpyDeviceToHost, st));
-            AM_CUDA(cudaStreamSynchronize(st));
-            for (long long r = 0; r < tail; ++r) {
-                if (hn[r] >= 3) sx.num_faces++;
-                sx.max_polygon_verts = std::max(sx.max_polygon_verts, hn[r]);
-                switch (hsx[r]) {
-                case kNoStart: sx.num_nostart++; break;
-                case kOpen: sx.num_open++; break;
-                case kTruncated: sx.num_truncated++; break;
-                case kSingular: sx.num_singular++; break;
-                default: break;
-                }
-            }
-        }
-        e->flip = flip_insideout ? 1 : 0;
-        e->iso = iso;
-        e->has_am = true;
+        run_end(e);
     });
+}
+
+int am_run_batch(am_engine *const *engines, const am_run_args *args, int count, double *wall_ms)
+{
+    if (!engines || !args || count < 1) return AM_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < count; ++i) {
+        if (!engines[i]) return AM_ERR_NOT_INITIALIZED;
+        for (int j = 0; j < i; ++j)
+            if (engines[j] == engines[i]) return AM_ERR_INVALID_ARGUMENT; // one run per engine
+    }
+    // the GPU is divided among the networks still marching (a power of two,
+    // so that each engine re-captures its wave graph only a few times); a
+    // graph launch runs at most kBatchWaves waves before its share is revised
+    constexpr int kBatchWaves = 8;
+    auto share_for = [](int active) {
+        int s = 1;
+        while (s < active) s <<= 1;
+        return s;
+    };
+    std::vector<char> active((size_t)count, 0);
+    int n_active = count;
+    // begin each network and start its wave loop right away, on its own stream
+    for (int i = 0; i < count; ++i) {
+        am_engine *e = engines[i];
+        const am_run_args &x = args[i];
+        e->has_am = false;
+        e->has_mesh = false;
+        e->lean = true;
+        e->share = share_for(n_active);
+        const RunArgs a{x.weights, x.biases, x.states, x.points, x.num_points, x.arc_tm, x.arc_tm_shapes,
+                        x.num_arc_tm, x.w_extra, x.b_extra, x.iso, x.flip_insideout, nullptr};
+        const int rc = guarded(e, [&] {
+            run_begin(e, a);
+            if (e->run.head < e->run.tail) {
+                run_graph_launch(e, kBatchWaves);
+                active[(size_t)i] = 1;
+            }
+        });
+        e->lean = false;
+        if (rc != AM_OK) return rc;
+    }
+    n_active = 0;
+    for (char a : active) n_active += a;
+    // serve whichever loop has stopped: finished, or due for a new share or
+    // a larger store
+    while (n_active > 0) {
+        bool progressed = false;
+        for (int i = 0; i < count; ++i) {
+            if (!active[(size_t)i]) continue;
+            am_engine *e = engines[i];
+            const cudaError_t q = cudaStreamQuery(e->st);
+            if (q == cudaErrorNotReady) continue;
+            progressed = true;
+            const int rc = guarded(e, [&] {
+                AM_CUDA(q);
+                if (!run_graph_done(e)) {
+                    active[(size_t)i] = 0;
+                    --n_active;
+                    return;
+                }
+                e->lean = true;
+                e->share = share_for(n_active);
+                run_graph_launch(e, kBatchWaves);
+                e->lean = false;
+            });
+            if (rc != AM_OK) return rc;
+        }
+        if (!progressed) std::this_thread::yield();
+    }
+    float wall = 0.f;
+    for (int i = 0; i < count; ++i) {
+        am_engine *e = engines[i];
+        e->share = 1;
+        const int rc = guarded(e, [&] {
+            run_end(e);
+            float ms = 0.f;
+            AM_CUDA(cudaEventElapsedTime(&ms, engines[0]->ev0, e->ev1));
+            wall = std::max(wall, ms);
+        });
+        if (rc != AM_OK) return rc;
+    }
+    if (wall_ms) *wall_ms = wall;
+    return AM_OK;
 }
 
 int am_get_stats(const am_engine *e, am_stats *out)

@@ -274,7 +274,7 @@ __global__ void wave_step_kernel(WaveCtl *ctl, cudaGraphConditionalHandle cond)
     c.count = (int)(rem < (long long)c.chunk_cap ? (rem > 0 ? rem : 0) : (long long)c.chunk_cap);
     c.work = 0u;
     const bool go = c.count > 0 && (c.err & (kErrTableFull | kErrCapacity)) == 0 &&
-                    c.tail + (long long)c.count * kVMax <= c.limit && c.waves < kMaxWaves;
+                    c.tail + (long long)c.count * kVMax <= c.limit && c.waves < c.max_waves;
     cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 
@@ -326,7 +326,7 @@ void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg,
     a.blockoff = d_blocksum;
     a.err = d_err;
     int nb = (n_items + kScanBlock - 1) / kScanBlock;
-    if (ch.ctl) nb = std::min(nb, 2 * device_sms()); // several tiles per block
+    if (ch.ctl) nb = std::min(nb, std::max(1, 2 * device_sms() / std::max(ch.share, 1))); // several tiles per block
     if (nb > nblocks_cap) { // the host sizes d_blocksum for the largest chunk
         int e = kErrCapacity;
         cudaMemcpyAsync(d_err, &e, sizeof(int), cudaMemcpyHostToDevice, st);

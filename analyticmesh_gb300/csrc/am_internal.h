@@ -79,6 +79,8 @@ struct WaveCtl {
     long long limit;    // go on only while tail + count * kVMax <= limit
     int chunk_cap;      // largest wave
     unsigned int work;  // next region of the wave for the polygon warps
+    int max_waves;      // waves one graph launch may run
+    int pad1;
 };
 
 struct ChunkDev {
@@ -88,6 +90,7 @@ struct ChunkDev {
     void *eq;           // [count][4] TC face plane (b already offset by iso)
     int32_t *rec;       // [count * kVMax] hash slot claimed by each child, -1 none
     WaveCtl *ctl = nullptr; // set: head and count come from the device (graph-driven loop)
+    int share = 1;          // graph-driven loop: networks sharing the GPU (fixed grids are divided by it)
 };
 
 #ifdef __CUDACC__

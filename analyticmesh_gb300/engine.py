@@ -195,6 +195,41 @@ class Engine:
         return Regions(N=self.N, **d)
 
 
+def run_batch(engines, nets, states_list, points_list, iso=0.0, flip_insideout=False):
+    """am_run_batch: march every network at once, each on its engine (made
+    for that network); returns the device wall time in ms.  Inputs may be
+    numpy arrays or tensors, on the host or the device."""
+    n = len(engines)
+    if not (len(nets) == len(states_list) == len(points_list) == n) or n == 0:
+        raise ValueError("one network, state set and point set per engine")
+    k = _Keep()
+    args = (_lib.AmRunArgs * n)()
+    for i, (eng, net, st, pt) in enumerate(zip(engines, nets, states_list, points_list)):
+        dt = _np_dtype(eng.float_type)
+        a = args[i]
+        a.weights = C.cast(k.ptr_array(net.W, dt), C.c_void_p)
+        a.biases = C.cast(k.ptr_array(net.b, dt), C.c_void_p)
+        a.states = k.ptr(st, np.uint8)
+        a.points = k.ptr(pt, dt)
+        a.num_points = int(st.shape[0])
+        shapes = np.ascontiguousarray([s for t in net.tms for s in tuple(t.shape)] or [0], dtype=np.int32)
+        k.objs.append(shapes)
+        a.arc_tm = C.cast(k.ptr_array(net.tms, dt), C.c_void_p)
+        a.arc_tm_shapes = shapes.ctypes.data
+        a.num_arc_tm = len(net.tms)
+        a.w_extra = k.ptr(net.w_extra, dt) if eng.E else None
+        a.b_extra = k.ptr(net.b_extra, dt) if eng.E else None
+        a.iso = float(iso)
+        a.flip_insideout = 1 if flip_insideout else 0
+    handles = (C.c_void_p * n)(*[e.h for e in engines])
+    wall = C.c_double(0.0)
+    rc = _lib.lib().am_run_batch(handles, args, n, C.byref(wall))
+    if rc != 0:
+        bad = next((e for e in engines if _lib.lib().am_last_error(e.h)), engines[0])
+        _lib.check(rc, bad.h)
+    return wall.value
+
+
 def march(net, states, points, float_type="float32", iso=0.0, flip_insideout=False, chunk=None, phase_timing=False):
     """One-shot: Init + AnalyticMarching on a ``workloads.NetArrays``; returns the engine."""
     eng = Engine(float_type, net.nodes, net.arc_table, net.num_extra)

@@ -138,21 +138,29 @@ def batched(count: int = 64, first_seed: int = 100) -> List[MLP]:
 
 
 def seeds_for(model: MLP, init_num: int = 1024, seed: int = 1234, iso: float = 0.0, w_extra=None, b_extra=None,
-              **kw):
+              device="cpu", **kw):
     """Dichotomy seed points and their activation states.  States are taken
-    from a float64 forward pass.  Returns (states uint8 (S, N), points float64 (S, 3))."""
+    from a float64 forward pass.  Returns (states uint8 (S, N), points float64 (S, 3)).
+    ``device`` runs the network there (the samples come from a CPU generator)."""
     g = torch.Generator().manual_seed(seed)
-    model = model.cpu().float().eval()
+    model = _float_copy(model).to(device).eval()
     we = None if w_extra is None else torch.as_tensor(w_extra, dtype=torch.float32)
     be = None if b_extra is None else torch.as_tensor(b_extra, dtype=torch.float32)
-    pts = dichotomy(model, iso, init_num=init_num, generator=g, w_extra_constraints=we, b_extra_constraints=be, **kw)
-    md = _double_copy(model)
+    pts = dichotomy(model, iso, init_num=init_num, generator=g, w_extra_constraints=we, b_extra_constraints=be,
+                    device=device, **kw)
+    md = _double_copy(model).to(device)
     with torch.no_grad():
         z = md.pre_activations(pts.double())
-    return (z > 0).numpy().astype(np.uint8), pts.double().numpy()
+    return (z > 0).cpu().numpy().astype(np.uint8), pts.double().cpu().numpy()
+
+
+def _float_copy(model: MLP) -> MLP:
+    m = MLP(model.nodes, model.arc_table, model.arc_tm_shape, initialization=None, enable_print=False)
+    m.load_state_dict(model.state_dict())
+    return m.float()
 
 
 def _double_copy(model: MLP) -> MLP:
     m = MLP(model.nodes, model.arc_table, model.arc_tm_shape, initialization=None, enable_print=False)
-    m.load_state_dict(model.state_dict())
+    m.load_state_dict({k: v.cpu() for k, v in model.state_dict().items()})
     return m.double()

@@ -45,7 +45,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--form", default="mixed", choices=["mixed", "float32", "float64"])
-    p.add_argument("--workload", default="sphere", choices=["sphere", "deep", "large_skip", "polytope"])
+    p.add_argument("--workload", default="sphere", choices=["sphere", "deep", "large_skip", "polytope", "batched"])
+    p.add_argument("--nets", type=int, default=64, help="batched workload: number of networks")
     p.add_argument("--seeds", type=int, default=1024)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--profile", action="store_true",
@@ -223,11 +224,109 @@ def cpu_baseline(net, states, points, dtype):
                 "sample": "full workload, oracle restatement (%s)" % type(exc).__name__}
 
 
+def bench_batched(args, ws, rank, local):
+    """--workload batched: the 64-network workload (seeds 100..163, widths
+    from {32, 64, 128, 256, 512}, depths 2..8, geometric init + N(0, 0.01)),
+    every network with its own dichotomy seeds.  Chosen form: mixed
+    precision, all networks marched at once (am_run_batch).  Plain form: FP32,
+    one network after the other (am_analytic_marching each), as a user of the
+    reference marches them (it re-Inits per architecture)."""
+    import numpy as np
+    import torch
+
+    from analyticmesh_gb300 import engine, workloads as wl
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    models = wl.batched(args.nets, 100)
+    nets, sts, pts = [], [], []
+    for i, m in enumerate(models):
+        nets.append(wl.net_arrays(m))
+        st, pt = wl.seeds_for(m, init_num=args.seeds, seed=100 + i, device=dev)
+        sts.append(torch.tensor(st, device=dev))
+        pts.append(torch.tensor(pt, device=dev))
+
+    def dev_net(n, dt):
+        d = dict(W=[torch.tensor(w, dtype=dt, device=dev) for w in n.W], b=[torch.tensor(b, dtype=dt, device=dev) for b in n.b],
+                 tms=[torch.tensor(t, dtype=dt, device=dev) for t in n.tms], w_extra=n.w_extra, b_extra=n.b_extra)
+        return type("DevNet", (), d)
+
+    dnets = [dev_net(n, torch.float32) for n in nets]
+    pts = [p.float() for p in pts]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    chosen = [engine.Engine("mixed", n.nodes, n.arc_table, n.num_extra) for n in nets]
+    for _ in range(args.warmup):
+        engine.run_batch(chosen, dnets, sts, pts)
+    times, faces = [], 0
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            wall = engine.run_batch(chosen, dnets, sts, pts)
+            times.append(wall / 1e3)
+            faces = sum(e.stats()["num_faces"] for e in chosen)
+    value = ws * faces / (sum(times) / len(times))
+    clocks = clk.summary()
+    regions = [e.stats()["num_regions"] for e in chosen]
+
+    # end to end: host inputs copied in, every mesh welded and read back
+    hnets = [n for n in nets]
+    t0 = time.perf_counter()
+    engine.run_batch(chosen, hnets, [s.cpu().numpy() for s in sts], [p.cpu().numpy() for p in pts])
+    meshes = [e.combine() for e in chosen]
+    e2e = ws * faces / (time.perf_counter() - t0)
+    h2d = sum(np.asarray(x, np.float32).nbytes for n in nets for x in n.W + n.b + n.tms) + \
+        sum(int(s.numel()) + int(p.numel()) * 4 for s, p in zip(sts, pts))
+    d2h = sum(m.verts.nbytes + m.face_sizes.nbytes + m.face_indices.nbytes for m in meshes)
+
+    # plain form: FP32, one network at a time
+    plain_engines = [engine.Engine("float32", n.nodes, n.arc_table, n.num_extra) for n in nets]
+    for e, n, s_, p_ in zip(plain_engines, dnets, sts, pts):
+        e.run(n.W, n.b, s_, p_, n.tms)
+    torch.cuda.synchronize()
+    pt = []
+    for _ in range(max(1, args.steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        f = 0
+        for e, n, s_, p_ in zip(plain_engines, dnets, sts, pts):
+            f += e.run(n.W, n.b, s_, p_, n.tms)["num_faces"]
+        ev1.record()
+        ev1.synchronize()
+        pt.append(f / (ev0.elapsed_time(ev1) / 1e3))
+    plain = ws * statistics.mean(pt)
+    for e in chosen + plain_engines:
+        e.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": "analytic_faces_per_sec", "value": value, "unit": "faces/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (bf16x3 composition, f64 solves)",
+        "data": "synthetic (seeded networks and dichotomy seed points)",
+        "config": {"workload": "%d MLPs, seeds 100..%d, widths {32..512}, depths 2..8, all marched at once"
+                               % (args.nets, 99 + args.nets), "seeds": args.seeds, "form": "mixed, batched",
+                   "faces_per_step": faces, "regions_per_step": int(sum(regions)),
+                   "largest_network_regions": int(max(regions)), "l2": "256 MiB flush before every timed step",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": "faces/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "plain_fp32_value": plain, "plain_form": "float32, networks one after the other",
+        "chosen_vs_plain": value / plain, "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, ws)
+        return
+    if args.workload == "batched":
+        bench_batched(args, ws, rank, local)
         return
     import numpy as np
     import torch

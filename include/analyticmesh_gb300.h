@@ -107,6 +107,33 @@ int am_get_regions(am_engine *engine, uint32_t *bits, int32_t *nverts, double *v
                    double *seeds, int32_t *start);
 int am_vert_capacity(void);
 
+/* ---- batched marching of many networks (no counterpart in the reference,
+ * which marches one network per Init / AnalyticMarching pair and re-Inits
+ * when the architecture changes, backend/main.py:437-446).  engines[i] is an
+ * engine from am_init for network i (any widths, depths, precisions); args[i]
+ * holds the arguments am_analytic_marching would take for it.  Every
+ * network's wave loop runs on the device on the engine's own stream, all of
+ * them side by side, the grids sized for `count` networks sharing the GPU.
+ * Afterwards each engine holds its own result (am_get_stats,
+ * am_combine_mesh, ...), exactly as after am_analytic_marching.  wall_ms
+ * (optional) receives the device time from the first network's start to the
+ * last network's end. */
+typedef struct {
+    const void *const *weights;
+    const void *const *biases;
+    const uint8_t *states;
+    const void *points;
+    int num_points;
+    const void *const *arc_tm;
+    const int32_t *arc_tm_shapes;
+    int num_arc_tm;
+    const void *w_extra;
+    const void *b_extra;
+    double iso;
+    int flip_insideout;
+} am_run_args;
+int am_run_batch(am_engine *const *engines, const am_run_args *args, int count, double *wall_ms);
+
 /* Constraint rows of regions [first, first + count) of the last run,
  * recomposed with the engine's composition path (no counterpart in the
  * reference, where they live only inside a batch): rows count x ALL x 4
