@@ -214,7 +214,7 @@ __global__ void prepare_weights_kernel(const T *src, int M, int K, int Mp, T *ds
 void launch_compose(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, double iso, cudaStream_t st)
 {
     if (!ch.ctl && ch.count <= 0) return;
-    const int grid = ch.ctl ? std::max(1, device_sms() * 4 / std::max(ch.share, 1)) : (ch.count + kR - 1) / kR;
+    const int grid = ch.ctl ? device_sms() * 4 : (ch.count + kR - 1) / kR;
     if (prec == kFloat64)
         compose_kernel<double><<<grid, kThreads, 0, st>>>(net, reg, ch, iso);
     else

@@ -7,8 +7,9 @@
 // columns each, UMMA N = 4 x regions, chosen per launch from the chunk size so
 // that small frontier waves still spread over every SM) and keeps the masked
 // operand X_l = diag(s_l) A_l on chip the whole way through the network, as
-// bf16 terms in 128B-swizzled K-major shared memory: the B operand of
-// tcgen05.mma.  The layer weights are the A operand; they are pre-split and
+// bf16 terms in 128B-swizzled shared memory (MN-major, or K-major for layers
+// too wide for 64-column atoms): the B operand of tcgen05.mma.  The layer
+// weights are the A operand (K-major); they are pre-split and
 // stored in global memory as the exact shared-memory image of their 128 x 64
 // blocks, so one bulk copy (cp.async.bulk, completing on an mbarrier) stages a
 // block while the tensor core works on the previous one, and the first blocks
@@ -22,8 +23,8 @@
 // grows with the number of accumulate steps into one accumulator, so the
 // dominant hh product and the five small correction products accumulate in
 // two separate TMEM accumulators that the epilogue adds once: fp32-level
-// constraint rows.  The epilogue (eight warps; warps w and w + 4 share TMEM
-// lanes 32 (w % 4).. and split the columns) reads the accumulators with
+// constraint rows.  The epilogue (sixteen warps; the warps w with equal w % 4
+// share TMEM lanes 32 (w % 4).. and split the columns) reads the accumulators with
 // tcgen05.ld (one TMEM lane per output unit), adds bias and skips, writes the
 // sign-flipped constraint rows to HBM for the polygon kernel, and writes the
 // next layer's masked operand straight back into shared memory.  The face
@@ -602,8 +603,7 @@ void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg
     const int sms = device_sms();
     const size_t smem_max = tc_smem_bytes(tc, tc.ncols_max, net.W);
     cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-    // one resident tile per SM (per SM share when several networks march at once)
-    const int slots = std::max(1, sms / std::max(ch.share, 1));
+    const int slots = sms; // one resident tile per SM
     if (ch.ctl) { // wave size known on the device only: every resident tile slot, tiles strided
         compose_tc_kernel<<<slots, kThreads, smem_max, st>>>(net, tc, reg, ch, (float)iso, slots, d_err);
         return;

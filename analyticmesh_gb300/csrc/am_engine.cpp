@@ -26,6 +26,28 @@ using namespace am;
 
 namespace {
 
+// While a batch runs, device frees wait until its end: cudaFree synchronises
+// the whole device and would stall every other network's stream.
+thread_local std::vector<void *> *t_deferred_frees = nullptr;
+
+void release_device(void *p)
+{
+    if (!p) return;
+    if (t_deferred_frees) t_deferred_frees->push_back(p);
+    else cudaFree(p);
+}
+
+struct DeferFrees {
+    std::vector<void *> list;
+    DeferFrees() { t_deferred_frees = &list; }
+    ~DeferFrees()
+    {
+        t_deferred_frees = nullptr;
+        if (!list.empty()) cudaDeviceSynchronize();
+        for (void *p : list) cudaFree(p);
+    }
+};
+
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
@@ -35,7 +57,7 @@ struct DevBuf {
     ~DevBuf() { reset(); }
     void reset()
     {
-        if (p) cudaFree(p);
+        release_device(p);
         p = nullptr;
         bytes = 0;
     }
@@ -70,7 +92,7 @@ struct DevBuf {
             }
             cudaStreamSynchronize(st);
         }
-        if (p) cudaFree(p);
+        release_device(p);
         p = q;
         bytes = n;
         return cudaSuccess;
@@ -178,7 +200,6 @@ struct am_engine {
         bool flip = false;
     } run;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, pa = nullptr, pb = nullptr;
-    int share = 1; // networks marching side by side on the GPU (graph-driven grids are divided by it)
     bool lean = false; // batch member: region store and table start small and grow on demand
     void ensure_events()
     {
@@ -315,7 +336,6 @@ struct am_engine {
         const void *bufs[6] = {cons.p, eq.p, rec.p, blocksum.p, d_tail.p, (const void *)blocksum.bytes};
         add(&prec, sizeof(prec));
         add(&chunk, sizeof(chunk));
-        add(&share, sizeof(share));
         add(&iso, sizeof(iso));
         add(&tol, sizeof(tol));
         add(&net, sizeof(net));
@@ -345,7 +365,6 @@ struct am_engine {
                 ch.eq = eq.p;
                 ch.rec = rec.as<int32_t>();
                 ch.ctl = ctl();
-                ch.share = share;
                 if (prec == kMixed)
                     launch_compose_tc(net, tcnet, reg, ch, iso, d_err.as<int>(), st);
                 else
@@ -907,7 +926,6 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
     if (!e) return AM_ERR_NOT_INITIALIZED;
     e->has_am = false;
     e->has_mesh = false;
-    e->share = 1;
     const RunArgs a{weights, biases, states, points, num_points, arc_tm, arc_tm_shapes, num_arc_tm,
                     w_extra, b_extra, iso, flip_insideout, stream};
     return guarded(e, [&] {
@@ -933,41 +951,32 @@ int am_run_batch(am_engine *const *engines, const am_run_args *args, int count, 
         for (int j = 0; j < i; ++j)
             if (engines[j] == engines[i]) return AM_ERR_INVALID_ARGUMENT; // one run per engine
     }
-    // the GPU is divided among the networks still marching (a power of two,
-    // so that each engine re-captures its wave graph only a few times); a
-    // graph launch runs at most kBatchWaves waves before its share is revised
-    constexpr int kBatchWaves = 8;
-    auto share_for = [](int active) {
-        int s = 1;
-        while (s < active) s <<= 1;
-        return s;
-    };
+    DeferFrees defer;
     std::vector<char> active((size_t)count, 0);
-    int n_active = count;
-    // begin each network and start its wave loop right away, on its own stream
+    // begin each network and start its wave loop right away, on its own
+    // stream, with full grids: a network whose waves fill the GPU runs as
+    // fast as alone, the waves of smaller ones fill the gaps
     for (int i = 0; i < count; ++i) {
         am_engine *e = engines[i];
         const am_run_args &x = args[i];
         e->has_am = false;
         e->has_mesh = false;
-        e->lean = true;
-        e->share = share_for(n_active);
+        e->lean = true; // stores start small and grow on demand
         const RunArgs a{x.weights, x.biases, x.states, x.points, x.num_points, x.arc_tm, x.arc_tm_shapes,
                         x.num_arc_tm, x.w_extra, x.b_extra, x.iso, x.flip_insideout, nullptr};
         const int rc = guarded(e, [&] {
             run_begin(e, a);
             if (e->run.head < e->run.tail) {
-                run_graph_launch(e, kBatchWaves);
+                run_graph_launch(e, kMaxWaves);
                 active[(size_t)i] = 1;
             }
         });
         e->lean = false;
         if (rc != AM_OK) return rc;
     }
-    n_active = 0;
+    int n_active = 0;
     for (char a : active) n_active += a;
-    // serve whichever loop has stopped: finished, or due for a new share or
-    // a larger store
+    // serve whichever loop has stopped: finished, or waiting for a larger store
     while (n_active > 0) {
         bool progressed = false;
         for (int i = 0; i < count; ++i) {
@@ -978,15 +987,12 @@ int am_run_batch(am_engine *const *engines, const am_run_args *args, int count, 
             progressed = true;
             const int rc = guarded(e, [&] {
                 AM_CUDA(q);
-                if (!run_graph_done(e)) {
+                if (run_graph_done(e)) {
+                    run_graph_launch(e, kMaxWaves);
+                } else {
                     active[(size_t)i] = 0;
                     --n_active;
-                    return;
                 }
-                e->lean = true;
-                e->share = share_for(n_active);
-                run_graph_launch(e, kBatchWaves);
-                e->lean = false;
             });
             if (rc != AM_OK) return rc;
         }
@@ -995,7 +1001,6 @@ int am_run_batch(am_engine *const *engines, const am_run_args *args, int count, 
     float wall = 0.f;
     for (int i = 0; i < count; ++i) {
         am_engine *e = engines[i];
-        e->share = 1;
         const int rc = guarded(e, [&] {
             run_end(e);
             float ms = 0.f;
@@ -1082,6 +1087,14 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
         e->stats.mesh_num_faces = F;
         e->stats.mesh_num_indices = I;
         e->has_mesh = true;
+        // the mesh now lives on the host: large weld buffers go back (many
+        // engines of a batch weld one after the other)
+        DevBuf *weld[] = {&e->w_table, &e->w_rep, &e->w_flag, &e->w_vidx, &e->w_bsum, &e->w_fflag, &e->w_fsize,
+                          &e->w_fid, &e->w_foff, &e->w_verts, &e->w_fs, &e->w_fi};
+        size_t held = 0;
+        for (DevBuf *b : weld) held += b->bytes;
+        if (held > ((size_t)1 << 30))
+            for (DevBuf *b : weld) b->reset();
     });
 }
 

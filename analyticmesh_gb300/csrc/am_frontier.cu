@@ -326,7 +326,7 @@ void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg,
     a.blockoff = d_blocksum;
     a.err = d_err;
     int nb = (n_items + kScanBlock - 1) / kScanBlock;
-    if (ch.ctl) nb = std::min(nb, std::max(1, 2 * device_sms() / std::max(ch.share, 1))); // several tiles per block
+    if (ch.ctl) nb = std::min(nb, 2 * device_sms()); // several tiles per block
     if (nb > nblocks_cap) { // the host sizes d_blocksum for the largest chunk
         int e = kErrCapacity;
         cudaMemcpyAsync(d_err, &e, sizeof(int), cudaMemcpyHostToDevice, st);

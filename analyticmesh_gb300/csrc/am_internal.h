@@ -90,7 +90,6 @@ struct ChunkDev {
     void *eq;           // [count][4] TC face plane (b already offset by iso)
     int32_t *rec;       // [count * kVMax] hash slot claimed by each child, -1 none
     WaveCtl *ctl = nullptr; // set: head and count come from the device (graph-driven loop)
-    int share = 1;          // graph-driven loop: networks sharing the GPU (fixed grids are divided by it)
 };
 
 #ifdef __CUDACC__

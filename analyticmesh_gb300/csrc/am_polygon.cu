@@ -623,7 +623,7 @@ void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, co
     if (ch.ctl) { // wave size on the device: as many blocks as stay resident
         int per_sm = 1;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32 * wpb, smem);
-        grid = std::max(1, sms * std::max(per_sm, 1) / std::max(ch.share, 1));
+        grid = sms * std::max(per_sm, 1);
     } else {
         const long long need = (ch.count + wpb - 1) / wpb;
         grid = (int)std::min<long long>(need, (long long)sms * 16);

@@ -113,8 +113,8 @@ int am_vert_capacity(void);
  * engine from am_init for network i (any widths, depths, precisions); args[i]
  * holds the arguments am_analytic_marching would take for it.  Every
  * network's wave loop runs on the device on the engine's own stream, all of
- * them side by side, the grids sized for `count` networks sharing the GPU.
- * Afterwards each engine holds its own result (am_get_stats,
+ * them side by side: the waves of small networks fill the gaps the waves of
+ * large ones leave.  Afterwards each engine holds its own result (am_get_stats,
  * am_combine_mesh, ...), exactly as after am_analytic_marching.  wall_ms
  * (optional) receives the device time from the first network's start to the
  * last network's end. */
