@@ -121,9 +121,16 @@ def deep(seed: int = 2) -> MLP:
     return geometric([256] * 6, seed, radius=0.5, perturb=0.02)
 
 
+# The perturbation lifts the deep network above zero on the whole unit ball
+# (f grows with the radius from ~0.01 at the centre to ~0.75 at radius 1); its
+# level set at DEEP_ISO is a closed irregular surface near radius 0.5.
+DEEP_ISO = 0.35
+
+
 def large_skip(seed: int = 3) -> MLP:
-    # input added into the input of linear layer 4 (after hidden layer 4)
-    skips = [[0], [0], [0], [1, 0, 0], [0], [0], [0]]
+    # the input added into linear layer 4 (after hidden layer 4): the
+    # concatenation [h4 | x] of width 515 as W4 h4 + W4_x x
+    skips = [[0], [0], [0], [1, 0, 0], [0], [0], [0], [0]]
     return geometric([512] * 8, seed, radius=0.6, perturb=0.01, skips=skips, tm_shapes=[[512, 3]])
 
 

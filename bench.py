@@ -88,10 +88,14 @@ def workload(name, nseeds):
 
     model = {"sphere": wl.sphere, "deep": wl.deep, "large_skip": wl.large_skip, "polytope": wl.polytope}[name]()
     net = wl.net_arrays(model)
-    states, points = wl.seeds_for(model, init_num=nseeds, seed=1)
+    iso = wl.DEEP_ISO if name == "deep" else 0.0
+    states, points = wl.seeds_for(model, init_num=nseeds, seed=1, iso=iso)
     desc = {"sphere": "sphere MLP 3-[128]x4-1, seed 1", "deep": "perturbed MLP 3-[256]x6-1, seed 2",
             "large_skip": "skip MLP 3-[512]x8-1 (input into layer 4), seed 3",
             "polytope": "polytope MLP 3-14-1, seed 0"}[name]
+    if iso:
+        desc += ", level %g" % iso
+    net.iso = iso
     return net, states, points, desc
 
 
@@ -179,11 +183,12 @@ def run_reference(args, rank, ws):
     for i in range(args.warmup + args.steps):
         tm = {}
         if kind == "reference":
-            r = O.run_ref(net, states, points, dtype=dtype, threads=threads, region_budget=REF_SAMPLE_REGIONS, timing=tm)
+            r = O.run_ref(net, states, points, iso=net.iso, dtype=dtype, threads=threads, region_budget=REF_SAMPLE_REGIONS,
+                          timing=tm)
             secs = tm["am_seconds"]
         else:
             t0 = time.perf_counter()
-            r = O.run_oracle(net, states, points, dtype=dtype)
+            r = O.run_oracle(net, states, points, iso=net.iso, dtype=dtype)
             secs = time.perf_counter() - t0
         faces = int((r.nverts >= 3).sum())
         if i >= args.warmup:
@@ -213,13 +218,14 @@ def cpu_baseline(net, states, points, dtype):
         if not O.ref_available():
             build_ref.build_ref()
         tm = {}
-        r = O.run_ref(net, states, points, dtype=dtype, threads=threads, region_budget=REF_SAMPLE_REGIONS, timing=tm)
+        r = O.run_ref(net, states, points, iso=net.iso, dtype=dtype, threads=threads, region_budget=REF_SAMPLE_REGIONS,
+                      timing=tm)
         return {"value": float((r.nverts >= 3).sum()) / tm["am_seconds"], "unit": "faces/s", "cores": threads,
                 "kind": "reference", "sample": "first %d regions of the workload (reference loop built for the host, "
                                                 "OpenMP %d threads)" % (REF_SAMPLE_REGIONS, threads)}
     except Exception as exc:
         t0 = time.perf_counter()
-        r = O.run_oracle(net, states, points, dtype=dtype)
+        r = O.run_oracle(net, states, points, iso=net.iso, dtype=dtype)
         secs = time.perf_counter() - t0
         return {"value": float((r.nverts >= 3).sum()) / secs, "unit": "faces/s", "cores": threads, "kind": "port",
                 "sample": "full workload, oracle restatement (%s)" % type(exc).__name__}
@@ -352,7 +358,7 @@ def main():
     eng = engine.Engine(form, net.nodes, net.arc_table, net.num_extra)
 
     def step():
-        return eng.run(W, B, S, P, TM, None, None, 0.0, False, stream=stream)
+        return eng.run(W, B, S, P, TM, None, None, net.iso, False, stream=stream)
 
     for _ in range(args.warmup):
         step()
@@ -392,7 +398,7 @@ def main():
     e2e_rates, h2d, d2h = [], 0, 0
     for i in range(max(2, args.steps // 2) + 1):
         t0 = time.perf_counter()
-        s = eng.run(net.W, net.b, states.astype(np.uint8), points, net.tms, None, None, 0.0, False)
+        s = eng.run(net.W, net.b, states.astype(np.uint8), points, net.tms, None, None, net.iso, False)
         mesh = eng.combine()
         dt = time.perf_counter() - t0
         if i > 0:
@@ -431,14 +437,14 @@ def main():
         T32 = [t.float() for t in TM]
         P32 = P.float()
         for _ in range(2):
-            ep.run(W32, B32, S, P32, T32, None, None, 0.0, False, stream=stream)
+            ep.run(W32, B32, S, P32, T32, None, None, net.iso, False, stream=stream)
         pt = []
         for _ in range(max(3, args.steps // 2)):
             flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            s2 = ep.run(W32, B32, S, P32, T32, None, None, 0.0, False, stream=stream)
+            s2 = ep.run(W32, B32, S, P32, T32, None, None, net.iso, False, stream=stream)
             e1.record(stream)
             e1.synchronize()
             pt.append(s2["num_faces"] / (e0.elapsed_time(e1) / 1e3))
