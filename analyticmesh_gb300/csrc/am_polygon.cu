@@ -422,7 +422,7 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &
 // the reference's feasibility test computes as (w.x + b) * rsqrt(|w|^2)
 // (kernel.h:729-795).  TC is the scan precision, TS the solve precision.
 template <typename TC, typename TS>
-__global__ void __launch_bounds__(256) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
+__global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
                                                       int *err)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];

@@ -50,6 +50,9 @@ def parse():
                    help="batched workload: the first NETS of the 64 networks (all 64 take minutes per step)")
     p.add_argument("--seeds", type=int, default=1024)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--host-loop", action="store_true",
+                   help="drive the wave loop from the host (one launch sequence per wave): for ncu launch lists, "
+                        "which cannot see kernels inside conditional graphs")
     p.add_argument("--profile", action="store_true",
                    help="warm-up + timed steps only (for ncu launch lists): no e2e, phase, plain or CPU legs")
     return p.parse_args()
@@ -356,6 +359,8 @@ def main():
     stream = torch.cuda.current_stream(dev)
 
     eng = engine.Engine(form, net.nodes, net.arc_table, net.num_extra)
+    if args.host_loop:
+        eng.set_option(_lib.AM_OPT_GRAPH, 0)
 
     def step():
         return eng.run(W, B, S, P, TM, None, None, net.iso, False, stream=stream)
