@@ -35,6 +35,11 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 REF_SAMPLE_REGIONS = 65536
+# DRAM bytes (read + write) per region of the two heavy kernels on the sphere
+# workload in the mixed form, from one ncu capture each (a 12,672-region
+# wave): profiles/compose_tc_sphere_128x4.md, profiles/polygon_mixed_sphere_128x4.md
+NCU_TRAFFIC_PER_REGION = {("sphere", "mixed"): {"compose": (1.22e6 + 45.31e6) / 12672,
+                                                "polygon": (109.57e6 + 3.77e6) / 12672}}
 FLOPS_PER_REGION = {}
 
 
@@ -423,16 +428,21 @@ def main():
     flops = composition_flops(net.nodes, net.arc_table, net.tms) * regions
     elem = 8 if form == "float64" else 4
     poly_bytes = regions * (ALL * 4 * elem + 4 * elem + 12 * 6)
+    per_region = NCU_TRAFFIC_PER_REGION.get((args.workload, form), {})
     if phases["compose_ms"] >= phases["polygon_ms"]:
         ach = flops / (phases["compose_ms"] / 1e3) / 1e12
+        tr = per_region.get("compose")
         roof = {"kernel": "compose", "bound": "tensor", "achieved": ach, "peak": tflops, "unit": "TFLOP/s",
-                "frac": ach / tflops, "traffic": None, "peak_kind": peak_kind,
+                "frac": ach / tflops, "traffic": tr * regions if tr else None, "peak_kind": peak_kind,
                 "algorithmic": "%d FLOP/region x %d regions" % (flops // max(regions, 1), regions)}
     else:
         ach = poly_bytes / (phases["polygon_ms"] / 1e3) / 1e9
+        tr = per_region.get("polygon")
         roof = {"kernel": "polygon", "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
-                "frac": ach / hbm, "traffic": None, "peak_kind": peak_kind,
+                "frac": ach / hbm, "traffic": tr * regions if tr else None, "peak_kind": peak_kind,
                 "algorithmic": "%d B/region x %d regions" % (poly_bytes // max(regions, 1), regions)}
+    if roof["traffic"] is not None:
+        roof["traffic_note"] = "ncu dram bytes per region of one captured wave x regions per step (profiles/)"
 
     plain = None
     if form != "float32":
