@@ -284,7 +284,7 @@ struct am_engine {
         AM_CUDA(cons.alloc(tc * 4 * (size_t)ALLP * count));
         AM_CUDA(eq.alloc(tc * 4 * (size_t)count));
         AM_CUDA(rec.alloc(sizeof(int32_t) * (size_t)kVMax * count));
-        AM_CUDA(blocksum.alloc(sizeof(int) * ((size_t)count * kVMax / 1024 + 2)));
+        AM_CUDA(blocksum.alloc(sizeof(int) * ((size_t)count * kVMax / 1024 + 6)));
         chunk_cap = count;
     }
 
@@ -619,7 +619,7 @@ void run_begin(am_engine *e, const RunArgs &a)
     const long long first_wave = e->lean ? std::min<long long>(chunk, 4ll * S + 1024) : chunk;
     e->ensure_regions(std::max<long long>(S, 1) + first_wave * kVMax);
     e->ensure_table((long long)S + first_wave * kVMax, false);
-    AM_CUDA(e->blocksum.grow(sizeof(int) * ((size_t)S / 1024 + 2), 0, st));
+    AM_CUDA(e->blocksum.grow(sizeof(int) * ((size_t)S / 1024 + 6), 0, st));
     AM_CUDA(cudaStreamSynchronize(st));
 
     e->run.launches = 0;
@@ -634,7 +634,7 @@ void run_begin(am_engine *e, const RunArgs &a)
                       e->s_hash.as<uint64_t>(), e->s_pts.p, S, e->d_tail.as<long long>(), e->blocksum.as<int>(),
                       (int)(e->blocksum.bytes / sizeof(int)), e->d_err.as<int>(), st);
     }
-    e->run.launches += 5;
+    e->run.launches += 4;
     AM_CUDA(cudaGetLastError());
     const long long tail = e->poll();
     e->num_regions = tail;
@@ -689,7 +689,7 @@ bool run_graph_done(am_engine *e)
     AM_CHECK(h->waves < kMaxWaves, "wave bound reached");
     r.tail = h->tail;
     r.chunks += h->waves;
-    r.launches += 6ll * h->waves;
+    r.launches += 5ll * h->waves;
     r.head = h->head;
     e->num_regions = r.tail;
     return r.head < r.tail;
@@ -751,7 +751,7 @@ void run_host_loop(am_engine *e)
             AM_CUDA(cudaEventElapsedTime(&ms, pa, pb));
             t_front += ms;
         }
-        launches += 5;
+        launches += 4;
         AM_CUDA(cudaGetLastError());
         head += count;
         tail = e->poll();

@@ -8,8 +8,9 @@
 // is confirmed by comparing the keys.
 //
 // New regions are appended in candidate order: winners of the insert are
-// flagged, counted per block, scanned, and written at tail + prefix, so the
-// region ids of a run do not depend on thread scheduling.
+// flagged and counted per block; each block then writes its winners at the
+// tail plus the counts of the blocks before it, so the region ids of a run do
+// not depend on thread scheduling.
 #include <algorithm>
 #include <cuda/atomic>
 #include <cuda_runtime.h>
@@ -124,7 +125,8 @@ struct AppendArgs {
     const void *seed_points; // [S][3] TS
     int n_items;
     long long *tail;
-    int *blockoff;
+    int *blockoff;         // winners per block
+    long long *base;       // the tail before this append (written by the count pass)
     int *err;
 };
 
@@ -180,24 +182,7 @@ __global__ void __launch_bounds__(kScanBlock) append_count_kernel(AppendArgs a)
         sum += total;
     }
     if (threadIdx.x == 0) a.blockoff[blockIdx.x] = sum;
-}
-
-__global__ void __launch_bounds__(kScanBlock) append_offsets_kernel(AppendArgs a, int nblocks)
-{
-    __shared__ long long base;
-    if (threadIdx.x == 0) base = *a.tail;
-    __syncthreads();
-    for (int b0 = 0; b0 < nblocks; b0 += kScanBlock) {
-        const int b = b0 + threadIdx.x;
-        const int v = b < nblocks ? a.blockoff[b] : 0;
-        int total;
-        const int pre = block_exclusive_scan(v, &total);
-        if (b < nblocks) a.blockoff[b] = (int)(base + pre);
-        __syncthreads();
-        if (threadIdx.x == 0) base += total;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *a.tail = base;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *a.base = *a.tail;
 }
 
 template <typename TS>
@@ -244,15 +229,22 @@ __device__ void append_one(const AppendArgs &a, int q, long long rid, long long 
     a.hs.slots[a.ch.rec[q]] = slot_value(fp_of(h), 0, (uint32_t)rid);
 }
 
+// Appends this block's winners after the winners of every block before it
+// (the block sums them itself: at most a few thousand counts); the last
+// block moves the tail.
 template <typename TS>
 __global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
 {
     long long head;
     int n;
     append_range(a, head, n);
+    int part = 0;
+    for (int b = threadIdx.x; b < (int)blockIdx.x; b += kScanBlock) part += a.blockoff[b];
+    int before;
+    block_exclusive_scan(part, &before); // (its total: the winners of every earlier block)
+    long long base = *a.base + before;
     const int span = block_span(n);
     const int q1 = min(n, (int)blockIdx.x * span + span);
-    long long base = a.blockoff[blockIdx.x];
     for (int q0 = (int)blockIdx.x * span; q0 < q1; q0 += kScanBlock) {
         const int q = q0 + (int)threadIdx.x;
         int total;
@@ -261,6 +253,7 @@ __global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
         if (f) append_one<TS>(a, q, base + pre, head);
         base += total;
     }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) *a.tail = base;
 }
 
 // graph-driven loop: retire the wave, take the next one from the queue and
@@ -327,13 +320,15 @@ void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg,
     a.err = d_err;
     int nb = (n_items + kScanBlock - 1) / kScanBlock;
     if (ch.ctl) nb = std::min(nb, 2 * device_sms()); // several tiles per block
-    if (nb > nblocks_cap) { // the host sizes d_blocksum for the largest chunk
+    // d_blocksum: nb block counts, then (8-byte aligned) the tail snapshot
+    const int base_slot = (nblocks_cap - 2) & ~1;
+    if (nb > base_slot) { // the host sizes d_blocksum for the largest chunk
         int e = kErrCapacity;
         cudaMemcpyAsync(d_err, &e, sizeof(int), cudaMemcpyHostToDevice, st);
         return;
     }
+    a.base = reinterpret_cast<long long *>(d_blocksum + base_slot);
     append_count_kernel<<<nb, kScanBlock, 0, st>>>(a);
-    append_offsets_kernel<<<1, kScanBlock, 0, st>>>(a, nb);
     if (prec == kFloat32)
         append_write_kernel<float><<<nb, kScanBlock, 0, st>>>(a);
     else
