@@ -44,6 +44,7 @@ namespace {
 
 constexpr int kThreads = 512;
 constexpr int kWaitIters = 1 << 22;
+constexpr int kFaceSumBytes = kThreads * 16; // face-plane partial sums: a float4 per thread
 
 // x = hi + mid + lo in bf16 for two values at once (round to nearest each)
 __device__ __forceinline__ void split2(float a, float b, uint32_t &h, uint32_t &m, uint32_t &l)
@@ -336,6 +337,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     // face-plane weights (the output linear's only row)
     float4 *w0s = reinterpret_cast<float4 *>(keys + (size_t)(tc.ncols_max / 4) * net.W);
     float *wls = reinterpret_cast<float *>(w0s + net.nodes[1]);
+    float *fsum = reinterpret_cast<float *>(reinterpret_cast<uintptr_t>(wls + net.nodes[net.n_lin - 1] + 3) & ~(uintptr_t)15);
 
     WPipe pp{bars, bars + 2, ws, tc.nstage, 0, 0, err, 1};
     if (tid == 0) {
@@ -385,10 +387,11 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                 st4<float>(cons + (size_t)rr * rstride + (size_t)(net.N + e) * 4,
                            make_float4(we[3 * e], we[3 * e + 1], we[3 * e + 2], be[e]));
             }
-            // X_1 = diag(s_1) [W0 | b0]
+            // X_1 = diag(s_1) [W0 | b0]; regions fastest across the lanes:
+            // consecutive regions' columns share a 128-byte operand row
             const int Kp = (n1 + 63) / 64 * 64;
             for (int q = tid; q < R * Kp; q += kThreads) {
-                const int r = q / Kp, k = q % Kp;
+                const int r = q % R, k = q / R;
                 float x[4] = {0.f, 0.f, 0.f, 0.f};
                 if (r < nreg && k < n1 && key_bit(keys + (size_t)r * net.W, k)) {
                     const float4 w = w0s[k];
@@ -397,7 +400,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                     x[2] = w.z;
                     x[3] = w.w;
                 }
-                    X.put<2>(4 * r, k, x);
+                X.put<2>(4 * r, k, x);
             }
         }
         umma::fence_proxy_async();
@@ -434,7 +437,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             const float *bias = (const float *)net.bias[i];
             const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
             for (int q = tid; q < R * (Kn - M); q += kThreads) {
-                const int r = q / (Kn - M), k = M + q % (Kn - M);
+                const int r = q % R, k = M + q / R;
                 const float z[4] = {0.f, 0.f, 0.f, 0.f};
                 X.put<2>(4 * r, k, z);
             }
@@ -502,47 +505,54 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         }
 
         // face plane: w_eq = W_L . X_L (+ b_L, + connections into the output layer)
-        // in fp32, one warp per region, from the operand in shared memory
-        // (hi + mid + lo is exact)
+        // in fp32 from the operand in shared memory (hi + mid + lo is exact):
+        // lanes take regions (consecutive regions share operand rows), the
+        // warps split K, partial sums meet in shared memory
         {
             const int i = net.n_lin - 1;
             const int K = net.nodes[i];
             const float bl = ((const float *)net.bias[i])[0];
-            for (int r = warp; r < nreg; r += kThreads / 32) {
+            constexpr int kWarps = kThreads / 32;
+            for (int r0 = 0; r0 < R; r0 += 32) {
+                const int r = r0 + lane;
                 float acc[4] = {0.f, 0.f, 0.f, 0.f};
-                for (int k = lane; k < K; k += 32) {
-                    const float w = wls[k];
-                    float x[4];
-                    X.get4(4 * r, k, x);
-                    #pragma unroll
-                    for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, x[c], acc[c]);
-                }
-                #pragma unroll
-                for (int c = 0; c < 4; ++c)
-                    #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-                if (lane < 4) {
-                    const int c = lane;
-                    float a = c == 0 ? acc[0] : (c == 1 ? acc[1] : (c == 2 ? acc[2] : acc[3]));
-                    const uint32_t *key = keys + (size_t)r * net.W;
-                    const float *cr = cons + (size_t)r * rstride;
-                    for (int s = 0; s < net.nskip[i]; ++s) {
-                        const SkipDev &sk = net.skip[i][s];
-                        if (sk.kind == 0) {
-                            if (sk.from >= 1 && net.nodes[sk.from] == 1 && key_bit(key, net.hoff[sk.from]))
-                                a -= cr[(size_t)net.hoff[sk.from] * 4 + c];
-                        } else if (sk.from == 0) {
-                            if (c < 3) a += ((const float *)sk.tmt)[(size_t)c * sk.Mp];
-                        } else {
-                            const float *tt = (const float *)sk.tmt; // [dec][Mp]
-                            const int hs = net.hoff[sk.from];
-                            for (int k = 0; k < net.nodes[sk.from]; ++k)
-                                if (key_bit(key, hs + k)) a -= tt[(size_t)k * sk.Mp] * cr[(size_t)(hs + k) * 4 + c];
-                        }
+                if (r < R)
+                    for (int k = warp; k < K; k += kWarps) {
+                        const float w = wls[k];
+                        float x[4];
+                        X.get4(4 * r, k, x);
+#pragma unroll
+                        for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, x[c], acc[c]);
                     }
-                    if (c == 3) a += bl - iso;
-                    ((float *)ch.eq)[(size_t)(rl0 + r) * 4 + c] = a;
+                // partial sums: [warp][lane][4]
+                reinterpret_cast<float4 *>(fsum)[warp * 32 + lane] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+                __syncthreads();
+                if (tid < 128) {
+                    const int rr = tid >> 2, c = tid & 3, rg = r0 + rr;
+                    float a = 0.f;
+                    for (int w = 0; w < kWarps; ++w) a += fsum[(w * 32 + rr) * 4 + c];
+                    if (rg < nreg) {
+                        const uint32_t *key = keys + (size_t)rg * net.W;
+                        const float *cr = cons + (size_t)rg * rstride;
+                        for (int s = 0; s < net.nskip[i]; ++s) {
+                            const SkipDev &sk = net.skip[i][s];
+                            if (sk.kind == 0) {
+                                if (sk.from >= 1 && net.nodes[sk.from] == 1 && key_bit(key, net.hoff[sk.from]))
+                                    a -= cr[(size_t)net.hoff[sk.from] * 4 + c];
+                            } else if (sk.from == 0) {
+                                if (c < 3) a += ((const float *)sk.tmt)[(size_t)c * sk.Mp];
+                            } else {
+                                const float *tt = (const float *)sk.tmt; // [dec][Mp]
+                                const int hs = net.hoff[sk.from];
+                                for (int k = 0; k < net.nodes[sk.from]; ++k)
+                                    if (key_bit(key, hs + k)) a -= tt[(size_t)k * sk.Mp] * cr[(size_t)(hs + k) * 4 + c];
+                            }
+                        }
+                        if (c == 3) a += bl - iso;
+                        ((float *)ch.eq)[(size_t)(rl0 + rg) * 4 + c] = a;
+                    }
                 }
+                __syncthreads();
             }
         }
     } // tiles
@@ -593,7 +603,7 @@ size_t tc_smem_bytes(const TcNet &tc, int ncols, int W)
 {
     const size_t cols = tc.mn ? (size_t)(ncols + 63) / 64 * 64 : (size_t)ncols;
     return 1024 + 3 * cols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * W * 4 +
-           16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last;
+           16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last + 16 + (size_t)kFaceSumBytes;
 }
 
 void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg, const ChunkDev &ch, double iso,

@@ -571,7 +571,7 @@ void run_begin(am_engine *e, const RunArgs &a)
         for (int mn = 1; mn >= 0 && tc.ncols_max < 16; --mn)
             for (tc.nstage = 2; tc.nstage >= 1; --tc.nstage) {
                 const long long room = (long long)smem_cap - 1024 - (long long)tc.nstage * kWBlockBytes -
-                                       64ll * e->W * 4 - 16ll * tc.n1 - 4ll * tc.k_last;
+                                       64ll * e->W * 4 - 16ll * tc.n1 - 4ll * tc.k_last - 16 - 512 * 16;
                 long long c = std::max<long long>(0, room) / (6ll * tc.kp_max);
                 if (mn) c = c / 64 * 64;
                 int ncols = (int)std::min<long long>(c, 256);
