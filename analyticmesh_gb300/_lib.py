@@ -41,6 +41,7 @@ AM_OPT_CHUNK = 1
 AM_OPT_PHASE_TIMING = 2
 AM_OPT_WELD = 3
 AM_OPT_GRAPH = 4
+AM_OPT_MAX_REGIONS = 5
 
 
 class AmError(RuntimeError):

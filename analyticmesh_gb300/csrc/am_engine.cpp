@@ -201,6 +201,13 @@ struct am_engine {
     } run;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, pa = nullptr, pb = nullptr;
     bool lean = false; // batch member: region store and table start small and grow on demand
+    long long max_regions = 0; // AM_OPT_MAX_REGIONS (0: no limit)
+    bool limit_hit = false;    // the last run stopped at the region limit
+    bool over_limit(long long tail)
+    {
+        if (max_regions > 0 && tail > max_regions) limit_hit = true;
+        return limit_hit;
+    }
     void ensure_events()
     {
         for (cudaEvent_t *ev : {&ev0, &ev1, &pa, &pb})
@@ -692,6 +699,7 @@ bool run_graph_done(am_engine *e)
     r.launches += 5ll * h->waves;
     r.head = h->head;
     e->num_regions = r.tail;
+    if (e->over_limit(r.tail)) return false; // stop: the regions so far stay
     return r.head < r.tail;
 }
 
@@ -757,6 +765,7 @@ void run_host_loop(am_engine *e)
         tail = e->poll();
         e->num_regions = tail;
         chunks++;
+        if (e->over_limit(tail)) break;
     }
     run.head = head;
     run.tail = tail;
@@ -915,6 +924,11 @@ int am_set_option(am_engine *e, int option, int64_t value)
         e->use_graph = value != 0;
         return AM_OK;
     }
+    if (option == AM_OPT_MAX_REGIONS) {
+        if (value < 0) return AM_ERR_INVALID_ARGUMENT;
+        e->max_regions = value;
+        return AM_OK;
+    }
     return AM_ERR_INVALID_ARGUMENT;
 }
 
@@ -928,18 +942,22 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
     e->has_mesh = false;
     const RunArgs a{weights, biases, states, points, num_points, arc_tm, arc_tm_shapes, num_arc_tm,
                     w_extra, b_extra, iso, flip_insideout, stream};
+    e->limit_hit = false;
     return guarded(e, [&] {
         run_begin(e, a);
         if (e->use_graph && !e->phase_timing) {
             while (e->run.head < e->run.tail) {
                 run_graph_launch(e, kMaxWaves);
                 AM_CUDA(cudaStreamSynchronize(e->st));
-                run_graph_done(e);
+                if (!run_graph_done(e)) break;
             }
         } else {
             run_host_loop(e);
         }
         run_end(e);
+        if (e->limit_hit) // the results so far are kept (has_am) and reported as a stop
+            throw Failure{AM_ERR_CAPACITY,
+                          "region limit reached: stopped at " + std::to_string(e->run.tail) + " regions"};
     });
 }
 

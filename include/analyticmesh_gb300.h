@@ -148,10 +148,14 @@ typedef enum {
                                  its two edge planes and the region key without those bits, which is
                                  watertight by construction), 1 = quantised coordinates as the
                                  reference (int(v*1e6) fp32 / int(v*1e9) fp64, backend/inc/polymesh.h:192) */
-    AM_OPT_GRAPH = 4          /* 1 (default): the wave loop runs on the device as one CUDA graph with a
+    AM_OPT_GRAPH = 4,         /* 1 (default): the wave loop runs on the device as one CUDA graph with a
                                  conditional while node, no host round trip per wave; 0: host-driven loop.
                                  Phase timing always uses the host-driven loop.  Both give the same regions
                                  in the same order. */
+    AM_OPT_MAX_REGIONS = 5    /* a run that passes this many regions stops after the current wave and
+                                 returns AM_ERR_CAPACITY; the regions found so far are kept and can be
+                                 queried (am_get_stats, am_get_regions, am_region_rows).  0 (default):
+                                 no limit */
 } am_option;
 int am_set_option(am_engine *engine, int option, int64_t value);
 

@@ -231,3 +231,25 @@ def test_graph_loop_matches_host_loop(form, chunk):
     assert np.array_equal(r0.bits, r1.bits)
     assert np.array_equal(r0.nverts, r1.nverts)
     assert np.array_equal(r0.verts, r1.verts)
+
+
+def test_region_limit_stops_and_keeps_results():
+    """AM_OPT_MAX_REGIONS: the run stops after the wave that passes the limit,
+    returns AM_ERR_CAPACITY, and the regions found so far stay queryable."""
+    m = wl.geometric([64, 64], 21, perturb=0.01)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=4)
+    full = engine.march(net, st, pt, "float32")
+    total = full.stats()["num_regions"]
+    full.close()
+    for graph in (0, 1):
+        eng = engine.Engine("float32", net.nodes, net.arc_table, 0)
+        eng.set_option(_lib.AM_OPT_GRAPH, graph)
+        eng.set_option(_lib.AM_OPT_MAX_REGIONS, 2000)
+        with pytest.raises(_lib.AmError, match="region limit"):
+            eng.run_net(net, st, pt)
+        got = eng.stats()["num_regions"]
+        assert 2000 < got < total
+        rows, eq = eng.region_rows(0, 100)
+        assert np.isfinite(rows).all() and np.isfinite(eq).all()
+        eng.close()

@@ -86,3 +86,17 @@ def test_ply_roundtrip(tmp_path):
     write_ply(p, v, f, polymesh=False, float32=True)
     v3, f3 = read_ply(p)
     assert len(f3) == 3 and np.allclose(v3, v, atol=1e-6)
+
+
+def test_batch_and_option_argument_checks():
+    """Host-side validation that needs no device: am_run_batch with no
+    engines, am_set_option without an engine."""
+    L = _lib.lib()
+    wall = C.c_double(0.0)
+    assert L.am_run_batch(None, None, 1, C.byref(wall)) == 1          # AM_ERR_INVALID_ARGUMENT
+    handles = (C.c_void_p * 1)(None)
+    args = (_lib.AmRunArgs * 1)()
+    assert L.am_run_batch(handles, args, 0, C.byref(wall)) == 1      # count < 1
+    assert L.am_run_batch(handles, args, 1, C.byref(wall)) == 2      # AM_ERR_NOT_INITIALIZED
+    L.am_set_option.argtypes = [C.c_void_p, C.c_int, C.c_int64]
+    assert L.am_set_option(None, _lib.AM_OPT_MAX_REGIONS, 10) == 2
