@@ -42,6 +42,7 @@ AM_OPT_PHASE_TIMING = 2
 AM_OPT_WELD = 3
 AM_OPT_GRAPH = 4
 AM_OPT_MAX_REGIONS = 5
+AM_OPT_COMPOSE_TILE = 6
 
 
 class AmError(RuntimeError):

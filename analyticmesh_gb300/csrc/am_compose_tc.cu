@@ -561,6 +561,403 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     if (warp == 0) umma::tmem_dealloc(tslot, (uint32_t)tmem_cols);
 }
 
+// ---------------------------------------------------------------- streamed operand
+// Wide layers: three bf16 terms of a resident K x ncols operand leave room for
+// only a few regions per tile, and every tile streams all weight blocks again.
+// Here the operand is not resident.  The epilogue writes the constraint rows
+// only; the next layer's masked operand is rebuilt one 64-deep K block at a
+// time from those rows (just written, still in L2) into a two-stage ring by
+// sixteen builder warps while one issuing thread runs the products on the
+// other stage.  K blocks are the outer loop of the products, so one block of
+// the operand serves every M tile of the layer and the tile is as wide as
+// TMEM allows (two accumulators per M tile in 512 columns).  The operand
+// values, the order of the products into each accumulator and the epilogue
+// and face-plane arithmetic are those of compose_tc_kernel, so both kernels
+// give the same bits.
+constexpr int kSBuild = 512;            // builder threads (16 warps)
+constexpr int kSThreads = kSBuild + 32; // + the issuing warp
+constexpr int kSFaceSumBytes = kSBuild * 16;
+
+__device__ __forceinline__ int jobs_of(const NetDev &net, int i)
+{
+    int n = 1;
+    for (int s = 0; s < net.nskip[i]; ++s) n += tc_skip(net.skip[i][s]) ? 1 : 0;
+    return n;
+}
+
+// product job `job` of linear i: 0 = the linear itself on hidden layer i,
+// q >= 1 = its q-th tensor-core connection (a transform of an earlier layer)
+__device__ const TcMat &job_mat(const NetDev &net, const TcNet &tc, int i, int job, int &src)
+{
+    src = i;
+    if (job > 0) {
+        int q = 0;
+        for (int s = 0; s < net.nskip[i]; ++s)
+            if (tc_skip(net.skip[i][s]) && ++q == job) {
+                src = net.skip[i][s].from;
+                return tc.skip[i][s];
+            }
+    }
+    return tc.lin[i];
+}
+
+__device__ __forceinline__ void bar_builders() { asm volatile("bar.sync 1, %0;" ::"r"(kSBuild) : "memory"); }
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_addr(bar)) : "memory");
+}
+
+__device__ __forceinline__ void swait(uint64_t *bar, uint32_t parity, int *err)
+{
+    if (!umma::mbar_wait(bar, parity, kWaitIters)) {
+        atomicOr(err, kErrWalk);
+        umma::mbar_wait(bar, parity, kWaitIters);
+    }
+}
+
+// position in the product sequence: tile, layer, job, K block, M tile (innermost)
+struct SCur {
+    int t, i, job, kb, mt;
+    bool valid;
+};
+
+__device__ void scur_next(SCur &c, const NetDev &net, const TcNet &tc, int tiles)
+{
+    int src;
+    const TcMat &m = job_mat(net, tc, c.i, c.job, src);
+    if (++c.mt < m.Mp / 128) return;
+    c.mt = 0;
+    if (++c.kb < m.Kp / 64) return;
+    c.kb = 0;
+    if (++c.job < jobs_of(net, c.i)) return;
+    c.job = 0;
+    if (++c.i <= net.n_lin - 2) return;
+    c.i = 1;
+    if (++c.t < tiles) return;
+    c.valid = false;
+}
+
+// (one thread) weight blocks through the nstage ring, operand blocks through
+// the two-stage ring: six products per K step into the main (hi.hi) and the
+// correction accumulator of each M tile
+__device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, uint64_t *wfull, uint64_t *wdone,
+                               const XOp *XS, uint64_t *xfull, uint64_t *xdone, uint64_t *accdone, uint32_t tmem,
+                               int ncols, int tiles, int *err)
+{
+    const int nst = tc.nstage;
+    SCur cc{0, 1, 0, 0, 0, net.n_lin - 2 >= 1}; // next weight block to copy
+    SCur mc = cc;                                // next weight block to multiply
+    int issued = 0;
+    auto copy_next = [&]() {
+        const int s = issued % nst;
+        if (issued >= nst) swait(wdone + s, (uint32_t)((issued - nst) / nst) & 1u, err);
+        int src;
+        const TcMat &m = job_mat(net, tc, cc.i, cc.job, src);
+        umma::mbar_expect_tx(wfull + s, (uint32_t)kWBlockBytes);
+        umma::bulk_g2s(ws + (size_t)s * kWBlockBytes,
+                       m.blocks + (size_t)(cc.mt * (m.Kp / 64) + cc.kb) * kWBlockBytes, (uint32_t)kWBlockBytes,
+                       wfull + s);
+        ++issued;
+        scur_next(cc, net, tc, tiles);
+    };
+    while (cc.valid && issued < nst) copy_next();
+    int h = 0, xb = 0;
+    while (mc.valid) {
+        int src;
+        const TcMat &m = job_mat(net, tc, mc.i, mc.job, src);
+        const int mtiles = m.Mp / 128, kblocks = m.Kp / 64;
+        const int xs = xb & 1;
+        const XOp &X = XS[xs];
+        if (mc.mt == 0) swait(xfull + xs, (uint32_t)(xb >> 1) & 1u, err); // operand block built
+        while (cc.valid && issued <= h) copy_next();
+        const int s = h % nst;
+        swait(wfull + s, (uint32_t)(h / nst) & 1u, err);
+        umma::fence_after();
+        const uint32_t a0 = umma::smem_addr(ws + (size_t)s * kWBlockBytes);
+        const uint32_t d_main = tmem + (uint32_t)(mc.mt * ncols);
+        const uint32_t d_corr = tmem + (uint32_t)((mtiles + mc.mt) * ncols);
+        const uint32_t idesc = X.idesc();
+        const bool fresh = mc.job == 0 && mc.kb == 0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t o = (uint32_t)(j * 32);
+            umma::mma_bf16(d_main, umma::desc_sw128(a0 + o), X.desc(0, 0, j), idesc, (fresh && j == 0) ? 0u : 1u);
+            int q = 0;
+#pragma unroll
+            for (int t = 0; t < 3; ++t)
+#pragma unroll
+                for (int u = 0; u + t < 3; ++u) {
+                    if (t == 0 && u == 0) continue;
+                    umma::mma_bf16(d_corr, umma::desc_sw128(a0 + t * 16384u + o), X.desc(u, 0, j), idesc,
+                                   (fresh && j == 0 && q == 0) ? 0u : 1u);
+                    ++q;
+                }
+        }
+        umma::commit(umma::smem_addr(wdone + s));
+        if (mc.mt == mtiles - 1) {
+            umma::commit(umma::smem_addr(xdone + xs)); // the operand stage is free once these complete
+            ++xb;
+            if (mc.kb == kblocks - 1 && mc.job == jobs_of(net, mc.i) - 1)
+                umma::commit(umma::smem_addr(accdone)); // the layer's accumulators are complete
+        }
+        while (cc.valid && issued <= h + nst - 1) copy_next(); // refill the stage of block h - 1
+        ++h;
+        scur_next(mc, net, tc, tiles);
+    }
+    if (h > 0) swait(wdone + (h - 1) % nst, (uint32_t)((h - 1) / nst) & 1u, err);
+}
+
+__global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, TcNet tc, RegionsDev reg, ChunkDev ch,
+                                                                    float iso, int slots, int *err)
+{
+    extern __shared__ uint8_t smem_raw[];
+    // wfull[2], wdone[2] (weight ring), xfull[2], xdone[2] (operand ring), accdone
+    __shared__ uint64_t bars[9];
+    __shared__ uint32_t tslot;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    long long head;
+    int count;
+    chunk_range(ch, head, count);
+    if (count <= 0) return;
+    const int ncols = tile_cols(count, slots, tc.ncols_max);
+    const int R = ncols / 4;
+    const int ntiles = (count + R - 1) / R;
+    const int tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    if (tiles == 0) return;
+    int tmem_cols = 32;
+    while (tmem_cols < 2 * tc.mtiles_max * ncols) tmem_cols <<= 1;
+    const size_t rstride = (size_t)net.ALLP * 4;
+
+    uint8_t *base = smem_raw + ((1024u - (umma::smem_addr(smem_raw) & 1023u)) & 1023u);
+    XOp XS[2];
+    const int natoms = (ncols + 63) / 64;
+    const size_t plane = (size_t)(tc.mn ? natoms * 64 : ncols) * 64 * 2; // one term of one K block
+    for (int x = 0; x < 2; ++x) {
+        XS[x].mn = tc.mn != 0;
+        XS[x].ncols = ncols;
+        XS[x].natoms = natoms;
+        XS[x].xbytes = plane;
+        XS[x].xs = base + (size_t)x * 3 * plane; // hi, mid, lo
+    }
+    uint8_t *ws = base + 6 * plane;
+    uint32_t *keys = reinterpret_cast<uint32_t *>(ws + (size_t)tc.nstage * kWBlockBytes);
+    float4 *w0s = reinterpret_cast<float4 *>(keys + (size_t)(tc.ncols_max / 4) * net.W);
+    float *wls = reinterpret_cast<float *>(w0s + net.nodes[1]);
+    float *fsum = reinterpret_cast<float *>(reinterpret_cast<uintptr_t>(wls + net.nodes[net.n_lin - 1] + 3) & ~(uintptr_t)15);
+    uint64_t *wfull = bars, *wdone = bars + 2, *xfull = bars + 4, *xdone = bars + 6, *accdone = bars + 8;
+
+    if (tid == 0) {
+        for (int b = 0; b < 4; ++b) umma::mbar_init(bars + b, 1);
+        umma::mbar_init(xfull, kSBuild);
+        umma::mbar_init(xfull + 1, kSBuild);
+        umma::mbar_init(xdone, 1);
+        umma::mbar_init(xdone + 1, 1);
+        umma::mbar_init(accdone, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tmem_cols);
+    {
+        const float *W0 = (const float *)net.W0;
+        const float *b0 = (const float *)net.bias[0];
+        for (int m = tid; m < net.nodes[1]; m += kSThreads)
+            w0s[m] = make_float4(W0[3 * m], W0[3 * m + 1], W0[3 * m + 2], b0[m]);
+        const int il = net.n_lin - 1;
+        const float *wl = (const float *)net.Wt[il]; // [K][Mp], column 0
+        for (int k = tid; k < net.nodes[il]; k += kSThreads) wls[k] = wl[(size_t)k * net.Mp[il]];
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = tslot;
+
+    if (warp == kSBuild / 32) {
+        if (lane == 0) issue_streamed(net, tc, ws, wfull, wdone, XS, xfull, xdone, accdone, tmem, ncols, tiles, err);
+        __syncwarp(); // the warp reaches the block barrier below converged
+    } else {
+        // epilogue: warp w reads TMEM lanes 32 (w % 4).. and every fourth column block
+        const int q4 = warp & 3, cgrp = warp >> 2, ngrp = kSBuild / 128;
+        int xb = 0, accph = 0;
+        for (int j = 0; j < tiles; ++j) {
+            const long long rl0 = (long long)(blockIdx.x + (long long)j * gridDim.x) * R;
+            const int nreg = (int)min((long long)R, (long long)count - rl0);
+            float *cons = (float *)ch.cons + (size_t)rl0 * rstride;
+            const uint32_t *gkeys = reg.keys + (size_t)(head + rl0) * net.W;
+            bar_builders(); // the previous tile is done with the keys
+            for (int q = tid; q < R * net.W; q += kSBuild) keys[q] = q < nreg * net.W ? gkeys[q] : 0u;
+            bar_builders();
+            // hidden layer 1 = linear 0 rows (sign-flipped) and the extra constraints
+            const int n1 = net.nodes[1];
+            for (int q = tid; q < nreg * n1; q += kSBuild) {
+                const int rr = q / n1, m = q % n1;
+                const float sg = key_bit(keys + (size_t)rr * net.W, m) ? -1.f : 1.f;
+                const float4 w = w0s[m];
+                st4<float>(cons + (size_t)rr * rstride + (size_t)m * 4, make_float4(sg * w.x, sg * w.y, sg * w.z, sg * w.w));
+            }
+            const float *we = (const float *)net.w_extra;
+            const float *be = (const float *)net.b_extra;
+            for (int q = tid; q < nreg * net.E; q += kSBuild) {
+                const int rr = q / net.E, e = q % net.E;
+                st4<float>(cons + (size_t)rr * rstride + (size_t)(net.N + e) * 4,
+                           make_float4(we[3 * e], we[3 * e + 1], we[3 * e + 2], be[e]));
+            }
+            bar_builders(); // layer-1 rows written by every builder
+
+            for (int i = 1; i <= net.n_lin - 2; ++i) {
+                const int M = net.nodes[i + 1];
+                const int mtiles = (M + 127) / 128;
+                const int njobs = jobs_of(net, i);
+                for (int job = 0; job < njobs; ++job) {
+                    int src;
+                    const TcMat &mat = job_mat(net, tc, i, job, src);
+                    const int K = net.nodes[src], rows0 = net.hoff[src];
+                    for (int kb = 0; kb < mat.Kp / 64; ++kb) {
+                        const int xs = xb & 1, fill = xb >> 1;
+                        if (fill >= 1) swait(xdone + xs, (uint32_t)((fill - 1) & 1), err); // stage free
+                        const XOp &X = XS[xs];
+                        // X[4r + c][k] = s_k(r) ? -C[r][k][c] : 0 for the block's 64 rows k,
+                        // regions fastest across the lanes; two loads in flight per thread
+                        for (int q0 = tid; q0 < R * 64; q0 += 2 * kSBuild) {
+                            float x[2][4];
+#pragma unroll
+                            for (int u = 0; u < 2; ++u) {
+                                const int q = q0 + u * kSBuild;
+                                const int r = q % R, kk = q / R, k = kb * 64 + kk;
+                                x[u][0] = x[u][1] = x[u][2] = x[u][3] = 0.f;
+                                if (q < R * 64 && r < nreg && k < K && key_bit(keys + (size_t)r * net.W, rows0 + k)) {
+                                    if (src == 1) {
+                                        const float4 w = w0s[k];
+                                        x[u][0] = w.x, x[u][1] = w.y, x[u][2] = w.z, x[u][3] = w.w;
+                                    } else {
+                                        const float4 c = ld4<float>(cons + (size_t)r * rstride + (size_t)(rows0 + k) * 4);
+                                        x[u][0] = -c.x, x[u][1] = -c.y, x[u][2] = -c.z, x[u][3] = -c.w;
+                                    }
+                                }
+                            }
+#pragma unroll
+                            for (int u = 0; u < 2; ++u) {
+                                const int q = q0 + u * kSBuild;
+                                if (q < R * 64) X.put<2>(4 * (q % R), q / R, x[u]);
+                            }
+                        }
+                        umma::fence_proxy_async(); // generic-proxy stores -> the tensor cores
+                        mbar_arrive(xfull + xs);
+                        ++xb;
+                    }
+                }
+                swait(accdone, (uint32_t)(accph & 1), err); // the layer's products are in TMEM
+                ++accph;
+                umma::fence_after();
+                // epilogue: accumulators -> constraint rows of hidden layer i + 1
+                const float *bias = (const float *)net.bias[i];
+                for (int mt = 0; mt < mtiles; ++mt) {
+                    const int m = mt * 128 + q4 * 32 + lane;
+                    const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
+                    const float bm = m < M ? bias[m] : 0.f;
+                    const int row = net.hoff[i + 1] + m;
+                    for (int cb = cgrp; cb < ncols / 16; cb += ngrp) {
+                        float v[16], vc[16];
+                        umma::tmem_ld16x2(lane_base + (uint32_t)(mt * ncols + cb * 16),
+                                          lane_base + (uint32_t)((mtiles + mt) * ncols + cb * 16), v, vc);
+                        if (m >= M) continue;
+#pragma unroll
+                        for (int qq = 0; qq < 4; ++qq) {
+                            const int r = cb * 4 + qq;
+                            if (r >= nreg) continue;
+                            const uint32_t *key = keys + (size_t)r * net.W;
+                            float *cr = cons + (size_t)r * rstride;
+                            float o[4] = {v[4 * qq] + vc[4 * qq], v[4 * qq + 1] + vc[4 * qq + 1],
+                                          v[4 * qq + 2] + vc[4 * qq + 2], v[4 * qq + 3] + vc[4 * qq + 3] + bm};
+                            for (int s = 0; s < net.nskip[i]; ++s) {
+                                const SkipDev &sk = net.skip[i][s];
+                                if (sk.kind == 0) {
+                                    if (sk.from == 0) {
+                                        if (m < 3) o[m] += 1.f;
+                                    } else {
+                                        const int srow = net.hoff[sk.from] + m;
+                                        if (key_bit(key, srow)) {
+                                            const float4 c = ld4<float>(cr + (size_t)srow * 4);
+                                            o[0] -= c.x;
+                                            o[1] -= c.y;
+                                            o[2] -= c.z;
+                                            o[3] -= c.w;
+                                        }
+                                    }
+                                } else if (sk.from == 0) {
+                                    const float *tt = (const float *)sk.tmt;
+                                    o[0] += tt[m];
+                                    o[1] += tt[(size_t)sk.Mp + m];
+                                    o[2] += tt[2 * (size_t)sk.Mp + m];
+                                }
+                            }
+                            const float sg = key_bit(key, row) ? -1.f : 1.f;
+                            st4<float>(cr + (size_t)row * 4, make_float4(sg * o[0], sg * o[1], sg * o[2], sg * o[3]));
+                        }
+                    }
+                }
+                umma::fence_before(); // TMEM read out before the next products overwrite it
+                bar_builders();       // rows of hidden layer i + 1 written by every builder
+            }
+
+            // face plane: w_eq = W_L . X_L, X_L = -C of the last hidden layer
+            // where active; lanes take regions, the warps split K, partial
+            // sums meet in shared memory (the order of compose_tc_kernel)
+            {
+                const int i = net.n_lin - 1;
+                const int K = net.nodes[i], rows0 = net.hoff[i];
+                const float bl = ((const float *)net.bias[i])[0];
+                constexpr int kWarps = kSBuild / 32;
+                for (int r0 = 0; r0 < R; r0 += 32) {
+                    const int r = r0 + lane;
+                    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+                    if (r < nreg)
+                        for (int k = warp; k < K; k += kWarps) {
+                            const float w = wls[k];
+                            float x[4] = {0.f, 0.f, 0.f, 0.f};
+                            if (key_bit(keys + (size_t)r * net.W, rows0 + k)) {
+                                const float4 c = ld4<float>(cons + (size_t)r * rstride + (size_t)(rows0 + k) * 4);
+                                x[0] = -c.x, x[1] = -c.y, x[2] = -c.z, x[3] = -c.w;
+                            }
+#pragma unroll
+                            for (int c = 0; c < 4; ++c) acc[c] = fmaf(w, x[c], acc[c]);
+                        }
+                    reinterpret_cast<float4 *>(fsum)[warp * 32 + lane] = make_float4(acc[0], acc[1], acc[2], acc[3]);
+                    bar_builders();
+                    if (tid < 128) {
+                        const int rr = tid >> 2, c = tid & 3, rg = r0 + rr;
+                        float a = 0.f;
+                        for (int w = 0; w < kWarps; ++w) a += fsum[(w * 32 + rr) * 4 + c];
+                        if (rg < nreg) {
+                            const uint32_t *key = keys + (size_t)rg * net.W;
+                            const float *cr = cons + (size_t)rg * rstride;
+                            for (int s = 0; s < net.nskip[i]; ++s) {
+                                const SkipDev &sk = net.skip[i][s];
+                                if (sk.kind == 0) {
+                                    if (sk.from >= 1 && net.nodes[sk.from] == 1 && key_bit(key, net.hoff[sk.from]))
+                                        a -= cr[(size_t)net.hoff[sk.from] * 4 + c];
+                                } else if (sk.from == 0) {
+                                    if (c < 3) a += ((const float *)sk.tmt)[(size_t)c * sk.Mp];
+                                } else {
+                                    const float *tt = (const float *)sk.tmt; // [dec][Mp]
+                                    const int hs = net.hoff[sk.from];
+                                    for (int k = 0; k < net.nodes[sk.from]; ++k)
+                                        if (key_bit(key, hs + k)) a -= tt[(size_t)k * sk.Mp] * cr[(size_t)(hs + k) * 4 + c];
+                                }
+                            }
+                            if (c == 3) a += bl - iso;
+                            ((float *)ch.eq)[(size_t)(rl0 + rg) * 4 + c] = a;
+                        }
+                    }
+                    bar_builders();
+                }
+            }
+        }
+    }
+    umma::fence_before();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tslot, (uint32_t)tmem_cols);
+}
+
 // src (M x K fp32, row-major) -> three bf16 terms as the shared-memory image
 // of 128 x 64 blocks (K-major, 128-byte swizzle), zero padding to Mp x Kp
 __global__ void pack_weights_kernel(const float *src, int M, int K, int Mp, int Kp, uint8_t *dst)
@@ -601,6 +998,11 @@ int device_sms()
 
 size_t tc_smem_bytes(const TcNet &tc, int ncols, int W)
 {
+    if (tc.streamed) { // two operand stages of one K block each
+        const size_t cols = tc.mn ? (size_t)(ncols + 63) / 64 * 64 : (size_t)ncols;
+        return 1024 + 6 * cols * 64 * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * W * 4 +
+               16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last + 16 + (size_t)kSFaceSumBytes;
+    }
     const size_t cols = tc.mn ? (size_t)(ncols + 63) / 64 * 64 : (size_t)ncols;
     return 1024 + 3 * cols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * W * 4 +
            16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last + 16 + (size_t)kFaceSumBytes;
@@ -612,8 +1014,20 @@ void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg
     if (!ch.ctl && ch.count <= 0) return;
     const int sms = device_sms();
     const size_t smem_max = tc_smem_bytes(tc, tc.ncols_max, net.W);
-    cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     const int slots = sms; // one resident tile per SM
+    if (tc.streamed) {
+        cudaFuncSetAttribute(compose_tcs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
+        if (ch.ctl) {
+            compose_tcs_kernel<<<slots, kSThreads, smem_max, st>>>(net, tc, reg, ch, (float)iso, slots, d_err);
+            return;
+        }
+        const int ncols = tile_cols(ch.count, slots, tc.ncols_max);
+        const int R = ncols / 4;
+        compose_tcs_kernel<<<(ch.count + R - 1) / R, kSThreads, tc_smem_bytes(tc, ncols, net.W), st>>>(
+            net, tc, reg, ch, (float)iso, slots, d_err);
+        return;
+    }
+    cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (ch.ctl) { // wave size known on the device only: every resident tile slot, tiles strided
         compose_tc_kernel<<<slots, kThreads, smem_max, st>>>(net, tc, reg, ch, (float)iso, slots, d_err);
         return;

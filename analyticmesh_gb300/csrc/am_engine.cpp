@@ -11,6 +11,7 @@
 #include <cstddef>
 #include <cmath>
 #include <cstdio>
+#include <climits>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -202,6 +203,7 @@ struct am_engine {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, pa = nullptr, pb = nullptr;
     bool lean = false; // batch member: region store and table start small and grow on demand
     long long max_regions = 0; // AM_OPT_MAX_REGIONS (0: no limit)
+    int compose_tile = 0;      // AM_OPT_COMPOSE_TILE: 0 automatic, 1 resident operand, 2 streamed operand
     bool limit_hit = false;    // the last run stopped at the region limit
     bool over_limit(long long tail)
     {
@@ -587,6 +589,26 @@ void run_begin(am_engine *e, const RunArgs &a)
                 tc.mn = mn;
                 if (ncols >= 16) break;
             }
+        // streamed operand (wide layers): two 64-deep operand blocks, so the
+        // tile is as wide as TMEM allows; taken when that is wider
+        TcNet ts = tc;
+        ts.streamed = 1;
+        ts.ncols_max = 0;
+        for (int mn = 1; mn >= 0 && ts.ncols_max < 16; --mn)
+            for (ts.nstage = 2; ts.nstage >= 1; --ts.nstage) {
+                ts.mn = mn;
+                int ncols = std::min(256, 256 / ts.mtiles_max) / 16 * 16;
+                for (; ncols >= 16; ncols -= 16) {
+                    ts.ncols_max = ncols;
+                    if (tc_smem_bytes(ts, ncols, e->W) <= smem_cap) break;
+                }
+                ts.ncols_max = std::max(ncols, 0);
+                if (ts.ncols_max >= 16) break;
+            }
+        const bool want_streamed = e->compose_tile == 2 ||
+                                   (e->compose_tile == 0 && tc.kp_max >= 256 && ts.ncols_max > tc.ncols_max);
+        if (ts.ncols_max >= 16 && (want_streamed || tc.ncols_max < 16)) tc = ts;
+        AM_CHECK(e->compose_tile != 1 || !tc.streamed, "resident operand tile does not fit");
         AM_CHECK(tc.nstage >= 1 && tc.ncols_max >= 16, "layer widths too large for the tensor-core composition tile");
         AM_CHECK(tc_smem_bytes(tc, tc.ncols_max, e->W) <= smem_cap,
                  "tensor-core composition tile exceeds shared memory");
@@ -679,6 +701,7 @@ void run_graph_launch(am_engine *e, int max_waves)
     h->chunk_cap = r.chunk;
     h->work = 0u;
     h->max_waves = max_waves;
+    h->stop_tail = e->max_regions > 0 ? e->max_regions : LLONG_MAX;
     // tail and err stay as the device has them
     AM_CUDA(cudaMemcpyAsync((char *)e->d_tail.p + offsetof(WaveCtl, head), (char *)h + offsetof(WaveCtl, head),
                             sizeof(WaveCtl) - offsetof(WaveCtl, head), cudaMemcpyHostToDevice, st));
@@ -927,6 +950,11 @@ int am_set_option(am_engine *e, int option, int64_t value)
     if (option == AM_OPT_MAX_REGIONS) {
         if (value < 0) return AM_ERR_INVALID_ARGUMENT;
         e->max_regions = value;
+        return AM_OK;
+    }
+    if (option == AM_OPT_COMPOSE_TILE) {
+        if (value < 0 || value > 2) return AM_ERR_INVALID_ARGUMENT;
+        e->compose_tile = (int)value;
         return AM_OK;
     }
     return AM_ERR_INVALID_ARGUMENT;

@@ -267,7 +267,8 @@ __global__ void wave_step_kernel(WaveCtl *ctl, cudaGraphConditionalHandle cond)
     c.count = (int)(rem < (long long)c.chunk_cap ? (rem > 0 ? rem : 0) : (long long)c.chunk_cap);
     c.work = 0u;
     const bool go = c.count > 0 && (c.err & (kErrTableFull | kErrCapacity)) == 0 &&
-                    c.tail + (long long)c.count * kVMax <= c.limit && c.waves < c.max_waves;
+                    c.tail + (long long)c.count * kVMax <= c.limit && c.waves < c.max_waves &&
+                    c.tail <= c.stop_tail;
     cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 

@@ -81,6 +81,7 @@ struct WaveCtl {
     unsigned int work;  // next region of the wave for the polygon warps
     int max_waves;      // waves one graph launch may run
     int pad1;
+    long long stop_tail; // stop after the wave that takes tail past this (a region limit)
 };
 
 struct ChunkDev {

@@ -30,6 +30,7 @@ struct TcNet {
     int nstage;                         // weight blocks in flight (1 or 2)
     int mn;                             // operand layout: 1 MN-major (64-column atoms), 0 K-major
     int n1, k_last;                     // widths of hidden layer 1 and of the last hidden layer
+    int streamed;                       // operand rebuilt per 64-wide K block from the rows (wide layers)
 };
 
 size_t tc_smem_bytes(const TcNet &tc, int ncols, int W);

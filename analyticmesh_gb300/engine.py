@@ -230,12 +230,16 @@ def run_batch(engines, nets, states_list, points_list, iso=0.0, flip_insideout=F
     return wall.value
 
 
-def march(net, states, points, float_type="float32", iso=0.0, flip_insideout=False, chunk=None, phase_timing=False):
-    """One-shot: Init + AnalyticMarching on a ``workloads.NetArrays``; returns the engine."""
+def march(net, states, points, float_type="float32", iso=0.0, flip_insideout=False, chunk=None, phase_timing=False,
+          options=None):
+    """One-shot: Init + AnalyticMarching on a ``workloads.NetArrays``; returns
+    the engine.  ``options``: further {AM_OPT_*: value} set before the run."""
     eng = Engine(float_type, net.nodes, net.arc_table, net.num_extra)
     if chunk:
         eng.set_option(_lib.AM_OPT_CHUNK, chunk)
     if phase_timing:
         eng.set_option(_lib.AM_OPT_PHASE_TIMING, 1)
+    for opt, value in (options or {}).items():
+        eng.set_option(opt, value)
     eng.run_net(net, states, points, iso, flip_insideout)
     return eng

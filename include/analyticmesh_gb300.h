@@ -152,10 +152,14 @@ typedef enum {
                                  conditional while node, no host round trip per wave; 0: host-driven loop.
                                  Phase timing always uses the host-driven loop.  Both give the same regions
                                  in the same order. */
-    AM_OPT_MAX_REGIONS = 5    /* a run that passes this many regions stops after the current wave and
+    AM_OPT_MAX_REGIONS = 5,   /* a run that passes this many regions stops after the current wave and
                                  returns AM_ERR_CAPACITY; the regions found so far are kept and can be
                                  queried (am_get_stats, am_get_regions, am_region_rows).  0 (default):
                                  no limit */
+    AM_OPT_COMPOSE_TILE = 6   /* "mixed" composition on the tensor cores: 0 (default) automatic, 1 the
+                                 operand of a tile stays in shared memory for all layers, 2 it is rebuilt
+                                 per 64-deep block from the rows just written (wider tiles for layers of
+                                 256 units and more).  Both give the same bits. */
 } am_option;
 int am_set_option(am_engine *engine, int option, int64_t value);
 

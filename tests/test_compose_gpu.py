@@ -5,7 +5,7 @@ backend/inc/process.h:18-193, with connections into the output layer)."""
 import numpy as np
 import pytest
 
-from analyticmesh_gb300 import engine, workloads as wl
+from analyticmesh_gb300 import _lib, engine, workloads as wl
 
 pytestmark = pytest.mark.gpu
 
@@ -87,3 +87,40 @@ def test_tensor_core_rows_match_fp32_accuracy(factory):
     # fp32-level rows and face planes from the tensor cores
     assert errs["mixed"][0] <= max(4 * errs["float32"][0], 2e-6), errs
     assert errs["mixed"][1] <= max(4 * errs["float32"][1], 2e-6), errs
+
+
+@pytest.mark.parametrize("factory", [
+    lambda: wl.geometric([256, 256, 256], 14, perturb=0.02),
+    lambda: wl.geometric([512] * 3, 16, perturb=0.01),
+    lambda: wl.geometric([20, 50, 20, 80, 20], 13, skips=[[0], [1, 1, 0], [1, 1, 1], [0], [0]], tm_shapes=[[0, 0], [80, 20]]),
+    lambda: wl.geometric([64] * 5, 15, perturb=0.01, skips=[[0], [0], [1, 0, 0], [0], [0]], tm_shapes=[[64, 3]]),
+], ids=["wide256", "wide512", "odd_widths_tc_skip", "input_skip"])
+def test_streamed_and_resident_operand_tiles_agree(factory):
+    """The tensor-core composition with the operand resident in shared memory
+    for all layers and with the operand rebuilt per 64-deep block from the
+    rows just written: same rows, same face planes, same regions, bit for bit."""
+    m = factory()
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=7)
+    out = {}
+    for tile in (1, 2):
+        try:
+            eng = engine.march(net, st, pt, "mixed", options={_lib.AM_OPT_COMPOSE_TILE: tile})
+        except RuntimeError as e:  # the resident tile of a 512-wide net may not fit
+            assert tile == 1 and "does not fit" in str(e), e
+            continue
+        s = eng.stats()
+        n = min(s["num_regions"], 4000)
+        rows, eq = eng.region_rows(0, n)
+        out[tile] = (s["num_regions"], s["num_faces"], eng.regions().bits[:n], rows, eq)
+        eng.close()
+    assert 2 in out
+    if 1 in out:
+        a, b = out[1], out[2]
+        assert a[0] == b[0] and a[1] == b[1]
+        assert np.array_equal(a[2], b[2])
+        assert np.array_equal(a[3].view(np.int64), b[3].view(np.int64))
+        assert np.array_equal(a[4].view(np.int64), b[4].view(np.int64))
+    ref_rows, ref_eq = compose_fp64(net, out[2][2])
+    assert rel_err(out[2][3], ref_rows) <= 1e-5
+    assert rel_err(out[2][4], ref_eq) <= 1e-5

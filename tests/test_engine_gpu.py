@@ -238,18 +238,22 @@ def test_region_limit_stops_and_keeps_results():
     returns AM_ERR_CAPACITY, and the regions found so far stay queryable."""
     m = wl.geometric([64, 64], 21, perturb=0.01)
     net = wl.net_arrays(m)
+    # four seeds: the search spreads over many waves
     st, pt = wl.seeds_for(m, init_num=128, seed=4)
+    st, pt = st[:4], pt[:4]
     full = engine.march(net, st, pt, "float32")
-    total = full.stats()["num_regions"]
+    total, seeds = full.stats()["num_regions"], full.stats()["num_seeds"]
     full.close()
+    limit = 200
+    assert seeds <= 4 and limit < total // 4
     for graph in (0, 1):
         eng = engine.Engine("float32", net.nodes, net.arc_table, 0)
         eng.set_option(_lib.AM_OPT_GRAPH, graph)
-        eng.set_option(_lib.AM_OPT_MAX_REGIONS, 2000)
+        eng.set_option(_lib.AM_OPT_MAX_REGIONS, limit)
         with pytest.raises(_lib.AmError, match="region limit"):
             eng.run_net(net, st, pt)
         got = eng.stats()["num_regions"]
-        assert 2000 < got < total
+        assert limit < got < total
         rows, eq = eng.region_rows(0, 100)
         assert np.isfinite(rows).all() and np.isfinite(eq).all()
         eng.close()
