@@ -43,6 +43,7 @@ AM_OPT_WELD = 3
 AM_OPT_GRAPH = 4
 AM_OPT_MAX_REGIONS = 5
 AM_OPT_COMPOSE_TILE = 6
+AM_OPT_FACE_WARPS = 7
 
 
 class AmError(RuntimeError):
@@ -75,6 +76,7 @@ def lib():
     L.am_region_rows.argtypes = [vp, C.c_int64, C.c_int, vp, vp]
     L.am_run_batch.argtypes = [vp, C.POINTER(AmRunArgs), C.c_int, C.POINTER(C.c_double)]
     L.am_compose_rows_noalloc.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, C.c_double, vp, vp, vp]
+    L.am_autotune.argtypes = [vp, C.POINTER(AmRunArgs), C.c_int64, C.POINTER(C.c_int32)]
     _LIB = L
     return L
 

@@ -13,7 +13,9 @@
 #include <cstdio>
 #include <climits>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -204,6 +206,7 @@ struct am_engine {
     bool lean = false; // batch member: region store and table start small and grow on demand
     long long max_regions = 0; // AM_OPT_MAX_REGIONS (0: no limit)
     int compose_tile = 0;      // AM_OPT_COMPOSE_TILE: 0 automatic, 1 resident operand, 2 streamed operand
+    int face_warps = 0;        // AM_OPT_FACE_WARPS: warps per face polygon, 0 automatic
     bool limit_hit = false;    // the last run stopped at the region limit
     bool over_limit(long long tail)
     {
@@ -345,6 +348,7 @@ struct am_engine {
         const void *bufs[6] = {cons.p, eq.p, rec.p, blocksum.p, d_tail.p, (const void *)blocksum.bytes};
         add(&prec, sizeof(prec));
         add(&chunk, sizeof(chunk));
+        add(&face_warps, sizeof(face_warps));
         add(&iso, sizeof(iso));
         add(&tol, sizeof(tol));
         add(&net, sizeof(net));
@@ -378,7 +382,7 @@ struct am_engine {
                     launch_compose_tc(net, tcnet, reg, ch, iso, d_err.as<int>(), st);
                 else
                     launch_compose(prec, net, reg, ch, iso, st);
-                launch_polygon(prec, net, reg, ch, hs, tol, d_err.as<int>(), st);
+                launch_polygon(prec, net, reg, ch, hs, tol, face_warps, d_err.as<int>(), st);
                 launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, chunk * kVMax,
                               d_tail.as<long long>(), blocksum.as<int>(), (int)(blocksum.bytes / sizeof(int)),
                               d_err.as<int>(), st);
@@ -766,7 +770,7 @@ void run_host_loop(am_engine *e)
             t_comp += ms;
             AM_CUDA(cudaEventRecord(pa, st));
         }
-        launch_polygon(prec, net, reg, ch, hs, tol, e->d_err.as<int>(), st);
+        launch_polygon(prec, net, reg, ch, hs, tol, e->face_warps, e->d_err.as<int>(), st);
         if (e->phase_timing) {
             AM_CUDA(cudaEventRecord(pb, st));
             AM_CUDA(cudaEventSynchronize(pb));
@@ -952,6 +956,11 @@ int am_set_option(am_engine *e, int option, int64_t value)
         e->max_regions = value;
         return AM_OK;
     }
+    if (option == AM_OPT_FACE_WARPS) {
+        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8) return AM_ERR_INVALID_ARGUMENT;
+        e->face_warps = (int)value;
+        return AM_OK;
+    }
     if (option == AM_OPT_COMPOSE_TILE) {
         if (value < 0 || value > 2) return AM_ERR_INVALID_ARGUMENT;
         e->compose_tile = (int)value;
@@ -987,6 +996,98 @@ int am_analytic_marching(am_engine *e, const void *const *weights, const void *c
             throw Failure{AM_ERR_CAPACITY,
                           "region limit reached: stopped at " + std::to_string(e->run.tail) + " regions"};
     });
+}
+
+// Autotuner: the composition tile (resident or streamed operand, mixed form)
+// and the warps per face polygon, chosen for a network architecture by
+// marching a sample of it (the first sample_regions regions, the region limit
+// of AM_OPT_MAX_REGIONS) once per candidate with per-phase device timing,
+// after one untimed pass over the candidates (first launches load modules).
+// Every candidate produces the same regions (the options change the work
+// split, not the result), so the samples time the same waves.  The choice
+// is kept per architecture for the process.
+namespace {
+std::mutex g_tune_mu;
+std::map<std::vector<int64_t>, std::pair<int, int>> g_tune;
+} // namespace
+
+int am_autotune(am_engine *e, const am_run_args *x, int64_t sample_regions, int32_t *chosen)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (!x || sample_regions < 1) return AM_ERR_INVALID_ARGUMENT;
+    std::vector<int64_t> key = {e->prec, e->E, sample_regions};
+    key.insert(key.end(), e->nodes.begin(), e->nodes.end());
+    key.insert(key.end(), e->arc.begin(), e->arc.end());
+    for (int t = 0; t < x->num_arc_tm && x->arc_tm_shapes; ++t) {
+        key.push_back(x->arc_tm_shapes[2 * t]);
+        key.push_back(x->arc_tm_shapes[2 * t + 1]);
+    }
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            e->compose_tile = it->second.first;
+            e->face_warps = it->second.second;
+            if (chosen) chosen[0] = e->compose_tile, chosen[1] = e->face_warps;
+            return AM_OK;
+        }
+    }
+    const RunArgs a{x->weights, x->biases, x->states, x->points, x->num_points, x->arc_tm, x->arc_tm_shapes,
+                    x->num_arc_tm, x->w_extra, x->b_extra, x->iso, x->flip_insideout, nullptr};
+    const long long keep_max = e->max_regions;
+    const bool keep_pt = e->phase_timing;
+    const int keep_ct = e->compose_tile, keep_fw = e->face_warps;
+    int last_rc = AM_OK;
+    auto sample = [&](int ct, int fw, double &comp, double &poly) {
+        e->compose_tile = ct;
+        e->face_warps = fw;
+        e->max_regions = sample_regions;
+        e->phase_timing = true;
+        e->has_am = false;
+        e->has_mesh = false;
+        e->limit_hit = false;
+        const int rc = guarded(e, [&] {
+            run_begin(e, a);
+            run_host_loop(e);
+            run_end(e);
+        });
+        if (rc != AM_OK) last_rc = rc;
+        comp = e->stats.compose_ms;
+        poly = e->stats.polygon_ms;
+        return rc == AM_OK;
+    };
+    std::vector<int> cts = {0};
+    if (e->prec == kMixed) cts = {1, 2};
+    const int fws[] = {1, 2, 4, 8};
+    double c = 0, p = 0;
+    for (int ct : cts) sample(ct, 0, c, p); // untimed pass
+    for (int fw : fws) sample(0, fw, c, p);
+    int best_ct = -1, best_fw = -1;
+    double best = 1e300;
+    for (int ct : cts)
+        if (sample(ct, 0, c, p) && c < best) best = c, best_ct = ct;
+    best = 1e300;
+    if (best_ct >= 0)
+        for (int fw : fws)
+            if (sample(best_ct, fw, c, p) && p < best) best = p, best_fw = fw;
+    e->max_regions = keep_max;
+    e->phase_timing = keep_pt;
+    e->has_am = false; // the samples are not a result
+    e->has_mesh = false;
+    e->limit_hit = false;
+    if (best_ct < 0 || best_fw < 0) {
+        e->compose_tile = keep_ct;
+        e->face_warps = keep_fw;
+        return last_rc != AM_OK ? last_rc : AM_ERR_CUDA;
+    }
+    e->compose_tile = best_ct;
+    e->face_warps = best_fw;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tune[key] = {best_ct, best_fw};
+    }
+    if (chosen) chosen[0] = best_ct, chosen[1] = best_fw;
+    return AM_OK;
 }
 
 int am_run_batch(am_engine *const *engines, const am_run_args *args, int count, double *wall_ms)

@@ -162,15 +162,127 @@ __device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long 
     return true;
 }
 
+// A face belongs to a group of G warps (G = 1, 2, 4 or 8; wide networks use
+// more, so that a block holds fewer faces' rows and more warps).  The group
+// stages the rows together and splits the walk's per-step scan over them;
+// warp 0 of the group (the leader) runs everything else and sends each scan
+// to the others through shared memory: named barrier, every warp scans rows
+// k = 32 gw + lane (mod 32 G), partial (t, plane) pairs meet in shared
+// memory, barrier, the leader takes the minimum.  G = 1 is the plain warp
+// per face with no barrier.
+template <typename TC>
+struct GroupShared {
+    long long rl;  // the group's region (chunk-local)
+    int op, e, prev, pad;
+    TC v[8];       // scan: edge direction d0..d2, parallel threshold, point c0..c2
+    TC bt[8];      // partial minima per warp
+    int bk[8];
+};
+
+template <typename TC>
+struct Grp {
+    int G, gw, bar;
+    GroupShared<TC> *sh;
+    // named barrier 1 + group (at most four groups per block when G > 1);
+    // constant ids, so that a block reserves five barriers, not sixteen
+    __device__ __forceinline__ void sync() const
+    {
+        const int n = 32 * G;
+        switch (bar) {
+        case 1: asm volatile("bar.sync 1, %0;" ::"r"(n) : "memory"); break;
+        case 2: asm volatile("bar.sync 2, %0;" ::"r"(n) : "memory"); break;
+        case 3: asm volatile("bar.sync 3, %0;" ::"r"(n) : "memory"); break;
+        default: asm volatile("bar.sync 4, %0;" ::"r"(n) : "memory"); break;
+        }
+    }
+};
+
+template <typename TC>
+__host__ __device__ constexpr size_t group_shared_bytes()
+{
+    return (sizeof(GroupShared<TC>) + 15) / 16 * 16;
+}
+
+// first hit along the edge line over rows k0, k0 + kstep, ...: min over
+// crossing planes of t = max(0, -g) / a, compared as fractions within a lane
+// (two interleaved candidates per lane halve the compare chain), then across
+// the warp; every lane returns the warp's (t, plane), plane 0x7fffffff if none
+template <typename TC>
+__device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, int k0, int kstep, TC d0, TC d1, TC d2,
+                                         TC thr, TC c0, TC c1, TC c2, int e, int prev, TC &bt_out, int &bk_out)
+{
+    TC bnum = TC(1), bden = TC(0), bnum1 = TC(1), bden1 = TC(0);
+    int bk = 0x7fffffff, bk1 = 0x7fffffff;
+    auto consider = [&](int k, TC &bn, TC &bd, int &bi) {
+        const vec4_t<TC> r = rows[k];
+        const TC a = r.x * d0 + r.y * d1 + r.z * d2;
+        if (!(a > thr) || k == e || k == prev) return;
+        TC num = -(r.x * c0 + r.y * c1 + r.z * c2 + r.w);
+        num = num > TC(0) ? num : TC(0);
+        const TC lhs = num * bd, rhs = bn * a;
+        if (lhs < rhs || (lhs == rhs && k < bi)) {
+            bn = num;
+            bd = a;
+            bi = k;
+        }
+    };
+    int k = k0;
+    for (; k + kstep < ALL; k += 2 * kstep) {
+        consider(k, bnum, bden, bk);
+        consider(k + kstep, bnum1, bden1, bk1);
+    }
+    if (k < ALL) consider(k, bnum, bden, bk);
+    {
+        const TC lhs = bnum1 * bden, rhs = bnum * bden1;
+        if (bk1 != 0x7fffffff && (lhs < rhs || (lhs == rhs && bk1 < bk))) {
+            bnum = bnum1;
+            bden = bden1;
+            bk = bk1;
+        }
+    }
+    TC bt = bk == 0x7fffffff ? TC(INFINITY) : bnum / bden;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const TC ot = __shfl_xor_sync(0xffffffffu, bt, o);
+        const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+        if (ot < bt || (ot == bt && ok < bk)) {
+            bt = ot;
+            bk = ok;
+        }
+    }
+    bt_out = bt;
+    bk_out = bk;
+}
+
+// (helper warps of a group) scans on command until the leader ends the face
+template <typename TC>
+__device__ void group_helper(const vec4_t<TC> *rows, int ALL, const Grp<TC> &g, int lane)
+{
+    for (int guard = 0; guard < 4 * kWalkSteps; ++guard) { // the leader sends at most 2 kWalkSteps scans
+        g.sync();
+        if (g.sh->op == 0) return;
+        const TC *v = g.sh->v;
+        TC bt;
+        int bk;
+        hit_scan<TC>(rows, ALL, 32 * g.gw + lane, 32 * g.G, v[0], v[1], v[2], v[3], v[4], v[5], v[6], g.sh->e,
+                     g.sh->prev, bt, bk);
+        if (lane == 0) {
+            g.sh->bt[g.gw] = bt;
+            g.sh->bk[g.gw] = bk;
+        }
+        g.sync();
+    }
+}
+
 // One face walk: from the start plane s, ray shooting along each edge line
 // in the scan precision TC, vertices solved in TS.  Lane i ends with vertex
 // i (vx, vy, vz) and the plane of the edge leaving it (ve); lane j records
 // step j's hit plane (sbk) and merge decision (sdec, 0 append, 1 merge with
 // the previous vertex, 2 merge with the first), nsteps the steps taken.
-template <typename TC, typename TS>
+template <typename TC, typename TS, bool kGroup>
 __device__ void walk(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TS *eqv, const TS *p, int s, TC par_eps,
                      TS same_eps, int lane, TS &vx, TS &vy, TS &vz, int &ve, int &n, bool &closed, int8_t &status,
-                     int &sbk, int &sdec, int &nsteps)
+                     int &sbk, int &sdec, int &nsteps, const Grp<TC> &g)
 {
     TC cx = 0, cy = 0, cz = 0; // the vertex rounded to the scan precision
     vx = vy = vz = TS(0);
@@ -191,46 +303,29 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, con
         const TC d2 = eqc.x * ref_.y - eqc.y * ref_.x;
         const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
         const TC c0 = curc[0], c1 = curc[1], c2 = curc[2];
-        // first hit along the edge line: min over crossing planes of
-        // t = max(0, -g) / a, compared as fractions
-        // (two interleaved candidates per lane halve the compare chain)
-        TC bnum = TC(1), bden = TC(0), bnum1 = TC(1), bden1 = TC(0);
-        int bk = 0x7fffffff, bk1 = 0x7fffffff;
-        auto consider = [&](int k, TC &bn, TC &bd, int &bi) {
-            const vec4_t<TC> r = rows[k];
-            const TC a = r.x * d0 + r.y * d1 + r.z * d2;
-            if (!(a > thr) || k == e || k == prev) return;
-            TC num = -(r.x * c0 + r.y * c1 + r.z * c2 + r.w);
-            num = num > TC(0) ? num : TC(0);
-            const TC lhs = num * bd, rhs = bn * a;
-            if (lhs < rhs || (lhs == rhs && k < bi)) {
-                bn = num;
-                bd = a;
-                bi = k;
+        // first hit along the edge line, the scan split over the group
+        if (kGroup) {
+            if (lane == 0) {
+                TC *v = g.sh->v;
+                v[0] = d0, v[1] = d1, v[2] = d2, v[3] = thr, v[4] = c0, v[5] = c1, v[6] = c2;
+                g.sh->e = e;
+                g.sh->prev = prev;
+                g.sh->op = 1;
             }
-        };
-        int k = lane;
-        for (; k + 32 < ALL; k += 64) {
-            consider(k, bnum, bden, bk);
-            consider(k + 32, bnum1, bden1, bk1);
+            g.sync();
         }
-        if (k < ALL) consider(k, bnum, bden, bk);
-        {
-            const TC lhs = bnum1 * bden, rhs = bnum * bden1;
-            if (bk1 != 0x7fffffff && (lhs < rhs || (lhs == rhs && bk1 < bk))) {
-                bnum = bnum1;
-                bden = bden1;
-                bk = bk1;
-            }
-        }
-        TC bt = bk == 0x7fffffff ? TC(INFINITY) : bnum / bden;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const TC ot = __shfl_xor_sync(0xffffffffu, bt, o);
-            const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
-            if (ot < bt || (ot == bt && ok < bk)) {
-                bt = ot;
-                bk = ok;
+        TC bt;
+        int bk;
+        hit_scan<TC>(rows, ALL, lane, kGroup ? 32 * g.G : 32, d0, d1, d2, thr, c0, c1, c2, e, prev, bt, bk);
+        if (kGroup) {
+            g.sync();
+            for (int w = 1; w < g.G; ++w) {
+                const TC ot = g.sh->bt[w];
+                const int ok = g.sh->bk[w];
+                if (ot < bt || (ot == bt && ok < bk)) {
+                    bt = ot;
+                    bk = ok;
+                }
             }
         }
         if (bk == 0x7fffffff) { // the edge line never leaves the region
@@ -320,10 +415,10 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, con
 // solve at every step, when the TC walk did not close normally, took more
 // than 32 steps, met a vertex that is not finite in TS, or a decision comes
 // out differently in TS.
-template <typename TC, typename TS>
+template <typename TC, typename TS, bool kGroup>
 __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TS *eqv, const TS *p, int s,
                              TC par_eps, TS same_eps, int lane, TS &vx, TS &vy, TS &vz, int &ve, int &n, bool &closed,
-                             int8_t &status)
+                             int8_t &status, const Grp<TC> &g)
 {
     const unsigned full = 0xffffffffu;
     const TC eqf[4] = {eqc.x, eqc.y, eqc.z, eqc.w};
@@ -332,8 +427,8 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &
     int fve, fn, sbk, sdec, nsteps;
     bool fclosed;
     int8_t fst = kOk;
-    walk<TC, TC>(rows, ALL, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz, fve, fn, fclosed, fst, sbk, sdec,
-                 nsteps);
+    walk<TC, TC, kGroup>(rows, ALL, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz, fve, fn, fclosed, fst,
+                         sbk, sdec, nsteps, g);
     if (fst != kOk || !fclosed || nsteps < 1 || nsteps > 32) return false;
 
     // step j's vertex in TS, into lane j
@@ -421,31 +516,51 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &
 // signed geometric distances are then plain dot products, the same quantity
 // the reference's feasibility test computes as (w.x + b) * rsqrt(|w|^2)
 // (kernel.h:729-795).  TC is the scan precision, TS the solve precision.
-template <typename TC, typename TS>
+template <typename TC, typename TS, bool kGroup>
 __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
-                                                      int *err)
+                                                      int G_, int *err)
 {
+    const int G = kGroup ? G_ : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const int wpb = blockDim.x >> 5;
+    const int F = (blockDim.x >> 5) / G; // faces per block
+    const int gid = wib / G;
     const int ALL = net.ALL;
     const int N = net.N;
     const int W = net.W;
-    vec4_t<TC> *rows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)wib * net.ALLP;
+    vec4_t<TC> *rows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)gid * net.ALLP;
+    Grp<TC> g;
+    g.G = G;
+    g.gw = wib % G;
+    g.bar = 1 + gid;
+    g.sh = reinterpret_cast<GroupShared<TC> *>(smem_raw + (size_t)F * net.ALLP * sizeof(vec4_t<TC>) +
+                                               (size_t)gid * group_shared_bytes<TC>());
     const TC eps = (TC)tol.eps, par_eps = (TC)tol.par_eps;
     const TS same_eps = (TS)tol.same_eps;
 
     long long head;
     int count;
     chunk_range(ch, head, count);
-    // a region per warp: by launch position, or (fixed grid of the
-    // graph-driven loop) from the wave's work counter
-    for (long long rl = ch.ctl ? next_work(ch.ctl, lane) : (long long)blockIdx.x * wpb + wib; rl < count;
-         rl = ch.ctl ? next_work(ch.ctl, lane) : rl + (long long)gridDim.x * wpb) {
+    // a region per group: by launch position, or (fixed grid of the
+    // graph-driven loop) from the wave's work counter; the leader takes it
+    // and the group reads it from shared memory
+    long long rl_next = (long long)blockIdx.x * F + gid;
+    for (;;) {
+        long long rl;
+        if (g.gw == 0) {
+            rl = ch.ctl ? next_work(ch.ctl, lane) : rl_next;
+            if (kGroup && lane == 0) g.sh->rl = rl;
+        }
+        rl_next += (long long)gridDim.x * F;
+        if (kGroup) {
+            g.sync();
+            rl = g.sh->rl;
+        }
+        if (rl >= count) break;
         const long long rid = head + rl;
         const vec4_t<TC> *grows = reinterpret_cast<const vec4_t<TC> *>((const TC *)ch.cons + (size_t)rl * net.ALLP * 4);
-        for (int q = lane; q < ALL; q += 32) {
+        for (int q = 32 * g.gw + lane; q < ALL; q += 32 * G) {
             vec4_t<TC> v = grows[q];
             const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
             if (n2 > TC(0)) {
@@ -459,7 +574,14 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             }
             rows[q] = v;
         }
-        __syncwarp();
+        if (kGroup)
+            g.sync();
+        else
+            __syncwarp();
+        if (kGroup && g.gw != 0) { // the other warps of the group scan on the leader's command
+            group_helper<TC>(rows, ALL, g, lane);
+            continue;
+        }
         TS eqv[4];
         const vec4_t<TC> eqc = ld4<TC>((const TC *)ch.eq + (size_t)rl * 4); // scan precision copy
         eqv[0] = (TS)eqc.x;
@@ -550,13 +672,17 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         if (s >= 0) {
             bool done = false;
             if (sizeof(TS) > sizeof(TC)) // scan-precision walk, vertices refined in the solve precision
-                done = walk_refined<TC, TS>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n,
-                                            closed, status);
+                done = walk_refined<TC, TS, kGroup>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve,
+                                                    n, closed, status, g);
             if (!done) {
                 int sbk, sdec, nsteps;
-                walk<TC, TS>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n, closed, status,
-                             sbk, sdec, nsteps);
+                walk<TC, TS, kGroup>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n, closed,
+                                     status, sbk, sdec, nsteps, g);
             }
+        }
+        if (kGroup) { // the group is done with the rows
+            if (lane == 0) g.sh->op = 0;
+            g.sync();
         }
 
         // ---------------------------------------------------- outputs
@@ -612,38 +738,58 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
 
 } // namespace
 
+// Faces per block for G warps per face: as many as keep a block's rows
+// within 72 KB (three blocks per SM), at most 8 / G, a power of two.
+int polygon_faces_per_block(size_t row_bytes, int G)
+{
+    int F = 1;
+    while (2 * F * G <= 8 && (size_t)(2 * F) * row_bytes <= 72u * 1024u) F *= 2;
+    return F;
+}
+
+// Automatic warps per face: eight warps per block, split between faces
+// and the warps of a face as the rows allow.
+int polygon_face_warps(int prec, int ALLP)
+{
+    const size_t row_bytes = (prec == kFloat64 ? sizeof(double4) : sizeof(float4)) * (size_t)ALLP;
+    const int F = polygon_faces_per_block(row_bytes, 1);
+    return 8 / F;
+}
+
 template <typename TC, typename TS>
 void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs, const Tolerances &tol,
-                int *d_err, int wpb, size_t smem, cudaStream_t st)
+                int *d_err, int G, cudaStream_t st)
 {
-    auto k = polygon_kernel<TC, TS>;
+    const size_t row_bytes = sizeof(vec4_t<TC>) * (size_t)net.ALLP;
+    const int F = polygon_faces_per_block(row_bytes, G);
+    const size_t smem = row_bytes * F + (G > 1 ? group_shared_bytes<TC>() * F : 0);
+    auto k = G > 1 ? polygon_kernel<TC, TS, true> : polygon_kernel<TC, TS, false>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int sms = device_sms();
+    const int threads = 32 * F * G;
     int grid;
     if (ch.ctl) { // wave size on the device: as many blocks as stay resident
         int per_sm = 1;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 32 * wpb, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem);
         grid = sms * std::max(per_sm, 1);
     } else {
-        const long long need = (ch.count + wpb - 1) / wpb;
+        const long long need = (ch.count + F - 1) / F;
         grid = (int)std::min<long long>(need, (long long)sms * 16);
     }
-    k<<<grid, 32 * wpb, smem, st>>>(net, reg, ch, hs, tol, d_err);
+    k<<<grid, threads, smem, st>>>(net, reg, ch, hs, tol, G, d_err);
 }
 
 void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs,
-                    const Tolerances &tol, int *d_err, cudaStream_t st)
+                    const Tolerances &tol, int face_warps, int *d_err, cudaStream_t st)
 {
     if (!ch.ctl && ch.count <= 0) return;
-    const size_t row_bytes = (prec == kFloat64 ? sizeof(double4) : sizeof(float4)) * (size_t)net.ALLP;
-    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96u * 1024u) / std::max<size_t>(row_bytes, 1)));
-    const size_t smem = row_bytes * wpb; // the host rejects networks whose rows do not fit (am_init)
+    const int G = face_warps > 0 ? face_warps : polygon_face_warps(prec, net.ALLP);
     if (prec == kFloat64)
-        launch_one<double, double>(net, reg, ch, hs, tol, d_err, wpb, smem, st);
+        launch_one<double, double>(net, reg, ch, hs, tol, d_err, G, st);
     else if (prec == kMixed)
-        launch_one<float, double>(net, reg, ch, hs, tol, d_err, wpb, smem, st);
+        launch_one<float, double>(net, reg, ch, hs, tol, d_err, G, st);
     else
-        launch_one<float, float>(net, reg, ch, hs, tol, d_err, wpb, smem, st);
+        launch_one<float, float>(net, reg, ch, hs, tol, d_err, G, st);
 }
 
 } // namespace am

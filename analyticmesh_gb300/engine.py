@@ -195,6 +195,37 @@ class Engine:
         return Regions(N=self.N, **d)
 
 
+def _fill_run_args(a, k, eng, net, st, pt, iso, flip_insideout):
+    """One am_run_args record for network ``net`` on engine ``eng``; ``k``
+    keeps the converted arrays alive."""
+    dt = _np_dtype(eng.float_type)
+    a.weights = C.cast(k.ptr_array(net.W, dt), C.c_void_p)
+    a.biases = C.cast(k.ptr_array(net.b, dt), C.c_void_p)
+    a.states = k.ptr(st, np.uint8)
+    a.points = k.ptr(pt, dt)
+    a.num_points = int(st.shape[0])
+    shapes = np.ascontiguousarray([s for t in net.tms for s in tuple(t.shape)] or [0], dtype=np.int32)
+    k.objs.append(shapes)
+    a.arc_tm = C.cast(k.ptr_array(net.tms, dt), C.c_void_p)
+    a.arc_tm_shapes = shapes.ctypes.data
+    a.num_arc_tm = len(net.tms)
+    a.w_extra = k.ptr(net.w_extra, dt) if eng.E else None
+    a.b_extra = k.ptr(net.b_extra, dt) if eng.E else None
+    a.iso = float(iso)
+    a.flip_insideout = 1 if flip_insideout else 0
+
+
+def autotune(eng, net, states, points, iso=0.0, flip_insideout=False, sample_regions=65536):
+    """am_autotune: choose the composition tile and the warps per face for
+    this engine's architecture from sample runs; returns (tile, warps)."""
+    k = _Keep()
+    a = _lib.AmRunArgs()
+    _fill_run_args(a, k, eng, net, states, points, iso, flip_insideout)
+    chosen = (C.c_int32 * 2)()
+    _lib.check(_lib.lib().am_autotune(eng.h, C.byref(a), int(sample_regions), chosen), eng.h)
+    return int(chosen[0]), int(chosen[1])
+
+
 def run_batch(engines, nets, states_list, points_list, iso=0.0, flip_insideout=False):
     """am_run_batch: march every network at once, each on its engine (made
     for that network); returns the device wall time in ms.  Inputs may be
@@ -205,22 +236,7 @@ def run_batch(engines, nets, states_list, points_list, iso=0.0, flip_insideout=F
     k = _Keep()
     args = (_lib.AmRunArgs * n)()
     for i, (eng, net, st, pt) in enumerate(zip(engines, nets, states_list, points_list)):
-        dt = _np_dtype(eng.float_type)
-        a = args[i]
-        a.weights = C.cast(k.ptr_array(net.W, dt), C.c_void_p)
-        a.biases = C.cast(k.ptr_array(net.b, dt), C.c_void_p)
-        a.states = k.ptr(st, np.uint8)
-        a.points = k.ptr(pt, dt)
-        a.num_points = int(st.shape[0])
-        shapes = np.ascontiguousarray([s for t in net.tms for s in tuple(t.shape)] or [0], dtype=np.int32)
-        k.objs.append(shapes)
-        a.arc_tm = C.cast(k.ptr_array(net.tms, dt), C.c_void_p)
-        a.arc_tm_shapes = shapes.ctypes.data
-        a.num_arc_tm = len(net.tms)
-        a.w_extra = k.ptr(net.w_extra, dt) if eng.E else None
-        a.b_extra = k.ptr(net.b_extra, dt) if eng.E else None
-        a.iso = float(iso)
-        a.flip_insideout = 1 if flip_insideout else 0
+        _fill_run_args(args[i], k, eng, net, st, pt, iso, flip_insideout)
     handles = (C.c_void_p * n)(*[e.h for e in engines])
     wall = C.c_double(0.0)
     rc = _lib.lib().am_run_batch(handles, args, n, C.byref(wall))

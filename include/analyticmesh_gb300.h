@@ -156,12 +156,26 @@ typedef enum {
                                  returns AM_ERR_CAPACITY; the regions found so far are kept and can be
                                  queried (am_get_stats, am_get_regions, am_region_rows).  0 (default):
                                  no limit */
-    AM_OPT_COMPOSE_TILE = 6   /* "mixed" composition on the tensor cores: 0 (default) automatic, 1 the
+    AM_OPT_COMPOSE_TILE = 6,  /* "mixed" composition on the tensor cores: 0 (default) automatic, 1 the
                                  operand of a tile stays in shared memory for all layers, 2 it is rebuilt
                                  per 64-deep block from the rows just written (wider tiles for layers of
                                  256 units and more).  Both give the same bits. */
+    AM_OPT_FACE_WARPS = 7     /* warps per face polygon: 0 (default) automatic (one for narrow networks,
+                                 up to eight for wide ones, whose rows leave room for few faces per SM),
+                                 or 1, 2, 4, 8.  The warps of a face split the walk's scan over the rows. */
 } am_option;
 int am_set_option(am_engine *engine, int option, int64_t value);
+
+/* ---- autotuner (no counterpart in the reference): chooses AM_OPT_COMPOSE_TILE
+ * (mixed form) and AM_OPT_FACE_WARPS for this engine's network architecture by
+ * marching the first sample_regions regions of args once per candidate with
+ * per-phase device timing (after an untimed pass), and sets them on the
+ * engine.  The choice is remembered per architecture (widths, connections,
+ * precision, sample size) for the life of the process; a later call for the
+ * same architecture sets it without marching.  chosen (optional) receives
+ * {compose tile, warps per face}.  The engine holds no marching result
+ * afterwards: run am_analytic_marching. */
+int am_autotune(am_engine *engine, const am_run_args *args, int64_t sample_regions, int32_t *chosen);
 
 /* ---- self-test of the tensor-core tile used by the mixed-precision
  * composition (no counterpart in the reference): D (128 x N, fp32) =

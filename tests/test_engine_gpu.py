@@ -257,3 +257,43 @@ def test_region_limit_stops_and_keeps_results():
         rows, eq = eng.region_rows(0, 100)
         assert np.isfinite(rows).all() and np.isfinite(eq).all()
         eng.close()
+
+
+@pytest.mark.parametrize("form", ["mixed", "float32"])
+def test_warps_per_face_give_the_same_faces(form):
+    """AM_OPT_FACE_WARPS: one warp per face, or 2, 4, 8 warps splitting the
+    walk's scan over the rows -- the same regions, faces and vertices."""
+    m = wl.geometric([256, 256, 256], 14, perturb=0.02)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=7)
+    out = {}
+    for G in (1, 2, 4, 8):
+        eng = engine.march(net, st, pt, form, options={_lib.AM_OPT_FACE_WARPS: G})
+        r = eng.regions()
+        out[G] = (eng.stats()["num_regions"], r.bits.copy(), r.nverts.copy(), r.verts.copy(), r.edges.copy())
+        eng.close()
+    for G in (2, 4, 8):
+        assert out[G][0] == out[1][0], G
+        for a, b in zip(out[G][1:], out[1][1:]):
+            assert np.array_equal(a, b), G
+
+
+def test_autotune_chooses_options_and_keeps_results():
+    """am_autotune: sample runs pick the composition tile and the warps per
+    face; the marching afterwards gives the same regions as the defaults, and
+    a second engine of the same architecture takes the remembered choice."""
+    m = wl.geometric([256, 256], 5, perturb=0.01)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=2)
+    ref = engine.march(net, st, pt, "mixed")
+    want = ref.regions().bits.copy()
+    ref.close()
+    eng = engine.Engine("mixed", net.nodes, net.arc_table, 0)
+    tile, warps = engine.autotune(eng, net, st, pt, sample_regions=3000)
+    assert tile in (1, 2) and warps in (1, 2, 4, 8)
+    eng.run_net(net, st, pt)
+    assert np.array_equal(eng.regions().bits, want)
+    eng.close()
+    again = engine.Engine("mixed", net.nodes, net.arc_table, 0)
+    assert engine.autotune(again, net, st, pt, sample_regions=3000) == (tile, warps)
+    again.close()

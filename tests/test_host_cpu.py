@@ -100,3 +100,5 @@ def test_batch_and_option_argument_checks():
     assert L.am_run_batch(handles, args, 1, C.byref(wall)) == 2      # AM_ERR_NOT_INITIALIZED
     L.am_set_option.argtypes = [C.c_void_p, C.c_int, C.c_int64]
     assert L.am_set_option(None, _lib.AM_OPT_MAX_REGIONS, 10) == 2
+    assert L.am_set_option(None, _lib.AM_OPT_FACE_WARPS, 2) == 2
+    assert L.am_autotune(None, args, 1000, None) == 2                 # AM_ERR_NOT_INITIALIZED
