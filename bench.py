@@ -55,6 +55,8 @@ def parse():
                    help="batched workload: the first NETS of the 64 networks (all 64 take minutes per step)")
     p.add_argument("--seeds", type=int, default=1024)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--tune-sample", type=int, default=65536,
+                   help="batched workload: regions per autotuner sample run")
     p.add_argument("--host-loop", action="store_true",
                    help="drive the wave loop from the host (one launch sequence per wave): for ncu launch lists, "
                         "which cannot see kernels inside conditional graphs")
@@ -270,6 +272,9 @@ def bench_batched(args, ws, rank, local):
     pts = [p.float() for p in pts]
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     chosen = [engine.Engine("mixed", n.nodes, n.arc_table, n.num_extra) for n in nets]
+    # autotuner (untimed setup): composition tile and warps per face per architecture
+    tuned = [engine.autotune(e, n, s_, p_, sample_regions=args.tune_sample)
+             for e, n, s_, p_ in zip(chosen, dnets, sts, pts)]
     for _ in range(args.warmup):
         engine.run_batch(chosen, dnets, sts, pts)
     times, faces = [], 0
@@ -326,6 +331,8 @@ def bench_batched(args, ws, rank, local):
                                % (args.nets, 99 + args.nets), "seeds": args.seeds, "form": "mixed, batched",
                    "faces_per_step": faces, "regions_per_step": int(sum(regions)),
                    "largest_network_regions": int(max(regions)), "l2": "256 MiB flush before every timed step",
+                   "autotune": {"sample_regions": args.tune_sample,
+                                "tile_and_face_warps": ["%d/%d" % t for t in tuned]},
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "faces/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "plain_fp32_value": plain, "plain_form": "float32, networks one after the other",
