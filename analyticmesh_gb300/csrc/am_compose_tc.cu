@@ -148,6 +148,11 @@ struct XOp {
     {
         return mn ? umma::idesc_bf16_bmn(128, ncols) : umma::idesc_bf16(128, ncols);
     }
+    // descriptor steps (16-byte units of the start address field) from term
+    // u to u + 1 and from K step j to j + 1: desc(u, kb, j) = desc(0, kb, 0)
+    // + u * ustep() + j * jstep()
+    __device__ __forceinline__ uint32_t ustep() const { return (uint32_t)(xbytes >> 4); }
+    __device__ __forceinline__ uint32_t jstep() const { return mn ? (uint32_t)natoms * 128u : 2u; }
 };
 
 // X[n = 4r + c][k] = s_k(r) ? -C[r][src + k][c] : 0 for k < K, 0 up to Kp
@@ -242,6 +247,7 @@ __device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const T
 {
     const int ncols = X.ncols;
     const uint32_t idesc = X.idesc();
+    const uint64_t xu = X.ustep(), xj = X.jstep();
     const int kblocks = m.Kp / 64;
     for (int mt = 0; mt < mtiles; ++mt) {
         for (int kb = 0; kb < kblocks; ++kb) {
@@ -253,17 +259,18 @@ __device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const T
             const uint32_t d_main = tmem + (uint32_t)(mt * ncols);            // hh
             const uint32_t d_corr = tmem + (uint32_t)((mtiles + mt) * ncols); // the rest
             const bool fresh = first && kb == 0;
+            // A: term t at +16 KB (1024 units), K step j at +32 B (2 units)
+            const uint64_t ad = umma::desc_sw128(a0), xd = X.desc(0, kb, 0);
             #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const uint32_t o = (uint32_t)(j * 32); // A: 16 K columns = 32 bytes of each row
-                umma::mma_bf16(d_main, umma::desc_sw128(a0 + o), X.desc(0, kb, j), idesc, (fresh && j == 0) ? 0u : 1u);
+                umma::mma_bf16(d_main, ad + 2u * j, xd + xj * j, idesc, (fresh && j == 0) ? 0u : 1u);
                 int q = 0;
                 #pragma unroll
                 for (int t = 0; t < 3; ++t)
                     #pragma unroll
                     for (int u = 0; u + t < 3; ++u) {
                         if (t == 0 && u == 0) continue;
-                        umma::mma_bf16(d_corr, umma::desc_sw128(a0 + t * 16384u + o), X.desc(u, kb, j), idesc,
+                        umma::mma_bf16(d_corr, ad + 1024u * t + 2u * j, xd + xu * u + xj * j, idesc,
                                        (fresh && j == 0 && q == 0) ? 0u : 1u);
                         ++q;
                     }
@@ -294,6 +301,10 @@ __device__ __forceinline__ void gemm_observe(const WPipe &p, int last)
     umma::fence_after();
 }
 
+// words between two regions' keys in shared memory: odd, so that lanes
+// reading consecutive regions' bits hit distinct banks
+__host__ __device__ __forceinline__ int key_stride(int W) { return W | 1; }
+
 // tile width for a wave of `count` regions: one tile per resident slot
 // while the wave is small, the widest tile otherwise
 __host__ __device__ __forceinline__ int tile_cols(int count, int slots, int ncols_max)
@@ -323,6 +334,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     int tmem_cols = 32;
     while (tmem_cols < 2 * tc.mtiles_max * ncols) tmem_cols <<= 1;
     const size_t rstride = (size_t)net.ALLP * 4;
+    const int KW = key_stride(net.W); // odd: lanes on consecutive regions read distinct banks
 
     uint8_t *base = smem_raw + ((1024u - (umma::smem_addr(smem_raw) & 1023u)) & 1023u);
     XOp X;
@@ -335,7 +347,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     uint32_t *keys = reinterpret_cast<uint32_t *>(ws + (size_t)tc.nstage * kWBlockBytes); // the tile's bits
     // per CTA, for every tile: linear 0 as (w0, w1, w2, b) per unit and the
     // face-plane weights (the output linear's only row)
-    float4 *w0s = reinterpret_cast<float4 *>(keys + (size_t)(tc.ncols_max / 4) * net.W);
+    float4 *w0s = reinterpret_cast<float4 *>(keys + (size_t)(tc.ncols_max / 4) * key_stride(net.W));
     float *wls = reinterpret_cast<float *>(w0s + net.nodes[1]);
     float *fsum = reinterpret_cast<float *>(reinterpret_cast<uintptr_t>(wls + net.nodes[net.n_lin - 1] + 3) & ~(uintptr_t)15);
 
@@ -368,7 +380,8 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         float *cons = (float *)ch.cons + (size_t)rl0 * rstride;
         const uint32_t *gkeys = reg.keys + (size_t)(head + rl0) * net.W;
         __syncthreads(); // the previous tile is done with the keys and the operand
-        for (int q = tid; q < R * net.W; q += kThreads) keys[q] = q < nreg * net.W ? gkeys[q] : 0u;
+        for (int q = tid; q < R * net.W; q += kThreads)
+            keys[(q / net.W) * KW + q % net.W] = q < nreg * net.W ? gkeys[q] : 0u;
         __syncthreads(); // every thread reads every region's bits below
 
         // hidden layer 1 = linear 0 rows (sign-flipped) and the extra constraints
@@ -376,7 +389,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             const int n1 = net.nodes[1];
             for (int q = tid; q < nreg * n1; q += kThreads) {
                 const int rr = q / n1, m = q % n1;
-                const float sg = key_bit(keys + (size_t)rr * net.W, m) ? -1.f : 1.f;
+                const float sg = key_bit(keys + (size_t)rr * KW, m) ? -1.f : 1.f;
                 const float4 w = w0s[m];
                 st4<float>(cons + (size_t)rr * rstride + (size_t)m * 4, make_float4(sg * w.x, sg * w.y, sg * w.z, sg * w.w));
             }
@@ -393,7 +406,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             for (int q = tid; q < R * Kp; q += kThreads) {
                 const int r = q % R, k = q / R;
                 float x[4] = {0.f, 0.f, 0.f, 0.f};
-                if (r < nreg && k < n1 && key_bit(keys + (size_t)r * net.W, k)) {
+                if (r < nreg && k < n1 && key_bit(keys + (size_t)r * KW, k)) {
                     const float4 w = w0s[k];
                     x[0] = w.x;
                     x[1] = w.y;
@@ -419,13 +432,16 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                     // the operand is about to be overwritten: the products so far must be done
                     if (tid == 0) gemm_finish(pp, net, tc, g);
                     __syncthreads();
-                    stage_x_from_rows(X, cons, rstride, keys, net.W, nreg, net.hoff[sk.from],
+                    stage_x_from_rows(X, cons, rstride, keys, KW, nreg, net.hoff[sk.from],
                                       net.nodes[sk.from], tc.skip[i][s].Kp);
                     umma::fence_proxy_async();
                     __syncthreads();
                     if (tid == 0) gemm_issue(pp, net, tc, tc.skip[i][s], mtiles, X, tmem, false, g);
                 }
             }
+            // the first M tile's bias, loaded while the products run
+            const float *bias = (const float *)net.bias[i];
+            float bnext = q4 * 32 + lane < M ? bias[q4 * 32 + lane] : 0.f;
             if (tid == 0) {
                 gemm_finish(pp, net, tc, g);
                 s_last = g - 1;
@@ -434,7 +450,6 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             __syncthreads();
             gemm_observe(pp, s_last);
             // epilogue: accumulators -> constraint rows (HBM) and the next operand (smem)
-            const float *bias = (const float *)net.bias[i];
             const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
             for (int q = tid; q < R * (Kn - M); q += kThreads) {
                 const int r = q % R, k = M + q / R;
@@ -444,7 +459,8 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             for (int mt = 0; mt < mtiles; ++mt) {
                 const int m = mt * 128 + q4 * 32 + lane;
                 const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
-                const float bm = m < M ? bias[m] : 0.f;
+                const float bm = bnext;
+                if (mt + 1 < mtiles) bnext = m + 128 < M ? bias[m + 128] : 0.f;
                 const int row = net.hoff[i + 1] + m;
                 for (int cb = cgrp; cb < ncols / 16; cb += ngrp) {
                     float v[16], vc[16];
@@ -457,7 +473,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                         const int r = cb * 4 + qq;
                         x[4 * qq] = x[4 * qq + 1] = x[4 * qq + 2] = x[4 * qq + 3] = 0.f;
                         if (r < nreg) {
-                            const uint32_t *key = keys + (size_t)r * net.W;
+                            const uint32_t *key = keys + (size_t)r * KW;
                             float *cr = cons + (size_t)r * rstride;
                             float o[4] = {v[4 * qq] + vc[4 * qq], v[4 * qq + 1] + vc[4 * qq + 1],
                                           v[4 * qq + 2] + vc[4 * qq + 2], v[4 * qq + 3] + vc[4 * qq + 3] + bm};
@@ -532,7 +548,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                     float a = 0.f;
                     for (int w = 0; w < kWarps; ++w) a += fsum[(w * 32 + rr) * 4 + c];
                     if (rg < nreg) {
-                        const uint32_t *key = keys + (size_t)rg * net.W;
+                        const uint32_t *key = keys + (size_t)rg * KW;
                         const float *cr = cons + (size_t)rg * rstride;
                         for (int s = 0; s < net.nskip[i]; ++s) {
                             const SkipDev &sk = net.skip[i][s];
@@ -663,12 +679,16 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
     };
     while (cc.valid && issued < nst) copy_next();
     int h = 0, xb = 0;
+    // operand descriptors of the two stages; term and K step add constant offsets
+    const uint64_t xd0 = XS[0].desc(0, 0, 0), xd1 = XS[1].desc(0, 0, 0);
+    const uint64_t xu = XS[0].ustep(), xj = XS[0].jstep();
+    const uint32_t idesc = XS[0].idesc();
     while (mc.valid) {
         int src;
         const TcMat &m = job_mat(net, tc, mc.i, mc.job, src);
         const int mtiles = m.Mp / 128, kblocks = m.Kp / 64;
         const int xs = xb & 1;
-        const XOp &X = XS[xs];
+        const uint64_t xd = xs ? xd1 : xd0;
         if (mc.mt == 0) swait(xfull + xs, (uint32_t)(xb >> 1) & 1u, err); // operand block built
         while (cc.valid && issued <= h) copy_next();
         const int s = h % nst;
@@ -677,19 +697,18 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
         const uint32_t a0 = umma::smem_addr(ws + (size_t)s * kWBlockBytes);
         const uint32_t d_main = tmem + (uint32_t)(mc.mt * ncols);
         const uint32_t d_corr = tmem + (uint32_t)((mtiles + mc.mt) * ncols);
-        const uint32_t idesc = X.idesc();
         const bool fresh = mc.job == 0 && mc.kb == 0;
+        const uint64_t ad = umma::desc_sw128(a0); // term t at +16 KB, K step j at +32 B
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const uint32_t o = (uint32_t)(j * 32);
-            umma::mma_bf16(d_main, umma::desc_sw128(a0 + o), X.desc(0, 0, j), idesc, (fresh && j == 0) ? 0u : 1u);
+            umma::mma_bf16(d_main, ad + 2u * j, xd + xj * j, idesc, (fresh && j == 0) ? 0u : 1u);
             int q = 0;
 #pragma unroll
             for (int t = 0; t < 3; ++t)
 #pragma unroll
                 for (int u = 0; u + t < 3; ++u) {
                     if (t == 0 && u == 0) continue;
-                    umma::mma_bf16(d_corr, umma::desc_sw128(a0 + t * 16384u + o), X.desc(u, 0, j), idesc,
+                    umma::mma_bf16(d_corr, ad + 1024u * t + 2u * j, xd + xu * u + xj * j, idesc,
                                    (fresh && j == 0 && q == 0) ? 0u : 1u);
                     ++q;
                 }
@@ -712,8 +731,8 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                                                                     float iso, int slots, int *err)
 {
     extern __shared__ uint8_t smem_raw[];
-    // wfull[2], wdone[2] (weight ring), xfull[2], xdone[2] (operand ring), accdone
-    __shared__ uint64_t bars[9];
+    // wfull[3], wdone[3] (weight ring), xfull[2], xdone[2] (operand ring), accdone
+    __shared__ uint64_t bars[11];
     __shared__ uint32_t tslot;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     long long head;
@@ -728,6 +747,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
     int tmem_cols = 32;
     while (tmem_cols < 2 * tc.mtiles_max * ncols) tmem_cols <<= 1;
     const size_t rstride = (size_t)net.ALLP * 4;
+    const int KW = key_stride(net.W); // odd: lanes on consecutive regions read distinct banks
 
     uint8_t *base = smem_raw + ((1024u - (umma::smem_addr(smem_raw) & 1023u)) & 1023u);
     XOp XS[2];
@@ -742,13 +762,13 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
     }
     uint8_t *ws = base + 6 * plane;
     uint32_t *keys = reinterpret_cast<uint32_t *>(ws + (size_t)tc.nstage * kWBlockBytes);
-    float4 *w0s = reinterpret_cast<float4 *>(keys + (size_t)(tc.ncols_max / 4) * net.W);
+    float4 *w0s = reinterpret_cast<float4 *>(keys + (size_t)(tc.ncols_max / 4) * key_stride(net.W));
     float *wls = reinterpret_cast<float *>(w0s + net.nodes[1]);
     float *fsum = reinterpret_cast<float *>(reinterpret_cast<uintptr_t>(wls + net.nodes[net.n_lin - 1] + 3) & ~(uintptr_t)15);
-    uint64_t *wfull = bars, *wdone = bars + 2, *xfull = bars + 4, *xdone = bars + 6, *accdone = bars + 8;
+    uint64_t *wfull = bars, *wdone = bars + 3, *xfull = bars + 6, *xdone = bars + 8, *accdone = bars + 10;
 
     if (tid == 0) {
-        for (int b = 0; b < 4; ++b) umma::mbar_init(bars + b, 1);
+        for (int b = 0; b < 6; ++b) umma::mbar_init(bars + b, 1);
         umma::mbar_init(xfull, kSBuild);
         umma::mbar_init(xfull + 1, kSBuild);
         umma::mbar_init(xdone, 1);
@@ -784,13 +804,14 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
             float *cons = (float *)ch.cons + (size_t)rl0 * rstride;
             const uint32_t *gkeys = reg.keys + (size_t)(head + rl0) * net.W;
             bar_builders(); // the previous tile is done with the keys
-            for (int q = tid; q < R * net.W; q += kSBuild) keys[q] = q < nreg * net.W ? gkeys[q] : 0u;
+            for (int q = tid; q < R * net.W; q += kSBuild)
+                keys[(q / net.W) * KW + q % net.W] = q < nreg * net.W ? gkeys[q] : 0u;
             bar_builders();
             // hidden layer 1 = linear 0 rows (sign-flipped) and the extra constraints
             const int n1 = net.nodes[1];
             for (int q = tid; q < nreg * n1; q += kSBuild) {
                 const int rr = q / n1, m = q % n1;
-                const float sg = key_bit(keys + (size_t)rr * net.W, m) ? -1.f : 1.f;
+                const float sg = key_bit(keys + (size_t)rr * KW, m) ? -1.f : 1.f;
                 const float4 w = w0s[m];
                 st4<float>(cons + (size_t)rr * rstride + (size_t)m * 4, make_float4(sg * w.x, sg * w.y, sg * w.z, sg * w.w));
             }
@@ -824,7 +845,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                                 const int q = q0 + u * kSBuild;
                                 const int r = q % R, kk = q / R, k = kb * 64 + kk;
                                 x[u][0] = x[u][1] = x[u][2] = x[u][3] = 0.f;
-                                if (q < R * 64 && r < nreg && k < K && key_bit(keys + (size_t)r * net.W, rows0 + k)) {
+                                if (q < R * 64 && r < nreg && k < K && key_bit(keys + (size_t)r * KW, rows0 + k)) {
                                     if (src == 1) {
                                         const float4 w = w0s[k];
                                         x[u][0] = w.x, x[u][1] = w.y, x[u][2] = w.z, x[u][3] = w.w;
@@ -845,15 +866,17 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                         ++xb;
                     }
                 }
+                const float *bias = (const float *)net.bias[i];
+                float bnext = q4 * 32 + lane < M ? bias[q4 * 32 + lane] : 0.f; // loaded while the products run
                 swait(accdone, (uint32_t)(accph & 1), err); // the layer's products are in TMEM
                 ++accph;
                 umma::fence_after();
                 // epilogue: accumulators -> constraint rows of hidden layer i + 1
-                const float *bias = (const float *)net.bias[i];
                 for (int mt = 0; mt < mtiles; ++mt) {
                     const int m = mt * 128 + q4 * 32 + lane;
                     const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
-                    const float bm = m < M ? bias[m] : 0.f;
+                    const float bm = bnext;
+                    if (mt + 1 < mtiles) bnext = m + 128 < M ? bias[m + 128] : 0.f;
                     const int row = net.hoff[i + 1] + m;
                     for (int cb = cgrp; cb < ncols / 16; cb += ngrp) {
                         float v[16], vc[16];
@@ -864,7 +887,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                         for (int qq = 0; qq < 4; ++qq) {
                             const int r = cb * 4 + qq;
                             if (r >= nreg) continue;
-                            const uint32_t *key = keys + (size_t)r * net.W;
+                            const uint32_t *key = keys + (size_t)r * KW;
                             float *cr = cons + (size_t)r * rstride;
                             float o[4] = {v[4 * qq] + vc[4 * qq], v[4 * qq + 1] + vc[4 * qq + 1],
                                           v[4 * qq + 2] + vc[4 * qq + 2], v[4 * qq + 3] + vc[4 * qq + 3] + bm};
@@ -914,7 +937,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                         for (int k = warp; k < K; k += kWarps) {
                             const float w = wls[k];
                             float x[4] = {0.f, 0.f, 0.f, 0.f};
-                            if (key_bit(keys + (size_t)r * net.W, rows0 + k)) {
+                            if (key_bit(keys + (size_t)r * KW, rows0 + k)) {
                                 const float4 c = ld4<float>(cons + (size_t)r * rstride + (size_t)(rows0 + k) * 4);
                                 x[0] = -c.x, x[1] = -c.y, x[2] = -c.z, x[3] = -c.w;
                             }
@@ -928,7 +951,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                         float a = 0.f;
                         for (int w = 0; w < kWarps; ++w) a += fsum[(w * 32 + rr) * 4 + c];
                         if (rg < nreg) {
-                            const uint32_t *key = keys + (size_t)rg * net.W;
+                            const uint32_t *key = keys + (size_t)rg * KW;
                             const float *cr = cons + (size_t)rg * rstride;
                             for (int s = 0; s < net.nskip[i]; ++s) {
                                 const SkipDev &sk = net.skip[i][s];
@@ -1000,11 +1023,11 @@ size_t tc_smem_bytes(const TcNet &tc, int ncols, int W)
 {
     if (tc.streamed) { // two operand stages of one K block each
         const size_t cols = tc.mn ? (size_t)(ncols + 63) / 64 * 64 : (size_t)ncols;
-        return 1024 + 6 * cols * 64 * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * W * 4 +
+        return 1024 + 6 * cols * 64 * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * key_stride(W) * 4 +
                16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last + 16 + (size_t)kSFaceSumBytes;
     }
     const size_t cols = tc.mn ? (size_t)(ncols + 63) / 64 * 64 : (size_t)ncols;
-    return 1024 + 3 * cols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * W * 4 +
+    return 1024 + 3 * cols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * key_stride(W) * 4 +
            16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last + 16 + (size_t)kFaceSumBytes;
 }
 

@@ -584,7 +584,7 @@ void run_begin(am_engine *e, const RunArgs &a)
         for (int mn = 1; mn >= 0 && tc.ncols_max < 16; --mn)
             for (tc.nstage = 2; tc.nstage >= 1; --tc.nstage) {
                 const long long room = (long long)smem_cap - 1024 - (long long)tc.nstage * kWBlockBytes -
-                                       64ll * e->W * 4 - 16ll * tc.n1 - 4ll * tc.k_last - 16 - 512 * 16;
+                                       64ll * (e->W | 1) * 4 - 16ll * tc.n1 - 4ll * tc.k_last - 16 - 512 * 16;
                 long long c = std::max<long long>(0, room) / (6ll * tc.kp_max);
                 if (mn) c = c / 64 * 64;
                 int ncols = (int)std::min<long long>(c, 256);
@@ -595,20 +595,21 @@ void run_begin(am_engine *e, const RunArgs &a)
             }
         // streamed operand (wide layers): two 64-deep operand blocks, so the
         // tile is as wide as TMEM allows; taken when that is wider
+        // (the widest tile first, then the most weight stages in flight)
         TcNet ts = tc;
         ts.streamed = 1;
         ts.ncols_max = 0;
-        for (int mn = 1; mn >= 0 && ts.ncols_max < 16; --mn)
-            for (ts.nstage = 2; ts.nstage >= 1; --ts.nstage) {
-                ts.mn = mn;
-                int ncols = std::min(256, 256 / ts.mtiles_max) / 16 * 16;
-                for (; ncols >= 16; ncols -= 16) {
+        for (int mn = 1; mn >= 0 && ts.ncols_max < 16; --mn) {
+            ts.mn = mn;
+            for (int ncols = std::min(256, 256 / ts.mtiles_max) / 16 * 16; ncols >= 16 && ts.ncols_max < 16;
+                 ncols -= 16)
+                for (int ns = 3; ns >= 1; --ns) {
                     ts.ncols_max = ncols;
+                    ts.nstage = ns;
                     if (tc_smem_bytes(ts, ncols, e->W) <= smem_cap) break;
+                    ts.ncols_max = 0;
                 }
-                ts.ncols_max = std::max(ncols, 0);
-                if (ts.ncols_max >= 16) break;
-            }
+        }
         const bool want_streamed = e->compose_tile == 2 ||
                                    (e->compose_tile == 0 && tc.kp_max >= 256 && ts.ncols_max > tc.ncols_max);
         if (ts.ncols_max >= 16 && (want_streamed || tc.ncols_max < 16)) tc = ts;
@@ -830,22 +831,20 @@ void run_end(am_engine *e)
     sx.frontier_ms = t_front;
     sx.kernel_launches = launches;
     {
-        std::vector<int32_t> hn((size_t)tail);
-        std::vector<int8_t> hsx((size_t)tail);
-        AM_CUDA(cudaMemcpyAsync(hn.data(), e->nv.p, sizeof(int32_t) * tail, cudaMemcpyDeviceToHost, st));
-        AM_CUDA(cudaMemcpyAsync(hsx.data(), e->status.p, sizeof(int8_t) * tail, cudaMemcpyDeviceToHost, st));
+        // face and status counts, reduced on the device (48 bytes come back)
+        unsigned long long *d = (unsigned long long *)((char *)e->d_tail.p + kStatsOff);
+        const unsigned long long *h = (const unsigned long long *)((const char *)e->h_ctl + kStatsOff);
+        AM_CUDA(cudaMemsetAsync(d, 0, kStatsCount * sizeof(unsigned long long), st));
+        launch_region_stats(e->nv.as<int32_t>(), e->status.as<int8_t>(), tail, d, st);
+        AM_CUDA(cudaMemcpyAsync((char *)e->h_ctl + kStatsOff, d, kStatsCount * sizeof(unsigned long long),
+                                cudaMemcpyDeviceToHost, st));
         AM_CUDA(cudaStreamSynchronize(st));
-        for (long long r = 0; r < tail; ++r) {
-            if (hn[r] >= 3) sx.num_faces++;
-            sx.max_polygon_verts = std::max(sx.max_polygon_verts, hn[r]);
-            switch (hsx[r]) {
-            case kNoStart: sx.num_nostart++; break;
-            case kOpen: sx.num_open++; break;
-            case kTruncated: sx.num_truncated++; break;
-            case kSingular: sx.num_singular++; break;
-            default: break;
-            }
-        }
+        sx.num_faces = (int64_t)h[0];
+        sx.max_polygon_verts = (int32_t)h[1];
+        sx.num_nostart = (int64_t)h[2 + kNoStart - 1];
+        sx.num_open = (int64_t)h[2 + kOpen - 1];
+        sx.num_truncated = (int64_t)h[2 + kTruncated - 1];
+        sx.num_singular = (int64_t)h[2 + kSingular - 1];
     }
     e->flip = flip_insideout ? 1 : 0;
     e->iso = iso;
@@ -920,11 +919,11 @@ int am_init(am_engine **out, const char *float_type, const int32_t *nodesnum, in
                  "too many constraint rows for one face (sum of hidden widths + extra constraints)");
         AM_CUDA(cudaStreamCreateWithFlags(&e->own, cudaStreamNonBlocking));
         e->st = e->own;
-        AM_CUDA(e->d_tail.alloc(sizeof(WaveCtl)));
-        AM_CUDA(cudaMemset(e->d_tail.p, 0, sizeof(WaveCtl)));
+        AM_CUDA(e->d_tail.alloc(kCtlBytes));
+        AM_CUDA(cudaMemset(e->d_tail.p, 0, kCtlBytes));
         e->d_err.p = &((WaveCtl *)e->d_tail.p)->err;
-        AM_CUDA(cudaHostAlloc((void **)&e->h_ctl, sizeof(WaveCtl), cudaHostAllocDefault));
-        memset(e->h_ctl, 0, sizeof(WaveCtl));
+        AM_CUDA(cudaHostAlloc((void **)&e->h_ctl, kCtlBytes, cudaHostAllocDefault));
+        memset(e->h_ctl, 0, kCtlBytes);
     });
     if (rc == AM_OK) *out = e.release();
     return rc;

@@ -272,6 +272,41 @@ __global__ void wave_step_kernel(WaveCtl *ctl, cudaGraphConditionalHandle cond)
     cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 
+// run statistics: faces (>= 3 vertices), the largest polygon, and one count
+// per failure status
+__global__ void region_stats_kernel(const int32_t *nv, const int8_t *status, long long n, unsigned long long *out)
+{
+    __shared__ unsigned int s[kStatsCount];
+    if (threadIdx.x < kStatsCount) s[threadIdx.x] = 0u;
+    __syncthreads();
+    unsigned int faces = 0, vmax = 0, bad[4] = {0u, 0u, 0u, 0u};
+    for (long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+        const int v = nv[r];
+        faces += v >= 3 ? 1u : 0u;
+        vmax = max(vmax, (unsigned int)max(v, 0));
+        const int st = status[r];
+        if (st >= kNoStart && st <= kSingular) bad[st - kNoStart]++;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        faces += __shfl_xor_sync(0xffffffffu, faces, o);
+        vmax = max(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+#pragma unroll
+        for (int b = 0; b < 4; ++b) bad[b] += __shfl_xor_sync(0xffffffffu, bad[b], o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(&s[0], faces);
+        atomicMax(&s[1], vmax);
+        for (int b = 0; b < 4; ++b) atomicAdd(&s[2 + b], bad[b]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(out, (unsigned long long)s[0]);
+        atomicMax(out + 1, (unsigned long long)s[1]);
+        for (int b = 0; b < 4; ++b) atomicAdd(out + 2 + b, (unsigned long long)s[2 + b]);
+    }
+}
+
 __global__ void rehash_kernel(RegionsDev reg, long long n, HashDev hs, int *err)
 {
     const long long rid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -339,6 +374,14 @@ void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg,
 void launch_wave_step(WaveCtl *ctl, cudaGraphConditionalHandle cond, cudaStream_t st)
 {
     wave_step_kernel<<<1, 1, 0, st>>>(ctl, cond);
+}
+
+void launch_region_stats(const int32_t *nv, const int8_t *status, long long n, unsigned long long *out,
+                         cudaStream_t st)
+{
+    if (n <= 0) return;
+    const int grid = (int)std::min<long long>((n + 255) / 256, 4ll * device_sms());
+    region_stats_kernel<<<grid, 256, 0, st>>>(nv, status, n, out);
 }
 
 void launch_rehash(const RegionsDev &reg, long long n, const HashDev &hs, int *d_err, cudaStream_t st)

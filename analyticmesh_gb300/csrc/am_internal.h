@@ -84,6 +84,13 @@ struct WaveCtl {
     long long stop_tail; // stop after the wave that takes tail past this (a region limit)
 };
 
+// the control block's device / pinned allocation: WaveCtl, then the run's
+// statistics counters (faces, largest polygon, then one count per status
+// kNoStart .. kSingular)
+constexpr int kStatsCount = 6;
+constexpr size_t kStatsOff = (sizeof(WaveCtl) + 15) / 16 * 16;
+constexpr size_t kCtlBytes = kStatsOff + kStatsCount * sizeof(unsigned long long);
+
 struct ChunkDev {
     long long head;     // first rid of the chunk
     int count;          // regions in the chunk
@@ -128,6 +135,8 @@ void launch_append(int mode, int prec, const NetDev &net, const RegionsDev &reg,
                    int n_items, long long *d_tail, int *d_blocksum, int nblocks_cap, int *d_err, cudaStream_t st);
 void launch_rehash(const RegionsDev &reg, long long n, const HashDev &hs, int *d_err, cudaStream_t st);
 // graph-driven loop: advance ctl to the next wave and set the loop condition
+void launch_region_stats(const int32_t *nv, const int8_t *status, long long n, unsigned long long *out,
+                         cudaStream_t st);
 void launch_wave_step(WaveCtl *ctl, cudaGraphConditionalHandle cond, cudaStream_t st);
 int device_sms();
 void launch_prepare_weights(int prec, const void *src, int M, int K, int Mp, void *dst, cudaStream_t st);

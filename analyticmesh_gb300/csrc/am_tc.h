@@ -27,7 +27,7 @@ struct TcNet {
     int ncols_max;                      // widest UMMA N = 4 x regions per CTA (multiple of 16, <= 256)
     int kp_max;                         // largest padded K of any operand
     int mtiles_max;                     // largest number of 128-row tiles of any layer
-    int nstage;                         // weight blocks in flight (1 or 2)
+    int nstage;                         // weight blocks in flight (1 or 2; up to 3 with the streamed operand)
     int mn;                             // operand layout: 1 MN-major (64-column atoms), 0 K-major
     int n1, k_last;                     // widths of hidden layer 1 and of the last hidden layer
     int streamed;                       // operand rebuilt per 64-wide K block from the rows (wide layers)
