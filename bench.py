@@ -35,11 +35,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 REF_SAMPLE_REGIONS = 65536
-# DRAM bytes (read + write) per region of the two heavy kernels on the sphere
-# workload in the mixed form, from one ncu capture each (a 12,672-region
-# wave): profiles/compose_tc_sphere_128x4.md, profiles/polygon_mixed_sphere_128x4.md
-NCU_TRAFFIC_PER_REGION = {("sphere", "mixed"): {"compose": (1.22e6 + 45.31e6) / 12672,
-                                                "polygon": (109.57e6 + 3.77e6) / 12672}}
+# DRAM bytes (read + write) per region of the two heavy kernels in the mixed
+# form, from one ncu capture each (--set full, dram__bytes_read.sum +
+# dram__bytes_write.sum): the sphere workload's wave of 12,672 regions and the
+# deep workload's wave of ~40,150 regions
+NCU_TRAFFIC_PER_REGION = {("sphere", "mixed"): {"compose": (1.214e6 + 45.631e6) / 12672,
+                                                "polygon": (109.571e6 + 4.067e6) / 12672},
+                          ("deep", "mixed"): {"compose": (27.491e6 + 957.757e6) / 40150,
+                                              "polygon": (1018.464e6 + 20.326e6) / 40150}}
 FLOPS_PER_REGION = {}
 
 
@@ -449,7 +452,7 @@ def main():
                 "frac": ach / hbm, "traffic": tr * regions if tr else None, "peak_kind": peak_kind,
                 "algorithmic": "%d B/region x %d regions" % (poly_bytes // max(regions, 1), regions)}
     if roof["traffic"] is not None:
-        roof["traffic_note"] = "ncu dram bytes per region of one captured wave x regions per step (profiles/)"
+        roof["traffic_note"] = "ncu dram bytes per region of one captured wave x regions per step"
 
     # the chosen engine's stores go back before the plain form's are built
     # (large networks hold tens of GB of regions)
