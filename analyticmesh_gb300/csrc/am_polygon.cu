@@ -164,19 +164,19 @@ __device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long 
 
 // A face belongs to a group of G warps (G = 1, 2, 4 or 8; wide networks use
 // more, so that a block holds fewer faces' rows and more warps).  The group
-// stages the rows together and splits the walk's per-step scan over them;
-// warp 0 of the group (the leader) runs everything else and sends each scan
-// to the others through shared memory: named barrier, every warp scans rows
-// k = 32 gw + lane (mod 32 G), partial (t, plane) pairs meet in shared
-// memory, barrier, the leader takes the minimum.  G = 1 is the plain warp
-// per face with no barrier.
+// stages the rows together, and every warp of it runs the same walk on them:
+// each scans rows k = 32 gw + lane (mod 32 G), the partial (t, plane) minima
+// meet in shared memory (two slots, by step parity) behind one named barrier
+// per step, and every warp takes the same minimum, so the group stays in
+// step without further messages.  Warp 0 (the leader) alone re-solves the
+// vertices in the solve precision and writes the outputs.  G = 1 is the plain
+// warp per face with no barrier.
 template <typename TC>
 struct GroupShared {
-    long long rl;  // the group's region (chunk-local)
-    int op, e, prev, pad;
-    TC v[8];       // scan: edge direction d0..d2, parallel threshold, point c0..c2
-    TC bt[8];      // partial minima per warp
-    int bk[8];
+    long long rl;   // the group's region (chunk-local)
+    int done, pad;  // the leader's refinement verdict
+    TC bt[2][8];    // partial minima per step parity and warp
+    int bk[2][8];
 };
 
 template <typename TC>
@@ -254,26 +254,6 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, int k0
     bk_out = bk;
 }
 
-// (helper warps of a group) scans on command until the leader ends the face
-template <typename TC>
-__device__ void group_helper(const vec4_t<TC> *rows, int ALL, const Grp<TC> &g, int lane)
-{
-    for (int guard = 0; guard < 4 * kWalkSteps; ++guard) { // the leader sends at most 2 kWalkSteps scans
-        g.sync();
-        if (g.sh->op == 0) return;
-        const TC *v = g.sh->v;
-        TC bt;
-        int bk;
-        hit_scan<TC>(rows, ALL, 32 * g.gw + lane, 32 * g.G, v[0], v[1], v[2], v[3], v[4], v[5], v[6], g.sh->e,
-                     g.sh->prev, bt, bk);
-        if (lane == 0) {
-            g.sh->bt[g.gw] = bt;
-            g.sh->bk[g.gw] = bk;
-        }
-        g.sync();
-    }
-}
-
 // One face walk: from the start plane s, ray shooting along each edge line
 // in the scan precision TC, vertices solved in TS.  Lane i ends with vertex
 // i (vx, vy, vz) and the plane of the edge leaving it (ve); lane j records
@@ -304,24 +284,22 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, con
         const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
         const TC c0 = curc[0], c1 = curc[1], c2 = curc[2];
         // first hit along the edge line, the scan split over the group
-        if (kGroup) {
-            if (lane == 0) {
-                TC *v = g.sh->v;
-                v[0] = d0, v[1] = d1, v[2] = d2, v[3] = thr, v[4] = c0, v[5] = c1, v[6] = c2;
-                g.sh->e = e;
-                g.sh->prev = prev;
-                g.sh->op = 1;
-            }
-            g.sync();
-        }
         TC bt;
         int bk;
-        hit_scan<TC>(rows, ALL, lane, kGroup ? 32 * g.G : 32, d0, d1, d2, thr, c0, c1, c2, e, prev, bt, bk);
+        hit_scan<TC>(rows, ALL, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1, d2, thr, c0, c1, c2, e,
+                     prev, bt, bk);
         if (kGroup) {
+            const int par = step & 1;
+            if (lane == 0) {
+                g.sh->bt[par][g.gw] = bt;
+                g.sh->bk[par][g.gw] = bk;
+            }
             g.sync();
+            bt = g.sh->bt[par][0];
+            bk = g.sh->bk[par][0];
             for (int w = 1; w < g.G; ++w) {
-                const TC ot = g.sh->bt[w];
-                const int ok = g.sh->bk[w];
+                const TC ot = g.sh->bt[par][w];
+                const int ok = g.sh->bk[par][w];
                 if (ot < bt || (ot == bt && ok < bk)) {
                     bt = ot;
                     bk = ok;
@@ -430,6 +408,7 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &
     walk<TC, TC, kGroup>(rows, ALL, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz, fve, fn, fclosed, fst,
                          sbk, sdec, nsteps, g);
     if (fst != kOk || !fclosed || nsteps < 1 || nsteps > 32) return false;
+    if (kGroup && g.gw != 0) return true; // the leader refines; the caller shares its verdict
 
     // step j's vertex in TS, into lane j
     const int G = lane >> 2, L = lane & 3, gbase = lane & ~3;
@@ -578,10 +557,6 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             g.sync();
         else
             __syncwarp();
-        if (kGroup && g.gw != 0) { // the other warps of the group scan on the leader's command
-            group_helper<TC>(rows, ALL, g, lane);
-            continue;
-        }
         TS eqv[4];
         const vec4_t<TC> eqc = ld4<TC>((const TC *)ch.eq + (size_t)rl * 4); // scan precision copy
         eqv[0] = (TS)eqc.x;
@@ -672,18 +647,22 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         if (s >= 0) {
             bool done = false;
             if (sizeof(TS) > sizeof(TC)) // scan-precision walk, vertices refined in the solve precision
+            {
                 done = walk_refined<TC, TS, kGroup>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve,
                                                     n, closed, status, g);
+                if (kGroup) { // the leader's verdict for the group
+                    if (g.gw == 0 && lane == 0) g.sh->done = done ? 1 : 0;
+                    g.sync();
+                    done = g.sh->done != 0;
+                }
+            }
             if (!done) {
                 int sbk, sdec, nsteps;
                 walk<TC, TS, kGroup>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n, closed,
                                      status, sbk, sdec, nsteps, g);
             }
         }
-        if (kGroup) { // the group is done with the rows
-            if (lane == 0) g.sh->op = 0;
-            g.sync();
-        }
+        if (kGroup && g.gw != 0) continue; // the leader writes the face
 
         // ---------------------------------------------------- outputs
         if (lane == 0) {
