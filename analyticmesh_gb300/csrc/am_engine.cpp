@@ -232,6 +232,7 @@ struct am_engine {
     DevBuf w_table, w_rep, w_flag, w_vidx, w_bsum, w_fflag, w_fsize, w_fid, w_foff, w_verts, w_fs, w_fi, w_counts;
     std::vector<double> mesh_verts;
     std::vector<int32_t> mesh_fs, mesh_fi;
+    bool mesh_host = false; // the welded mesh has been copied into the vectors above
 
     ~am_engine()
     {
@@ -1167,6 +1168,29 @@ int am_get_stats(const am_engine *e, am_stats *out)
     return AM_OK;
 }
 
+// the welded mesh from its device buffers into the engine's host vectors
+static void fetch_mesh(am_engine *e)
+{
+    if (e->mesh_host) return;
+    cudaStream_t st = e->st;
+    const long long V = e->stats.mesh_num_verts, F = e->stats.mesh_num_faces, I = e->stats.mesh_num_indices;
+    e->mesh_verts.resize((size_t)V * 3);
+    e->mesh_fs.resize((size_t)F);
+    e->mesh_fi.resize((size_t)I);
+    if (e->ts == 8) {
+        AM_CUDA(cudaMemcpyAsync(e->mesh_verts.data(), e->w_verts.p, sizeof(double) * 3 * V, cudaMemcpyDeviceToHost, st));
+    } else {
+        std::vector<float> tmp((size_t)V * 3);
+        AM_CUDA(cudaMemcpyAsync(tmp.data(), e->w_verts.p, sizeof(float) * 3 * V, cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        for (size_t q = 0; q < tmp.size(); ++q) e->mesh_verts[q] = tmp[q];
+    }
+    AM_CUDA(cudaMemcpyAsync(e->mesh_fs.data(), e->w_fs.p, sizeof(int) * F, cudaMemcpyDeviceToHost, st));
+    AM_CUDA(cudaMemcpyAsync(e->mesh_fi.data(), e->w_fi.p, sizeof(int) * I, cudaMemcpyDeviceToHost, st));
+    AM_CUDA(cudaStreamSynchronize(st));
+    e->mesh_host = true;
+}
+
 int am_combine_mesh(am_engine *e, double scale, const double *center3)
 {
     if (!e) return AM_ERR_NOT_INITIALIZED;
@@ -1214,33 +1238,21 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
         AM_CUDA(cudaMemcpyAsync(cnt, wb.counts, sizeof(cnt), cudaMemcpyDeviceToHost, st));
         AM_CUDA(cudaStreamSynchronize(st));
         e->check_err();
-        const long long V = cnt[0], F = cnt[1], I = cnt[2];
-        e->mesh_verts.assign((size_t)V * 3, 0.0);
-        e->mesh_fs.assign((size_t)F, 0);
-        e->mesh_fi.assign((size_t)I, 0);
-        if (e->ts == 8) {
-            AM_CUDA(cudaMemcpyAsync(e->mesh_verts.data(), e->w_verts.p, sizeof(double) * 3 * V, cudaMemcpyDeviceToHost, st));
-        } else {
-            std::vector<float> tmp((size_t)V * 3);
-            AM_CUDA(cudaMemcpyAsync(tmp.data(), e->w_verts.p, sizeof(float) * 3 * V, cudaMemcpyDeviceToHost, st));
-            AM_CUDA(cudaStreamSynchronize(st));
-            for (size_t q = 0; q < tmp.size(); ++q) e->mesh_verts[q] = tmp[q];
-        }
-        AM_CUDA(cudaMemcpyAsync(e->mesh_fs.data(), e->w_fs.p, sizeof(int) * F, cudaMemcpyDeviceToHost, st));
-        AM_CUDA(cudaMemcpyAsync(e->mesh_fi.data(), e->w_fi.p, sizeof(int) * I, cudaMemcpyDeviceToHost, st));
-        AM_CUDA(cudaStreamSynchronize(st));
-        e->stats.mesh_num_verts = V;
-        e->stats.mesh_num_faces = F;
-        e->stats.mesh_num_indices = I;
+        e->stats.mesh_num_verts = cnt[0];
+        e->stats.mesh_num_faces = cnt[1];
+        e->stats.mesh_num_indices = cnt[2];
         e->has_mesh = true;
-        // the mesh now lives on the host: large weld buffers go back (many
-        // engines of a batch weld one after the other)
+        e->mesh_host = false; // read back on demand: am_get_mesh copies straight into the caller's arrays
+        // large weld buffers go back (many engines of a batch weld one after
+        // the other): their mesh moves to the host first
         DevBuf *weld[] = {&e->w_table, &e->w_rep, &e->w_flag, &e->w_vidx, &e->w_bsum, &e->w_fflag, &e->w_fsize,
                           &e->w_fid, &e->w_foff, &e->w_verts, &e->w_fs, &e->w_fi};
         size_t held = 0;
         for (DevBuf *b : weld) held += b->bytes;
-        if (held > ((size_t)1 << 30))
+        if (held > ((size_t)1 << 30)) {
+            fetch_mesh(e);
             for (DevBuf *b : weld) b->reset();
+        }
     });
 }
 
@@ -1248,10 +1260,31 @@ int am_get_mesh(am_engine *e, double *verts, int32_t *face_sizes, int32_t *face_
 {
     if (!e) return AM_ERR_NOT_INITIALIZED;
     if (!e->has_mesh) return AM_ERR_NO_RESULT;
-    if (verts) std::copy(e->mesh_verts.begin(), e->mesh_verts.end(), verts);
-    if (face_sizes) std::copy(e->mesh_fs.begin(), e->mesh_fs.end(), face_sizes);
-    if (face_indices) std::copy(e->mesh_fi.begin(), e->mesh_fi.end(), face_indices);
-    return AM_OK;
+    if (e->mesh_host) {
+        if (verts) std::copy(e->mesh_verts.begin(), e->mesh_verts.end(), verts);
+        if (face_sizes) std::copy(e->mesh_fs.begin(), e->mesh_fs.end(), face_sizes);
+        if (face_indices) std::copy(e->mesh_fi.begin(), e->mesh_fi.end(), face_indices);
+        return AM_OK;
+    }
+    return guarded(e, [&] { // from the weld buffers straight into the caller's arrays
+        cudaStream_t st = e->st;
+        const long long V = e->stats.mesh_num_verts, F = e->stats.mesh_num_faces, I = e->stats.mesh_num_indices;
+        std::vector<float> tmp;
+        if (verts && V > 0) {
+            if (e->ts == 8) {
+                AM_CUDA(cudaMemcpyAsync(verts, e->w_verts.p, sizeof(double) * 3 * V, cudaMemcpyDeviceToHost, st));
+            } else {
+                tmp.resize((size_t)V * 3);
+                AM_CUDA(cudaMemcpyAsync(tmp.data(), e->w_verts.p, sizeof(float) * 3 * V, cudaMemcpyDeviceToHost, st));
+            }
+        }
+        if (face_sizes && F > 0)
+            AM_CUDA(cudaMemcpyAsync(face_sizes, e->w_fs.p, sizeof(int) * F, cudaMemcpyDeviceToHost, st));
+        if (face_indices && I > 0)
+            AM_CUDA(cudaMemcpyAsync(face_indices, e->w_fi.p, sizeof(int) * I, cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        for (size_t q = 0; q < tmp.size(); ++q) verts[q] = tmp[q];
+    });
 }
 
 int am_export_mesh(am_engine *e, const char *file_path, int is_polymesh, int is_float32)
@@ -1259,6 +1292,10 @@ int am_export_mesh(am_engine *e, const char *file_path, int is_polymesh, int is_
     if (!e) return AM_ERR_NOT_INITIALIZED;
     if (!e->has_mesh) return AM_ERR_NO_RESULT;
     if (!file_path) return AM_ERR_INVALID_ARGUMENT;
+    if (!e->mesh_host) {
+        const int rc = guarded(e, [&] { fetch_mesh(e); });
+        if (rc != AM_OK) return rc;
+    }
     FILE *f = fopen(file_path, "wb");
     if (!f) {
         e->last_error = std::string("cannot open ") + file_path;

@@ -174,7 +174,7 @@ __device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long 
 template <typename TC>
 struct GroupShared {
     long long rl;   // the group's region (chunk-local)
-    int done, pad;  // the leader's refinement verdict
+    int done, pad;  // the leader's refinement outcome
     TC bt[2][8];    // partial minima per step parity and warp
     int bk[2][8];
 };
@@ -408,7 +408,7 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &
     walk<TC, TC, kGroup>(rows, ALL, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz, fve, fn, fclosed, fst,
                          sbk, sdec, nsteps, g);
     if (fst != kOk || !fclosed || nsteps < 1 || nsteps > 32) return false;
-    if (kGroup && g.gw != 0) return true; // the leader refines; the caller shares its verdict
+    if (kGroup && g.gw != 0) return true; // the leader refines; the caller shares its outcome
 
     // step j's vertex in TS, into lane j
     const int G = lane >> 2, L = lane & 3, gbase = lane & ~3;
@@ -650,7 +650,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             {
                 done = walk_refined<TC, TS, kGroup>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve,
                                                     n, closed, status, g);
-                if (kGroup) { // the leader's verdict for the group
+                if (kGroup) { // the leader's outcome for the group
                     if (g.gw == 0 && lane == 0) g.sh->done = done ? 1 : 0;
                     g.sync();
                     done = g.sh->done != 0;
