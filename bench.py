@@ -86,12 +86,13 @@ def dist_init(args):
 
 def composition_flops(nodes, arc_table, tms):
     """Algorithmic FLOPs of one region's composition: 4 columns x 2 flop per
-    multiply-add over every layer product and transformed skip."""
+    multiply-add over every layer product and every transformed connection
+    (the input's included: 8 (sum n_l n_l+1 + sum n_dst n_src))."""
     macs = sum(nodes[i] * nodes[i + 1] for i in range(1, len(nodes) - 1))
     for row in arc_table:
         for c in range(int(row[0])):
-            src, t = int(row[1 + 2 * c]), int(row[2 + 2 * c])
-            if tms[t].size and src >= 1:
+            t = int(row[2 + 2 * c])
+            if tms[t].size:
                 macs += tms[t].shape[0] * tms[t].shape[1]
     return 8 * macs
 
