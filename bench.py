@@ -84,6 +84,20 @@ def dist_init(args):
     return ws, rank, local
 
 
+def max_over_ranks(value, device="cpu"):
+    """The largest ``value`` over all ranks (the slowest replica's time under
+    torchrun); ``value`` itself in a single process.  ``device`` is where the
+    process group's backend reduces (a CUDA device for NCCL, "cpu" for gloo)."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def composition_flops(nodes, arc_table, tms):
     """Algorithmic FLOPs of one region's composition: 4 columns x 2 flop per
     multiply-add over every layer product and every transformed connection
@@ -176,73 +190,112 @@ def measured_peaks():
         return 6800.0, 1900.0, "fallback"
 
 
-def run_reference(args, rank, ws):
-    """--impl reference: the reference's own loop on the host cores."""
-    if rank != 0:
-        return
-    net, states, points, desc = workload(args.workload, args.seeds)
+def reference_workload(args):
+    """The networks, seeds and per-network region budgets the reference arm
+    marches: the bench's workload, or for ``batched`` the same NETS networks
+    one after the other (the reference re-Inits per architecture,
+    backend/main.py:437-446), the sample split evenly between them."""
+    if args.workload != "batched":
+        net, states, points, desc = workload(args.workload, args.seeds)
+        return [(net, states, points, REF_SAMPLE_REGIONS)], desc
+    from analyticmesh_gb300 import workloads as wl
+
+    items = []
+    budget = max(1024, REF_SAMPLE_REGIONS // max(1, args.nets))
+    for i, m in enumerate(wl.batched(args.nets, 100)):
+        net = wl.net_arrays(m)
+        net.iso = 0.0
+        st, pt = wl.seeds_for(m, init_num=args.seeds, seed=100 + i)
+        items.append((net, st, pt, budget))
+    desc = "%d MLPs, seeds 100..%d, widths {32..512}, depths 2..8, one after the other" % (args.nets, 99 + args.nets)
+    return items, desc
+
+
+def reference_step(items, dtype, threads, kind):
+    """One step of the reference arm: (faces, seconds) over every item,
+    each marched up to its region budget inside the reference's am_time
+    window (the oracle restatement's wall time when the reference build is
+    unavailable)."""
+    from oracle import oracle as O
+
+    faces, secs = 0, 0.0
+    for net, states, points, budget in items:
+        if kind == "reference":
+            tm = {}
+            r = O.run_ref(net, states, points, iso=net.iso, dtype=dtype, threads=threads, region_budget=budget,
+                          timing=tm)
+            secs += tm["am_seconds"]
+        else:
+            t0 = time.perf_counter()
+            r = O.run_oracle(net, states, points, iso=net.iso, dtype=dtype, region_budget=budget)
+            secs += time.perf_counter() - t0
+        faces += int((r.nverts >= 3).sum())
+    return faces, secs
+
+
+def reference_kind():
+    """The cpu_baseline kind: ``reference`` when the reference's own loop is
+    built for the host (or can be built), else ``port`` (the oracle
+    restatement)."""
     from oracle import build_ref
     from oracle import oracle as O
 
-    threads = os.cpu_count() or 1
     try:
         if not O.ref_available():
             build_ref.build_ref()
-        kind = "reference" if O.ref_available() else "port"
+        return "reference" if O.ref_available() else "port"
     except Exception:
-        kind = "port"
+        return "port"
+
+
+def run_reference(args, rank, ws):
+    """--impl reference: the reference's own loop on the host cores.  Under
+    torchrun rank 0 alone runs and prints; the other ranks return."""
+    if rank != 0:
+        return
+    items, desc = reference_workload(args)
+    threads = os.cpu_count() or 1
+    kind = reference_kind()
     dtype = "float64" if args.form == "float64" else "float32"
     rates = []
-    steps_done = 0
+    faces = 0
     for i in range(args.warmup + args.steps):
-        tm = {}
-        if kind == "reference":
-            r = O.run_ref(net, states, points, iso=net.iso, dtype=dtype, threads=threads, region_budget=REF_SAMPLE_REGIONS,
-                          timing=tm)
-            secs = tm["am_seconds"]
-        else:
-            t0 = time.perf_counter()
-            r = O.run_oracle(net, states, points, iso=net.iso, dtype=dtype)
-            secs = time.perf_counter() - t0
-        faces = int((r.nverts >= 3).sum())
+        faces, secs = reference_step(items, dtype, threads, kind)
         if i >= args.warmup:
             rates.append(faces / secs)
-            steps_done += 1
     value = statistics.mean(rates)
+    sample = "first %d regions of %s per step" % (
+        items[0][3], "the workload" if len(items) == 1 else "each network")
     line = {
         "impl": "reference", "metric": "analytic_faces_per_sec", "value": value, "unit": "faces/s",
-        "n_gpus": args.gpus, "steps": steps_done, "warmup": args.warmup, "ms_per_step": 1e3 * faces / value,
+        "n_gpus": args.gpus, "steps": len(rates), "warmup": args.warmup, "ms_per_step": 1e3 * faces / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dtype == "float32" else "f64",
         "data": "synthetic (seeded network and dichotomy seeds)",
-        "config": {"workload": desc, "seeds": args.seeds, "sample": "first %d regions per step" % REF_SAMPLE_REGIONS},
+        "config": {"workload": desc, "seeds": args.seeds, "sample": sample},
         "cpu_baseline": {"value": value, "unit": "faces/s", "cores": threads, "kind": kind,
-                         "sample": "first %d regions of the workload per step, reference loop built for the host "
-                                   "(OpenMP, %d threads)" % (REF_SAMPLE_REGIONS, threads)},
+                         "sample": "%s, %s (OpenMP, %d threads)" % (
+                             sample, "reference loop built for the host" if kind == "reference"
+                             else "oracle restatement", threads)},
         "e2e": {"value": value, "unit": "faces/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 def cpu_baseline(net, states, points, dtype):
-    from oracle import build_ref
-    from oracle import oracle as O
-
+    """The cpu_baseline object of the bench line: the reference's loop built
+    for the host (all threads) on the first REF_SAMPLE_REGIONS regions of the
+    workload, or the oracle restatement on the same sample."""
     threads = os.cpu_count() or 1
+    kind = reference_kind()
     try:
-        if not O.ref_available():
-            build_ref.build_ref()
-        tm = {}
-        r = O.run_ref(net, states, points, iso=net.iso, dtype=dtype, threads=threads, region_budget=REF_SAMPLE_REGIONS,
-                      timing=tm)
-        return {"value": float((r.nverts >= 3).sum()) / tm["am_seconds"], "unit": "faces/s", "cores": threads,
-                "kind": "reference", "sample": "first %d regions of the workload (reference loop built for the host, "
-                                                "OpenMP %d threads)" % (REF_SAMPLE_REGIONS, threads)}
-    except Exception as exc:
-        t0 = time.perf_counter()
-        r = O.run_oracle(net, states, points, iso=net.iso, dtype=dtype)
-        secs = time.perf_counter() - t0
-        return {"value": float((r.nverts >= 3).sum()) / secs, "unit": "faces/s", "cores": threads, "kind": "port",
-                "sample": "full workload, oracle restatement (%s)" % type(exc).__name__}
+        faces, secs = reference_step([(net, states, points, REF_SAMPLE_REGIONS)], dtype, threads, kind)
+    except Exception:  # a reference build that loads but cannot run: the restatement instead
+        kind = "port"
+        faces, secs = reference_step([(net, states, points, REF_SAMPLE_REGIONS)], dtype, threads, kind)
+    return {"value": faces / secs, "unit": "faces/s", "cores": threads, "kind": kind,
+            "sample": "first %d regions of the workload, %s (OpenMP, %d threads)" % (
+                REF_SAMPLE_REGIONS, "reference loop built for the host" if kind == "reference"
+                else "oracle restatement", threads)}
 
 
 def bench_batched(args, ws, rank, local):
@@ -281,6 +334,9 @@ def bench_batched(args, ws, rank, local):
              for e, n, s_, p_ in zip(chosen, dnets, sts, pts)]
     for _ in range(args.warmup):
         engine.run_batch(chosen, dnets, sts, pts)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
     times, faces = [], 0
     with Clocks(local) as clk:
         for _ in range(args.steps):
@@ -289,7 +345,8 @@ def bench_batched(args, ws, rank, local):
             wall = engine.run_batch(chosen, dnets, sts, pts)
             times.append(wall / 1e3)
             faces = sum(e.stats()["num_faces"] for e in chosen)
-    value = ws * faces / (sum(times) / len(times))
+    step_s = max_over_ranks(sum(times) / len(times), dev)
+    value = ws * faces / step_s
     clocks = clk.summary()
     regions = [e.stats()["num_regions"] for e in chosen]
 
@@ -328,7 +385,7 @@ def bench_batched(args, ws, rank, local):
         return
     line = {
         "metric": "analytic_faces_per_sec", "value": value, "unit": "faces/s", "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times), "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (bf16x3 composition, f64 solves)",
         "data": "synthetic (seeded networks and dichotomy seed points)",
         "config": {"workload": "%d MLPs, seeds 100..%d, widths {32..512}, depths 2..8, all marched at once"
@@ -406,11 +463,8 @@ def main():
                               "profile": True, "steps": args.steps, "launches": launches}), flush=True)
         eng.close()
         return
-    total = sum(times)
+    total = max_over_ranks(sum(times), dev)
     if ws > 1:
-        t = torch.tensor([total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total = float(t.item())
         torch.distributed.barrier()
     value = ws * sum(faces) / total
     clocks = clk.summary()

@@ -24,6 +24,13 @@ struct amo_result {
     int *mfaces;
 };
 
+/* Region budget for timed samples: 0 = none; otherwise the loop stops at the
+ * end of the first batch after which this many regions have been recorded
+ * (the same point as the hook of the reference's CPU build). */
+static long g_region_budget = 0;
+
+void amo_set_region_budget(long regions) { g_region_budget = regions > 0 ? regions : 0; }
+
 /* FNV-1a (hash1) and FNV-1 (hash2), 32-bit, backend/src/states.cu:11-26 */
 uint32_t amo_fnv1a(const uint8_t *data, int n)
 {

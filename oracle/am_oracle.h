@@ -88,6 +88,10 @@ void amo_get_mesh(const amo_result *r, double *verts, int *faces);
 
 void amo_free(amo_result *r);
 
+/* Timed samples: stop the marching loop at the end of the first batch after
+ * which `regions` regions have been recorded (0 = run to completion). */
+void amo_set_region_budget(long regions);
+
 /* FNV helpers (states.cu:11-26), exported for tests. */
 uint32_t amo_fnv1a(const uint8_t *data, int n);
 uint32_t amo_fnv1(const uint8_t *data, int n);

@@ -759,6 +759,7 @@ static int FN(run)(const amo_net *net, const uint8_t *states, const REAL *points
                     }
                 }
             }
+            if (g_region_budget > 0 && res->num >= g_region_budget) break;
         }
         free(bb_bits); free(bb_mid); free(sys); free(xs); free(ib); free(child);
         free(bt.w_in); free(bt.b_in); free(bt.weq); free(bt.idx); free(bt.start); free(bt.vert); free(bt.tab);

@@ -71,6 +71,7 @@ def oracle_lib():
         lib.amo_get_regions.argtypes = [C.c_void_p] + [C.c_void_p] * 7
         lib.amo_get_mesh.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         lib.amo_free.argtypes = [C.c_void_p]
+        lib.amo_set_region_budget.argtypes = [C.c_long]
         _ORACLE = lib
     return _ORACLE
 
@@ -143,8 +144,11 @@ def _ptrs(d):
     return [d[k].ctypes.data for k in ("bits", "nverts", "verts", "ntab", "tab", "mid", "start")]
 
 
-def run_oracle(net, states, points, iso=0.0, flip=False, dtype="float32", output_skips=False, combine=None):
-    """Run the restatement.  ``combine=(scale, center)`` also welds the mesh."""
+def run_oracle(net, states, points, iso=0.0, flip=False, dtype="float32", output_skips=False, combine=None,
+               region_budget=0):
+    """Run the restatement.  ``combine=(scale, center)`` also welds the mesh.
+    ``region_budget`` stops the loop at the end of the first batch that
+    reaches that many regions (timed samples; 0 = run to completion)."""
     lib = oracle_lib()
     p = _Packed(net, dtype)
     st, pt = _inputs(states, points, p.npt)
@@ -154,8 +158,12 @@ def run_oracle(net, states, points, iso=0.0, flip=False, dtype="float32", output
                   1 if output_skips else 0)
     res = C.c_void_p()
     fn = lib.amo_run_f64 if dtype == "float64" else lib.amo_run_f32
-    rc = fn(C.byref(cn), st.ctypes.data_as(C.c_void_p), pt.ctypes.data_as(C.c_void_p), st.shape[0], C.c_double(iso),
-            1 if flip else 0, C.byref(res))
+    lib.amo_set_region_budget(int(region_budget))
+    try:
+        rc = fn(C.byref(cn), st.ctypes.data_as(C.c_void_p), pt.ctypes.data_as(C.c_void_p), st.shape[0],
+                C.c_double(iso), 1 if flip else 0, C.byref(res))
+    finally:
+        lib.amo_set_region_budget(0)
     if rc != 0:
         raise RuntimeError("oracle run failed: %d" % rc)
     try:
