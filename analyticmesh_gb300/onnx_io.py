@@ -261,17 +261,124 @@ def _graph_bytes(model: MLP) -> bytes:
     return g
 
 
-def model_bytes(model: MLP) -> bytes:
-    """The ONNX ModelProto of ``model`` (ir_version 8, opset 17)."""
+def _is_relu(n) -> bool:
+    import torch.nn.functional as F
+
+    if n.op == "call_function":
+        return n.target in (torch.relu, F.relu, torch.relu_)
+    if n.op == "call_method":
+        return n.target in ("relu", "relu_")
+    return False
+
+
+def _is_add(n) -> bool:
+    import operator
+
+    if n.op == "call_function":
+        return n.target in (operator.add, operator.iadd, torch.add)
+    return n.op == "call_method" and n.target in ("add", "add_")
+
+
+def _traced_graph_bytes(module: torch.nn.Module) -> bytes:
+    """The ONNX graph of any torch module whose forward is a ReLU MLP:
+    ``nn.Linear`` layers, ReLUs after the hidden ones, and additive skip
+    connections (an identity, or a bias-free ``nn.Linear`` transform of an
+    earlier layer's output).  The reference exports such a module with
+    ``torch.onnx.export`` (backend/onnx_io.py:255-258; examples/2_polytope.py
+    saves a hand-written module that way); here the forward is traced with
+    ``torch.fx`` and written in the node forms ``load_model`` reads back:
+    ``Gemm`` per layer, ``Relu``, ``Add``, ``MatMul`` by the transposed
+    transform."""
+    import torch.fx as fx
+
+    try:
+        gm = fx.symbolic_trace(module)
+    except Exception as exc:
+        raise ValueError("save_model: the module's forward cannot be traced (%s)" % exc) from exc
+    nodes = list(gm.graph.nodes)
+    placeholders = [n for n in nodes if n.op == "placeholder"]
+    outs = [n for n in nodes if n.op == "output"]
+    if len(placeholders) != 1 or len(outs) != 1 or not isinstance(outs[0].args[0], fx.Node):
+        raise ValueError("save_model: expected a module with one input tensor and one output tensor")
+    result = outs[0].args[0]
+
+    def linear_of(n):
+        if n.op == "call_module":
+            mod = gm.get_submodule(n.target)
+            if isinstance(mod, torch.nn.Linear):
+                return mod
+        return None
+
+    def is_main(n):
+        lin = linear_of(n)
+        return (lin is not None and lin.bias is not None) or _is_add(n)
+
+    def is_transform(n):
+        # a bias-free linear added onto the main path: a skip transform
+        lin = linear_of(n)
+        if lin is None or lin.bias is not None or len(n.users) != 1:
+            return False
+        user = next(iter(n.users))
+        return _is_add(user) and any(is_main(a) for a in user.args if isinstance(a, fx.Node) and a is not n)
+
+    name = {placeholders[0]: "input"}
+    body, inits = [], []
+    for n in nodes:
+        if n.op in ("placeholder", "output"):
+            continue
+        out = "output" if n is result else n.name
+        args = [a for a in n.args if isinstance(a, fx.Node)]
+        lin = linear_of(n)
+        if lin is not None:
+            if len(args) != 1:
+                raise ValueError("save_model: unsupported call of %s" % n.target)
+            W = lin.weight.detach().cpu().float().numpy()
+            if is_transform(n):
+                inits.append(_tensor(n.name + ".weight_t", W.T))
+                body.append(_node("MatMul", [name[args[0]], n.name + ".weight_t"], [out], n.name))
+            else:
+                b = lin.bias.detach().cpu().float().numpy() if lin.bias is not None else np.zeros(W.shape[0], np.float32)
+                inits.append(_tensor(n.name + ".weight", W))
+                inits.append(_tensor(n.name + ".bias", b))
+                body.append(_node("Gemm", [name[args[0]], n.name + ".weight", n.name + ".bias"], [out], n.name,
+                                  _attr_float("alpha", 1.0) + _attr_float("beta", 1.0) + _attr_int("transB", 1)))
+        elif _is_relu(n) or (n.op == "call_module" and isinstance(gm.get_submodule(n.target), torch.nn.ReLU)):
+            if len(args) != 1:
+                raise ValueError("save_model: unsupported call of %s" % n.target)
+            body.append(_node("Relu", [name[args[0]]], [out], n.name))
+        elif _is_add(n):
+            if len(args) != 2 or len(n.args) != 2 or n.kwargs:
+                raise ValueError("save_model: only two-operand additions are supported")
+            body.append(_node("Add", [name[args[0]], name[args[1]]], [out], n.name))
+        else:
+            raise ValueError("save_model: unsupported operation %s %s (a ReLU MLP uses nn.Linear, ReLU and "
+                             "additions only)" % (n.op, n.target))
+        name[n] = out
+    if not body:
+        raise ValueError("save_model: the module computes nothing")
+    g = b"".join(_f_bytes(1, nb) for nb in body)
+    g += _f_str(2, "analytic_mlp")
+    g += b"".join(_f_bytes(5, t) for t in inits)
+    g += _f_bytes(11, _value_info("input", (1, 3)))
+    g += _f_bytes(12, _value_info("output", (1, 1)))
+    return g
+
+
+def model_bytes(model: torch.nn.Module) -> bytes:
+    """The ONNX ModelProto of ``model`` (ir_version 8, opset 17): an ``MLP``,
+    or any module whose forward is a ReLU MLP of ``nn.Linear`` layers."""
+    graph = _graph_bytes(model) if isinstance(model, MLP) else _traced_graph_bytes(model)
     m = _f_int(1, 8)                                        # ir_version
     m += _f_str(2, "analyticmesh_gb300")                    # producer_name
-    m += _f_bytes(7, _graph_bytes(model))                   # graph
+    m += _f_bytes(7, graph)                                 # graph
     m += _f_bytes(8, _f_str(1, "") + _f_int(2, 17))         # opset_import
     return m
 
 
-def save_model(model: MLP, model_path: str) -> None:
-    """Write ``model`` as an ONNX file (backend/onnx_io.py:255-258)."""
+def save_model(model: torch.nn.Module, model_path: str) -> None:
+    """Write ``model`` as an ONNX file (backend/onnx_io.py:255-258): an
+    ``MLP``, or any module whose forward is a ReLU MLP (``nn.Linear`` layers,
+    ReLU, additive skips), as the reference's examples save them."""
     with open(model_path, "wb") as fh:
         fh.write(model_bytes(model))
 

@@ -71,3 +71,78 @@ def test_reference_chair_network():
     x = torch.rand(512, 3, generator=g)
     with torch.no_grad():
         assert torch.equal(m(x), m2(x))
+
+
+class _TwoLayer(torch.nn.Module):
+    """A hand-written ReLU network, saved the way the reference's examples
+    save theirs (any module, not only MLP)."""
+
+    def __init__(self, width=14):
+        super().__init__()
+        g = torch.Generator().manual_seed(5)
+        self.first = torch.nn.Linear(3, width)
+        self.second = torch.nn.Linear(width, 1)
+        with torch.no_grad():
+            for p in self.parameters():
+                p.copy_(torch.randn(p.shape, generator=g))
+
+    def forward(self, x):
+        return self.second(torch.relu(self.first(x)))
+
+
+class _Skipped(torch.nn.Module):
+    """Identity skip between hidden layers and a bias-free transform of the
+    input added before the third layer's ReLU."""
+
+    def __init__(self):
+        super().__init__()
+        g = torch.Generator().manual_seed(6)
+        self.a = torch.nn.Linear(3, 24)
+        self.b = torch.nn.Linear(24, 24)
+        self.c = torch.nn.Linear(24, 16)
+        self.t = torch.nn.Linear(3, 16, bias=False)
+        self.out = torch.nn.Linear(16, 1)
+        with torch.no_grad():
+            for p in self.parameters():
+                p.copy_(torch.randn(p.shape, generator=g) * 0.5)
+
+    def forward(self, x):
+        h1 = torch.nn.functional.relu(self.a(x))
+        h2 = (self.b(h1) + h1).relu()
+        h3 = torch.relu(self.c(h2) + self.t(x))
+        return self.out(h3)
+
+
+@pytest.mark.parametrize("factory", [
+    _TwoLayer,
+    lambda: torch.nn.Sequential(torch.nn.Linear(3, 32), torch.nn.ReLU(), torch.nn.Linear(32, 32), torch.nn.ReLU(),
+                                torch.nn.Linear(32, 1)),
+    _Skipped,
+], ids=["hand_written", "sequential", "skips_and_transform"])
+def test_any_relu_module_saves_and_loads_as_mlp(tmp_path, factory):
+    torch.manual_seed(0)
+    m = factory().eval()
+    path = str(tmp_path / "net.onnx")
+    save_model(m, path)
+    mlp = load_model(path)
+    x = torch.randn(512, 3, generator=torch.Generator().manual_seed(1))
+    with torch.no_grad():
+        want, got = m(x), mlp(x)
+    assert got.shape == want.shape
+    assert torch.allclose(got, want, rtol=1e-6, atol=1e-6), (got - want).abs().max()
+    if factory is _Skipped:
+        assert mlp.nodes == [3, 24, 24, 16, 1]
+        assert mlp.arc_table == [[1, 1, 0], [1, 0, 1], [0]] and mlp.arc_tm_shape == [[0, 0], [16, 3]]
+
+
+def test_save_model_rejects_non_mlp_modules(tmp_path):
+    class Smooth(torch.nn.Module):
+        def __init__(self):
+            super().__init__()
+            self.l = torch.nn.Linear(3, 1)
+
+        def forward(self, x):
+            return torch.sigmoid(self.l(x))
+
+    with pytest.raises(ValueError):
+        save_model(Smooth(), str(tmp_path / "s.onnx"))
