@@ -1,0 +1,74 @@
+"""The package's public entry point ``AnalyticMarching(model, ...)`` (the
+reference's backend/main.py:335-559) on the GPU, used the way the reference's
+examples use it: a network built with ``MLP(...)`` or loaded with
+``load_model``, marched, its mesh returned and written as a PLY; and the
+voxel mode (backend/main.py:475-556)."""
+import numpy as np
+import pytest
+import torch
+
+from analyticmesh_gb300 import MLP, AnalyticMarching, load_model, save_model, workloads as wl
+from analyticmesh_gb300.main import read_ply
+
+pytestmark = pytest.mark.gpu
+
+# |f(v)| bounds per form: FP64 vertices, and the gate of the FP32-input forms
+F_TOL = {torch.float64: 1e-9, "mixed": 1e-5, torch.float32: 1e-5}
+
+
+def _f64(net, pts):
+    """FP64 forward pass of a plain MLP (no skips) at pts (n, 3)."""
+    x = np.asarray(pts, np.float64)
+    n_lin = len(net.W)
+    for i in range(n_lin):
+        x = x @ net.W[i].T + net.b[i]
+        if i < n_lin - 1:
+            x = np.maximum(x, 0.0)
+    return x[:, 0]
+
+
+def _check_mesh(verts, faces):
+    verts = np.asarray(verts)
+    assert verts.ndim == 2 and verts.shape[1] == 3 and len(faces) > 0
+    assert all(len(f) >= 3 for f in faces)
+    idx = np.concatenate([np.asarray(f) for f in faces])
+    assert idx.min() >= 0 and idx.max() < len(verts)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, "mixed"], ids=["float64", "mixed"])
+def test_saved_and_loaded_network_marches_and_writes_its_mesh(tmp_path, dtype):
+    torch.manual_seed(3)
+    model = MLP(nodes=[3, 48, 48, 1], arc_table=[[0]] * 2, arc_tm_shape=[], geometric_radius=0.5,
+                enable_print=False)
+    onnx_path = str(tmp_path / "sphere.onnx")
+    save_model(model, onnx_path)
+    loaded = load_model(onnx_path)
+    net = wl.net_arrays(loaded)  # float64 copies of the float32 parameters
+    ply = str(tmp_path / "sphere.ply")
+    out = AnalyticMarching(loaded, ply, dtype=dtype, generator=torch.Generator().manual_seed(4))
+    for key in ("init_point_time", "init_cuda_time", "am_time", "export_time", "vertices", "faces", "stats"):
+        assert key in out
+    verts, faces = np.asarray(out["vertices"]), out["faces"]
+    _check_mesh(verts, faces)
+    assert len(faces) == out["stats"]["num_faces"]
+    assert np.abs(_f64(net, verts)).max() <= F_TOL[dtype]
+    # the PLY holds the returned mesh (float32 vertices, polygons)
+    pv, pf = read_ply(ply)
+    assert pv.shape == verts.shape
+    np.testing.assert_allclose(pv, verts, rtol=0, atol=1e-6)
+    assert [list(map(int, f)) for f in pf] == [list(map(int, f)) for f in faces]
+
+
+def test_voxel_mode_meshes_on_the_level_set():
+    model = wl.geometric([32, 32], 7)
+    net = wl.net_arrays(model)
+    out = AnalyticMarching(model, None, dtype=torch.float64, voxel_configs={"voxel_size": 0.25},
+                           generator=torch.Generator().manual_seed(2))
+    verts, faces = np.asarray(out["vertices"]), out["faces"]
+    _check_mesh(verts, faces)
+    assert np.abs(_f64(net, verts)).max() <= F_TOL[torch.float64]
+    # every vertex lies on the surface of the unvoxelised network, which a
+    # whole marching of the same network covers: the same bounding box
+    whole = AnalyticMarching(model, None, dtype=torch.float64, generator=torch.Generator().manual_seed(2))
+    wv = np.asarray(whole["vertices"])
+    assert np.all(verts.min(0) >= wv.min(0) - 1e-9) and np.all(verts.max(0) <= wv.max(0) + 1e-9)
