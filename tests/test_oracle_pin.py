@@ -69,3 +69,29 @@ def test_oracle_matches_reference_live(factory, dtype):
     rr, mr = O.run_ref(net, st, pt, dtype=dtype, combine=(2.0, [0.1, -0.2, 0.3]))
     assert CM.exact_records(ro, rr) == []
     assert CM.exact_mesh(mo, mr)
+
+
+def test_oracle_seed_independence_and_deduplication():
+    """A connected surface: one seed reaches every region; seeds given three
+    times in shuffled order keep one of each state."""
+    m = wl.geometric([32, 32], 7)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=11)
+    full = O.run_oracle(net, st, pt)
+    one = O.run_oracle(net, st[:1], pt[:1])
+    idx = np.random.default_rng(0).permutation(np.concatenate([np.arange(len(st))] * 3))
+    dup = O.run_oracle(net, st[idx], pt[idx])
+    keys = lambda r: set(map(bytes, r.bits))
+    assert keys(one) == keys(full) == keys(dup)
+    assert dup.seeds_kept == full.seeds_kept == len(np.unique(st, axis=0))
+
+
+@_live
+def test_oracle_matches_reference_live_on_repeated_seeds():
+    m = wl.geometric([24, 24], 21)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=64, seed=2)
+    idx = np.random.default_rng(1).permutation(np.concatenate([np.arange(len(st))] * 2))
+    ro = O.run_oracle(net, st[idx], pt[idx])
+    rr = O.run_ref(net, st[idx], pt[idx])
+    assert CM.exact_records(ro, rr) == []
