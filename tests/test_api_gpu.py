@@ -72,3 +72,22 @@ def test_voxel_mode_meshes_on_the_level_set():
     whole = AnalyticMarching(model, None, dtype=torch.float64, generator=torch.Generator().manual_seed(2))
     wv = np.asarray(whole["vertices"])
     assert np.all(verts.min(0) >= wv.min(0) - 1e-9) and np.all(verts.max(0) <= wv.max(0) + 1e-9)
+
+
+def test_export_triangles_and_double_vertices(tmp_path):
+    """ExportMesh's other layouts (backend/inc/polymesh.h:350-423): triangle
+    fans instead of polygons, float64 instead of float32 vertices."""
+    from analyticmesh_gb300 import engine
+
+    m = wl.geometric([32, 32], 7)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=11)
+    eng = engine.march(net, st, pt, "float64")
+    mesh = eng.combine(scale=2.0, center=(0.5, 0.0, -1.0))
+    path = str(tmp_path / "tri.ply")
+    eng.export(path, is_polymesh=False, is_float32=False)
+    pv, pf = read_ply(path)
+    assert pv.dtype == np.float64 and np.array_equal(pv, mesh.verts)
+    fans = [[int(f[0]), int(f[j + 1]), int(f[j + 2])] for f in mesh.faces for j in range(len(f) - 2)]
+    assert [list(map(int, f)) for f in pf] == fans
+    eng.close()

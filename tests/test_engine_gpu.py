@@ -297,3 +297,39 @@ def test_autotune_chooses_options_and_keeps_results():
     again = engine.Engine("mixed", net.nodes, net.arc_table, 0)
     assert engine.autotune(again, net, st, pt, sample_regions=3000) == (tile, warps)
     again.close()
+
+
+def _outward_fraction(mesh):
+    """Share of faces whose right-hand normal points away from the origin
+    (the sphere-like surfaces here enclose it)."""
+    V = mesh.verts
+    dots = []
+    for f in mesh.faces:
+        P = V[f]
+        c = P.mean(0)
+        n = np.cross(P - c, np.roll(P, -1, 0) - c).sum(0)
+        dots.append(n @ c)
+    return float((np.array(dots) > 0).mean())
+
+
+@pytest.mark.parametrize("form", ["float32", "mixed"])
+def test_face_orientation_and_flip_insideout(form):
+    """Faces run counter-clockwise about the gradient, so their normals point
+    outward as the reference orients them (correctNormalDirection,
+    kernel.h:1325-1385); flip_insideout reverses every face."""
+    m = wl.geometric([32, 32], 7)
+    net = wl.net_arrays(m)
+    st, pt = wl.seeds_for(m, init_num=128, seed=11)
+    meshes = {}
+    for flip in (False, True):
+        eng = engine.march(net, st, pt, form, flip_insideout=flip)
+        meshes[flip] = eng.combine()
+        frac = _outward_fraction(meshes[flip])
+        assert (frac > 0.999) if not flip else (frac < 0.001), (flip, frac)
+        eng.close()
+    a, b = meshes[False], meshes[True]
+    # faces come in region order: face i of the flipped mesh is face i reversed
+    assert len(a.faces) == len(b.faces)
+    for fa, fb in zip(a.faces, b.faces):
+        assert len(fa) == len(fb)
+        np.testing.assert_allclose(a.verts[fa[::-1]], b.verts[fb], rtol=0, atol=1e-6)

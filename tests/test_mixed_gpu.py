@@ -62,3 +62,29 @@ def test_mixed_sphere_config():
     assert np.abs(f_at(net, v)).max() <= 1e-5
     em.close()
     ep.close()
+
+
+@pytest.mark.parametrize("name", ["extra_16x2_f32", "iso_16x2_f32"])
+def test_mixed_with_extra_constraints_and_iso(name):
+    """The mixed form with the reference's extra half-space constraints (a box
+    clip) and a non-zero level, on the golden fixtures' networks and seeds."""
+    from golden_io import load
+
+    g = load(name)
+    net, st, pt, iso = g["net"], g["states"], g["points"], g["iso"]
+    eng = engine.march(net, st, pt, "mixed", iso=iso)
+    reg = eng.regions()
+    o64 = O.run_oracle(net, st, pt, iso=iso, dtype="float64")
+    o32 = O.run_oracle(net, st, pt, iso=iso, dtype="float32")
+    ce = CM.parity_report(reg, o64, tol=1e-5)
+    co = CM.parity_report(o32, o64, tol=1e-5)
+    d_mixed = ce["regions_only_a"] + ce["regions_only_b"]
+    d_fp32 = co["regions_only_a"] + co["regions_only_b"]
+    assert d_mixed <= 2 * d_fp32 + 2, (ce, co)
+    assert ce["faces_count_mismatch"] <= 2 * co["faces_count_mismatch"] + 2, (ce, co)
+    v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in range(reg.num) if reg.nverts[i] >= 3])
+    assert np.abs(f_at(net, v) - iso).max() <= 1e-5
+    if net.num_extra:
+        # every vertex inside the clip box (w . v + b <= 0 up to rounding)
+        assert (v @ net.w_extra.T + net.b_extra).max() <= 1e-5
+    eng.close()
