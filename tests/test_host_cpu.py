@@ -40,6 +40,19 @@ def test_init_validates_like_the_reference():
     bad = np.array([2, 16, 1], np.int32)
     assert L.am_init(C.byref(h), b"float32", bad.ctypes.data_as(i32), 3, arc.ctypes.data_as(i32), 1, 1, 0) == 1
     assert L.am_init(C.byref(h), b"float32", nodes.ctypes.data_as(i32), 3, arc.ctypes.data_as(i32), 1, 2, 0) == 1
+    # a zero-width hidden layer, a negative extra-constraint count, a skip from a
+    # later layer, a row with more connections than columns: all rejected
+    # before anything touches a device
+    zero = np.array([3, 16, 0, 1], np.int32)
+    arc2 = np.zeros((2, 1), np.int32)
+    assert L.am_init(C.byref(h), b"float32", zero.ctypes.data_as(i32), 4, arc2.ctypes.data_as(i32), 2, 1, 0) == 1
+    assert L.am_init(C.byref(h), b"float32", nodes.ctypes.data_as(i32), 3, arc.ctypes.data_as(i32), 1, 1, -1) == 1
+    deep = np.array([3, 16, 16, 1], np.int32)
+    later = np.array([[0, 0, 0], [1, 3, 0]], np.int32)  # into linear 2 from hidden layer 3
+    assert L.am_init(C.byref(h), b"float32", deep.ctypes.data_as(i32), 4, later.ctypes.data_as(i32), 2, 3, 0) == 1
+    crowded = np.array([[0, 0, 0], [2, 1, 0]], np.int32)  # two connections, room for one
+    assert L.am_init(C.byref(h), b"float32", deep.ctypes.data_as(i32), 4, crowded.ctypes.data_as(i32), 2, 3, 0) == 1
+    assert not h.value
 
 
 def test_cuam_rejects_bad_arguments():
