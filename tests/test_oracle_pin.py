@@ -95,3 +95,15 @@ def test_oracle_matches_reference_live_on_repeated_seeds():
     ro = O.run_oracle(net, st[idx], pt[idx])
     rr = O.run_ref(net, st[idx], pt[idx])
     assert CM.exact_records(ro, rr) == []
+
+
+@_live
+@pytest.mark.parametrize("name", names())
+def test_golden_fixtures_are_the_references_output(name):
+    """Provenance of the committed fixtures: the reference's own loop, run
+    again on each fixture's inputs, gives its records and mesh bit for bit."""
+    g = load(name)
+    regions, mesh = O.run_ref(g["net"], g["states"], g["points"], iso=g["iso"], flip=g["flip"], dtype=g["dtype"],
+                              combine=(1.0, [0.0, 0.0, 0.0]))
+    assert CM.exact_records(regions, g["regions"]) == []
+    assert CM.exact_mesh(mesh, g["mesh"])
