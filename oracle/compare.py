@@ -62,6 +62,26 @@ def _key(bits_row):
     return bits_row.tobytes()
 
 
+def _row_keys(bits):
+    """One opaque (void) value per region: its packed activation bits."""
+    b = np.ascontiguousarray(bits)
+    width = max(1, b.shape[1] * b.itemsize) if b.ndim == 2 else 1
+    if b.ndim != 2 or b.shape[0] == 0 or b.shape[1] == 0:
+        return np.zeros(b.shape[0] if b.ndim else 0, dtype=np.dtype((np.void, width)))
+    return b.view(np.dtype((np.void, width))).ravel()
+
+
+def _last_of_each(keys, mask):
+    """Indices of the rows selected by ``mask``, one per distinct key (the
+    last occurrence, as a dict built in row order keeps), in key order."""
+    idx = np.nonzero(mask)[0]
+    if idx.size == 0:
+        return idx
+    rev = idx[::-1]
+    _, first = np.unique(keys[rev], return_index=True)
+    return rev[first]
+
+
 @dataclasses.dataclass
 class Polygons:
     """region key -> (V, 3) polygon, plus the key order."""
@@ -93,34 +113,68 @@ def cycle_distance(p, q):
     return best
 
 
+def _cycle_distances(P, Q):
+    """cycle_distance for m pairs of n-vertex cycles at once: P, Q (m, n, 3)."""
+    n = P.shape[1]
+    best = np.full(P.shape[0], np.inf)
+    with np.errstate(invalid="ignore"):
+        for cand in (Q, Q[:, ::-1]):
+            for s in range(n):
+                d = np.abs(P - np.roll(cand, -s, axis=1)).max(axis=(1, 2))
+                best = np.where(d < best, d, best)  # a NaN distance never wins, as in cycle_distance
+    return best
+
+
+def _matched(a, b, min_verts):
+    """Polygons of both runs (regions with >= min_verts vertices, one per
+    key) and the pairs with the same key: (sel_a, sel_b, ra, rb)."""
+    ka, kb = _row_keys(a.bits), _row_keys(b.bits)
+    sa = _last_of_each(ka, np.asarray(a.nverts) >= min_verts)
+    sb = _last_of_each(kb, np.asarray(b.nverts) >= min_verts)
+    _, ia, ib = np.intersect1d(ka[sa], kb[sb], assume_unique=True, return_indices=True)
+    return sa, sb, sa[ia], sb[ib]
+
+
+def _pair_distances(a, b, ra, rb):
+    """cycle_distance of every matched pair (inf where the vertex counts differ)."""
+    na = np.asarray(a.nverts)[ra].astype(np.int64)
+    nb = np.asarray(b.nverts)[rb].astype(np.int64)
+    d = np.full(ra.size, np.inf)
+    for n in np.unique(na[na == nb]):
+        m = (na == n) & (nb == n)
+        d[m] = _cycle_distances(np.asarray(a.verts[ra[m], :n], dtype=np.float64),
+                                np.asarray(b.verts[rb[m], :n], dtype=np.float64))
+    return d, na != nb
+
+
+def _key_sets(a, b):
+    ua, ub = np.unique(_row_keys(a.bits)), np.unique(_row_keys(b.bits))
+    return (ua.size, ub.size, np.setdiff1d(ua, ub, assume_unique=True).size,
+            np.setdiff1d(ub, ua, assume_unique=True).size)
+
+
 def canonical(a_regions, b_regions, tol=1e-5):
     """Order-free comparison.  Returns a dict of counts."""
-    ka = {_key(x) for x in a_regions.bits}
-    kb = {_key(x) for x in b_regions.bits}
-    pa = Polygons.from_regions(a_regions).faces
-    pb = Polygons.from_regions(b_regions).faces
-    common = set(pa) & set(pb)
-    worst = 0.0
-    bad = 0
-    for k in common:
-        d = cycle_distance(pa[k], pb[k])
-        worst = max(worst, d)
-        if d > tol:
-            bad += 1
-    return dict(regions_a=len(ka), regions_b=len(kb), only_a=len(ka - kb), only_b=len(kb - ka),
-                faces_a=len(pa), faces_b=len(pb), faces_only_a=len(set(pa) - set(pb)),
-                faces_only_b=len(set(pb) - set(pa)), faces_mismatch=bad, max_vertex_diff=worst)
+    na_, nb_, only_a, only_b = _key_sets(a_regions, b_regions)
+    sa, sb, ra, rb = _matched(a_regions, b_regions, 3)
+    d, _ = _pair_distances(a_regions, b_regions, ra, rb)
+    return dict(regions_a=na_, regions_b=nb_, only_a=only_a, only_b=only_b,
+                faces_a=int(sa.size), faces_b=int(sb.size), faces_only_a=int(sa.size - ra.size),
+                faces_only_b=int(sb.size - rb.size), faces_mismatch=int((d > tol).sum()),
+                max_vertex_diff=float(d.max()) if d.size else 0.0)
 
 
 def clean_walks(r):
     """Mask of oracle / reference records whose walk closed without a
     rejected pivot or merge (tab = [s, ..., s], no negative entries)."""
-    ok = np.zeros(r.num, bool)
-    for i in range(r.num):
-        nt = int(r.ntab[i])
-        t = r.tab[i, :nt]
-        ok[i] = nt >= 4 and t[0] == t[nt - 1] and (t >= 0).all()
-    return ok
+    nt = np.asarray(r.ntab).astype(np.int64)
+    tab = np.asarray(r.tab)
+    if nt.size == 0:
+        return np.zeros(0, bool)
+    cols = np.arange(tab.shape[1])[None, :]
+    negative = ((tab < 0) & (cols < nt[:, None])).any(1)
+    last = tab[np.arange(nt.size), np.clip(nt - 1, 0, tab.shape[1] - 1)]
+    return (nt >= 4) & (tab[:, 0] == last) & ~negative
 
 
 def parity_report(a, b, tol=1e-5):
@@ -131,24 +185,13 @@ def parity_report(a, b, tol=1e-5):
     vertex counts (combinatorial disagreement); faces_beyond_tol: same
     count but some vertex further than tol after the best rotation /
     orientation; max_diff over all common faces of equal size."""
-    ka = {x.tobytes() for x in a.bits}
-    kb = {x.tobytes() for x in b.bits}
-    pa = Polygons.from_regions(a, min_verts=1).faces
-    pb = Polygons.from_regions(b, min_verts=1).faces
-    common = set(pa) & set(pb)
-    count_mm = beyond = 0
-    worst = 0.0
-    for k in common:
-        if pa[k].shape != pb[k].shape:
-            count_mm += 1
-            continue
-        d = cycle_distance(pa[k], pb[k])
-        if not np.isfinite(d) or d > tol:
-            beyond += 1
-        if np.isfinite(d):
-            worst = max(worst, d)
-    fa = sum(1 for k in pa if pa[k].shape[0] >= 3)
-    fb = sum(1 for k in pb if pb[k].shape[0] >= 3)
-    return dict(regions_a=len(ka), regions_b=len(kb), regions_only_a=len(ka - kb), regions_only_b=len(kb - ka),
-                faces_a=fa, faces_b=fb, common_polygons=len(common), faces_count_mismatch=count_mm,
-                faces_beyond_tol=beyond, max_diff=worst)
+    na_, nb_, only_a, only_b = _key_sets(a, b)
+    sa, sb, ra, rb = _matched(a, b, 1)
+    d, count_differs = _pair_distances(a, b, ra, rb)
+    same = ~count_differs
+    fin = np.isfinite(d) & same
+    return dict(regions_a=na_, regions_b=nb_, regions_only_a=only_a, regions_only_b=only_b,
+                faces_a=int((np.asarray(a.nverts)[sa] >= 3).sum()), faces_b=int((np.asarray(b.nverts)[sb] >= 3).sum()),
+                common_polygons=int(ra.size), faces_count_mismatch=int(count_differs.sum()),
+                faces_beyond_tol=int((same & (~np.isfinite(d) | (d > tol))).sum()),
+                max_diff=float(d[fin].max()) if fin.any() else 0.0)
