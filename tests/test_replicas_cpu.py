@@ -104,3 +104,15 @@ def test_region_budget_stops_oracle_and_reference_at_the_same_batch():
     # the budget is per call: the next unbudgeted run is complete again
     again = O.run_oracle(net, st, pt)
     assert again.num == full.num and np.array_equal(again.bits, full.bits)
+
+
+def test_composition_flop_counts_of_the_bench_workloads():
+    """8 (sum n_l n_l+1 + sum n_dst n_src) FLOP per region: 4 columns x 2 per
+    multiply-add over every layer product and transformed connection."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    for factory, want in ((wl.sphere, 8 * (3 * 128 ** 2 + 128)), (wl.deep, 8 * (5 * 256 ** 2 + 256)),
+                          (wl.large_skip, 8 * (7 * 512 ** 2 + 512 + 512 * 3))):
+        net = wl.net_arrays(factory())
+        assert bench.composition_flops(net.nodes, net.arc_table, net.tms) == want
