@@ -59,6 +59,9 @@ def AnalyticMarching(model, save_ply_path="mesh.ply", iso=0.0, scale=1.0, center
 
     Returns ``{"init_point_time", "init_cuda_time", "am_time", "export_time",
     "vertices", "faces", "stats"}``; writes ``save_ply_path`` unless it is None.
+    In voxel mode (``voxel_configs``) every occupied voxel is marched on its
+    own and the sub-meshes are concatenated; ``stats`` then describes the
+    last voxel's marching.
     """
     global _ENVIRONMENT
     init_configs = copy.deepcopy(init_configs if init_configs is not None else DICHOTOMY_DICT)
