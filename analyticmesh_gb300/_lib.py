@@ -22,7 +22,18 @@ class AmStats(C.Structure):
         ("mesh_num_indices", C.c_int64), ("chunks", C.c_int32), ("max_polygon_verts", C.c_int32),
         ("am_time_ms", C.c_double), ("compose_ms", C.c_double), ("polygon_ms", C.c_double),
         ("frontier_ms", C.c_double), ("kernel_launches", C.c_int64),
+        ("max_abs_f", C.c_double), ("max_vertex_err", C.c_double), ("error_faces", C.c_int64),
+        ("num_fp64_predicates", C.c_int64),
     ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class AmErrorReport(C.Structure):
+    """am_error_report_t: max |f(v)| and vertex error of a result against FP64."""
+    _fields_ = [("faces", C.c_int64), ("vertices", C.c_int64), ("vertices_singular", C.c_int64),
+                ("max_abs_f", C.c_double), ("max_vertex_err", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -44,10 +55,23 @@ AM_OPT_GRAPH = 4
 AM_OPT_MAX_REGIONS = 5
 AM_OPT_COMPOSE_TILE = 6
 AM_OPT_FACE_WARPS = 7
+AM_OPT_TABLE_SLOTS = 8
+AM_OPT_INJECT_ERROR = 9
+
+# device error bits (AM_OPT_INJECT_ERROR)
+ERR_TABLE_FULL, ERR_WAIT, ERR_CAPACITY, ERR_NONFINITE = 1, 2, 4, 8
+
+# status codes (am_status)
+AM_OK, AM_ERR_INVALID_ARGUMENT, AM_ERR_NOT_INITIALIZED, AM_ERR_CUDA, AM_ERR_OUT_OF_MEMORY = 0, 1, 2, 3, 4
+AM_ERR_TABLE_FULL, AM_ERR_NO_RESULT, AM_ERR_IO, AM_ERR_CAPACITY = 5, 6, 7, 8
 
 
 class AmError(RuntimeError):
-    pass
+    """A failed call; ``status`` is the am_status code."""
+
+    def __init__(self, msg, status=None):
+        super().__init__(msg)
+        self.status = status
 
 
 def lib():
@@ -77,6 +101,7 @@ def lib():
     L.am_run_batch.argtypes = [vp, C.POINTER(AmRunArgs), C.c_int, C.POINTER(C.c_double)]
     L.am_compose_rows_noalloc.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int, C.c_double, vp, vp, vp]
     L.am_autotune.argtypes = [vp, C.POINTER(AmRunArgs), C.c_int64, C.POINTER(C.c_int32)]
+    L.am_error_report.argtypes = [vp, C.c_int64, C.POINTER(AmErrorReport)]
     _LIB = L
     return L
 
@@ -85,7 +110,7 @@ def check(rc: int, handle=None):
     if rc != 0:
         L = lib()
         detail = L.am_last_error(handle).decode() if handle else ""
-        raise AmError("%s%s" % (L.am_strerror(rc).decode(), (": " + detail) if detail else ""))
+        raise AmError("%s%s" % (L.am_strerror(rc).decode(), (": " + detail) if detail else ""), rc)
 
 
 def vert_capacity() -> int:

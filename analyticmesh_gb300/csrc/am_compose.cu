@@ -209,7 +209,31 @@ __global__ void prepare_weights_kernel(const T *src, int M, int K, int Mp, T *ds
     }
 }
 
+// every value of the listed buffers finite; kErrNonFinite otherwise
+template <typename T>
+__global__ void check_finite_kernel(FiniteList list, int *err)
+{
+    const int b = blockIdx.y;
+    const T *p = (const T *)list.p[b];
+    bool bad = false;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < list.n[b]; q += (long long)gridDim.x * blockDim.x)
+        bad |= !isfinite(p[q]);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(err, kErrNonFinite);
+}
+
 } // namespace
+
+void launch_check_finite(int prec, const FiniteList &list, int *d_err, cudaStream_t st)
+{
+    if (list.count <= 0) return;
+    long long most = 1;
+    for (int b = 0; b < list.count; ++b) most = std::max(most, list.n[b]);
+    const dim3 grid((unsigned)std::min<long long>((most + 255) / 256, 64), (unsigned)list.count);
+    if (prec == kFloat64)
+        check_finite_kernel<double><<<grid, 256, 0, st>>>(list, d_err);
+    else
+        check_finite_kernel<float><<<grid, 256, 0, st>>>(list, d_err);
+}
 
 void launch_compose(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, double iso, cudaStream_t st)
 {

@@ -214,30 +214,43 @@ __device__ int total_blocks(const NetDev &net, const TcNet &tc)
 // h's products wait for its bytes (full barrier).  Phase parity of either
 // barrier for block h is (h / nstage) & 1.  h counts on across the CTA's
 // tiles, so the next tile's first blocks load during this tile's last layer.
+//
+// Every wait is bounded.  A wait that runs out sets the error bit kErrWait
+// and the CTA's abort flag: from then on thread 0 issues no copy and no
+// product, the other threads skip the epilogues, and before the CTA returns
+// thread 0 waits (again bounded) for the copies and products already in
+// flight, so that nothing lands in shared memory or TMEM after the CTA has
+// released them.  The host reports kErrWait as a failed run.
 struct WPipe {
     uint64_t *full, *done;
     uint8_t *ws;
     int nstage, total, issued;
     int *err;
-    int per_tile; // blocks one tile consumes; the sequence repeats per tile
+    int per_tile;          // blocks one tile consumes; the sequence repeats per tile
+    int consumed;          // blocks whose bytes were observed and whose products were issued
+    volatile int *abort;   // the CTA's abort flag (shared memory)
 };
 
-__device__ __forceinline__ void wp_wait(WPipe &p, uint64_t *bar, uint32_t parity)
+__device__ __forceinline__ bool wp_wait(WPipe &p, uint64_t *bar, uint32_t parity)
 {
-    if (!umma::mbar_wait(bar, parity, kWaitIters)) {
-        atomicOr(p.err, kErrWalk);
-        umma::mbar_wait(bar, parity, kWaitIters);
-    }
+    if (umma::mbar_wait(bar, parity, kWaitIters)) return true;
+    atomicOr(p.err, kErrWait);
+    *p.abort = 1;
+    return false;
 }
 
-__device__ void wp_issue(WPipe &p, const NetDev &net, const TcNet &tc)
+// copy the next weight block into its stage; false (nothing issued) once the
+// CTA is aborting
+__device__ bool wp_issue(WPipe &p, const NetDev &net, const TcNet &tc)
 {
+    if (*p.abort) return false;
     const int h = p.issued, s = h % p.nstage;
-    if (h >= p.nstage) wp_wait(p, p.done + s, (uint32_t)((h - p.nstage) / p.nstage) & 1u);
+    if (h >= p.nstage && !wp_wait(p, p.done + s, (uint32_t)((h - p.nstage) / p.nstage) & 1u)) return false;
     umma::mbar_expect_tx(p.full + s, (uint32_t)kWBlockBytes);
     umma::bulk_g2s(p.ws + (size_t)s * kWBlockBytes, block_ptr(net, tc, h % p.per_tile), (uint32_t)kWBlockBytes,
                    p.full + s);
     p.issued = h + 1;
+    return true;
 }
 
 // (thread 0) D[mt] (+)= M . X over all K blocks of the operand in shared
@@ -251,9 +264,9 @@ __device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const T
     const int kblocks = m.Kp / 64;
     for (int mt = 0; mt < mtiles; ++mt) {
         for (int kb = 0; kb < kblocks; ++kb) {
-            if (p.issued <= g) wp_issue(p, net, tc);
+            if (p.issued <= g && !wp_issue(p, net, tc)) return;
             const int s = g % p.nstage;
-            wp_wait(p, p.full + s, (uint32_t)(g / p.nstage) & 1u);
+            if (!wp_wait(p, p.full + s, (uint32_t)(g / p.nstage) & 1u)) return;
             umma::fence_after();
             const uint32_t a0 = umma::smem_addr(p.ws + (size_t)s * kWBlockBytes);
             const uint32_t d_main = tmem + (uint32_t)(mt * ncols);            // hh
@@ -276,8 +289,10 @@ __device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const T
                     }
             }
             umma::commit(umma::smem_addr(p.done + s));
+            p.consumed = g + 1;
             // refill the stage freed by the previous block
-            while (p.issued < p.total && p.issued <= g + p.nstage - 1) wp_issue(p, net, tc);
+            while (p.issued < p.total && p.issued <= g + p.nstage - 1 && wp_issue(p, net, tc)) {
+            }
             ++g;
         }
     }
@@ -287,18 +302,30 @@ __device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const T
 // TMEM, then start the next layer's blocks so they land during the epilogue
 __device__ void gemm_finish(WPipe &p, const NetDev &net, const TcNet &tc, int g)
 {
+    if (*p.abort) return;
     const int last = g - 1;
-    wp_wait(p, p.done + last % p.nstage, (uint32_t)(last / p.nstage) & 1u);
+    if (!wp_wait(p, p.done + last % p.nstage, (uint32_t)(last / p.nstage) & 1u)) return;
     umma::fence_before();
-    while (p.issued < p.total && p.issued <= last + p.nstage) wp_issue(p, net, tc);
+    while (p.issued < p.total && p.issued <= last + p.nstage && wp_issue(p, net, tc)) {
+    }
 }
 
 // (every thread, after the block barrier that follows gemm_finish) observe
 // the same completion before reading the accumulators
 __device__ __forceinline__ void gemm_observe(const WPipe &p, int last)
 {
-    if (!umma::mbar_wait(p.done + last % p.nstage, (uint32_t)(last / p.nstage) & 1u, kWaitIters)) atomicOr(p.err, kErrWalk);
+    if (!umma::mbar_wait(p.done + last % p.nstage, (uint32_t)(last / p.nstage) & 1u, kWaitIters)) atomicOr(p.err, kErrWait);
     umma::fence_after();
+}
+
+// (thread 0, aborting CTA) wait, bounded, for the copies issued but never
+// observed and for the products of the last committed block
+__device__ void wp_drain(WPipe &p)
+{
+    for (int h = p.consumed; h < p.issued; ++h)
+        umma::mbar_wait(p.full + h % p.nstage, (uint32_t)(h / p.nstage) & 1u, kWaitIters);
+    if (p.consumed > 0)
+        umma::mbar_wait(p.done + (p.consumed - 1) % p.nstage, (uint32_t)((p.consumed - 1) / p.nstage) & 1u, kWaitIters);
 }
 
 // words between two regions' keys in shared memory: odd, so that lanes
@@ -321,6 +348,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     __shared__ uint64_t bars[4];
     __shared__ uint32_t tslot;
     __shared__ int s_last;
+    __shared__ int s_abort; // set by thread 0 when a pipeline wait runs out
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     long long head;
     int count;
@@ -351,14 +379,16 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     float *wls = reinterpret_cast<float *>(w0s + net.nodes[1]);
     float *fsum = reinterpret_cast<float *>(reinterpret_cast<uintptr_t>(wls + net.nodes[net.n_lin - 1] + 3) & ~(uintptr_t)15);
 
-    WPipe pp{bars, bars + 2, ws, tc.nstage, 0, 0, err, 1};
+    WPipe pp{bars, bars + 2, ws, tc.nstage, 0, 0, err, 1, 0, &s_abort};
     if (tid == 0) {
+        s_abort = 0;
         for (int b = 0; b < 4; ++b) umma::mbar_init(bars + b, 1);
         umma::fence_mbar_init();
         pp.per_tile = total_blocks(net, tc);
         pp.total = pp.per_tile * mytiles;
         // the first weight blocks do not depend on the tile: start them now
-        while (pp.issued < pp.total && pp.issued < pp.nstage) wp_issue(pp, net, tc);
+        while (pp.issued < pp.total && pp.issued < pp.nstage && wp_issue(pp, net, tc)) {
+        }
     }
     if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tmem_cols);
     {
@@ -432,6 +462,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                     // the operand is about to be overwritten: the products so far must be done
                     if (tid == 0) gemm_finish(pp, net, tc, g);
                     __syncthreads();
+                    if (s_abort) break; // written by thread 0 before the barrier: uniform
                     stage_x_from_rows(X, cons, rstride, keys, KW, nreg, net.hoff[sk.from],
                                       net.nodes[sk.from], tc.skip[i][s].Kp);
                     umma::fence_proxy_async();
@@ -448,6 +479,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             }
             __syncwarp();
             __syncthreads();
+            if (s_abort) break; // no epilogue: the accumulators are not complete
             gemm_observe(pp, s_last);
             // epilogue: accumulators -> constraint rows (HBM) and the next operand (smem)
             const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
@@ -520,6 +552,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             umma::fence_after();
         }
 
+        if (s_abort) break;
         // face plane: w_eq = W_L . X_L (+ b_L, + connections into the output layer)
         // in fp32 from the operand in shared memory (hi + mid + lo is exact):
         // lanes take regions (consecutive regions share operand rows), the
@@ -572,6 +605,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             }
         }
     } // tiles
+    if (tid == 0 && s_abort) wp_drain(pp);
     umma::fence_before();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tslot, (uint32_t)tmem_cols);
@@ -624,12 +658,18 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(umma::smem_addr(bar)) : "memory");
 }
 
-__device__ __forceinline__ void swait(uint64_t *bar, uint32_t parity, int *err)
+// Bounded wait of the streamed kernel: false at once when the CTA is
+// aborting, and false -- with the error bit kErrWait and the abort flag set --
+// when the wait runs out.  An aborting CTA keeps its arrive / commit / barrier
+// sequence (so that no thread waits on a partner that gave up) but issues no
+// copy or product and skips the epilogue work.
+__device__ __forceinline__ bool swait(uint64_t *bar, uint32_t parity, int *err, volatile int *abort)
 {
-    if (!umma::mbar_wait(bar, parity, kWaitIters)) {
-        atomicOr(err, kErrWalk);
-        umma::mbar_wait(bar, parity, kWaitIters);
-    }
+    if (*abort) return false;
+    if (umma::mbar_wait(bar, parity, kWaitIters)) return true;
+    atomicOr(err, kErrWait);
+    *abort = 1;
+    return false;
 }
 
 // position in the product sequence: tile, layer, job, K block, M tile (innermost)
@@ -659,15 +699,15 @@ __device__ void scur_next(SCur &c, const NetDev &net, const TcNet &tc, int tiles
 // correction accumulator of each M tile
 __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, uint64_t *wfull, uint64_t *wdone,
                                const XOp *XS, uint64_t *xfull, uint64_t *xdone, uint64_t *accdone, uint32_t tmem,
-                               int ncols, int tiles, int *err)
+                               int ncols, int tiles, int *err, volatile int *abort)
 {
     const int nst = tc.nstage;
     SCur cc{0, 1, 0, 0, 0, net.n_lin - 2 >= 1}; // next weight block to copy
     SCur mc = cc;                                // next weight block to multiply
-    int issued = 0;
-    auto copy_next = [&]() {
+    int issued = 0, consumed = 0;
+    auto copy_next = [&]() -> bool {
         const int s = issued % nst;
-        if (issued >= nst) swait(wdone + s, (uint32_t)((issued - nst) / nst) & 1u, err);
+        if (issued >= nst && !swait(wdone + s, (uint32_t)((issued - nst) / nst) & 1u, err, abort)) return false;
         int src;
         const TcMat &m = job_mat(net, tc, cc.i, cc.job, src);
         umma::mbar_expect_tx(wfull + s, (uint32_t)kWBlockBytes);
@@ -676,8 +716,10 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
                        wfull + s);
         ++issued;
         scur_next(cc, net, tc, tiles);
+        return true;
     };
-    while (cc.valid && issued < nst) copy_next();
+    while (cc.valid && issued < nst && copy_next()) {
+    }
     int h = 0, xb = 0;
     // operand descriptors of the two stages; term and K step add constant offsets
     const uint64_t xd0 = XS[0].desc(0, 0, 0), xd1 = XS[1].desc(0, 0, 0);
@@ -689,42 +731,52 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
         const int mtiles = m.Mp / 128, kblocks = m.Kp / 64;
         const int xs = xb & 1;
         const uint64_t xd = xs ? xd1 : xd0;
-        if (mc.mt == 0) swait(xfull + xs, (uint32_t)(xb >> 1) & 1u, err); // operand block built
-        while (cc.valid && issued <= h) copy_next();
-        const int s = h % nst;
-        swait(wfull + s, (uint32_t)(h / nst) & 1u, err);
-        umma::fence_after();
-        const uint32_t a0 = umma::smem_addr(ws + (size_t)s * kWBlockBytes);
-        const uint32_t d_main = tmem + (uint32_t)(mc.mt * ncols);
-        const uint32_t d_corr = tmem + (uint32_t)((mtiles + mc.mt) * ncols);
-        const bool fresh = mc.job == 0 && mc.kb == 0;
-        const uint64_t ad = umma::desc_sw128(a0); // term t at +16 KB, K step j at +32 B
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            umma::mma_bf16(d_main, ad + 2u * j, xd + xj * j, idesc, (fresh && j == 0) ? 0u : 1u);
-            int q = 0;
-#pragma unroll
-            for (int t = 0; t < 3; ++t)
-#pragma unroll
-                for (int u = 0; u + t < 3; ++u) {
-                    if (t == 0 && u == 0) continue;
-                    umma::mma_bf16(d_corr, ad + 1024u * t + 2u * j, xd + xu * u + xj * j, idesc,
-                                   (fresh && j == 0 && q == 0) ? 0u : 1u);
-                    ++q;
-                }
+        bool ok = mc.mt != 0 || swait(xfull + xs, (uint32_t)(xb >> 1) & 1u, err, abort); // operand block built
+        while (ok && cc.valid && issued <= h && copy_next()) {
         }
-        umma::commit(umma::smem_addr(wdone + s));
+        const int s = h % nst;
+        ok = ok && issued > h && swait(wfull + s, (uint32_t)(h / nst) & 1u, err, abort);
+        if (ok) {
+            umma::fence_after();
+            const uint32_t a0 = umma::smem_addr(ws + (size_t)s * kWBlockBytes);
+            const uint32_t d_main = tmem + (uint32_t)(mc.mt * ncols);
+            const uint32_t d_corr = tmem + (uint32_t)((mtiles + mc.mt) * ncols);
+            const bool fresh = mc.job == 0 && mc.kb == 0;
+            const uint64_t ad = umma::desc_sw128(a0); // term t at +16 KB, K step j at +32 B
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                umma::mma_bf16(d_main, ad + 2u * j, xd + xj * j, idesc, (fresh && j == 0) ? 0u : 1u);
+                int q = 0;
+#pragma unroll
+                for (int t = 0; t < 3; ++t)
+#pragma unroll
+                    for (int u = 0; u + t < 3; ++u) {
+                        if (t == 0 && u == 0) continue;
+                        umma::mma_bf16(d_corr, ad + 1024u * t + 2u * j, xd + xu * u + xj * j, idesc,
+                                       (fresh && j == 0 && q == 0) ? 0u : 1u);
+                        ++q;
+                    }
+            }
+            umma::commit(umma::smem_addr(wdone + s));
+            consumed = h + 1;
+        }
+        // the builders' barriers are served in every case
         if (mc.mt == mtiles - 1) {
             umma::commit(umma::smem_addr(xdone + xs)); // the operand stage is free once these complete
             ++xb;
             if (mc.kb == kblocks - 1 && mc.job == jobs_of(net, mc.i) - 1)
                 umma::commit(umma::smem_addr(accdone)); // the layer's accumulators are complete
         }
-        while (cc.valid && issued <= h + nst - 1) copy_next(); // refill the stage of block h - 1
+        while (ok && cc.valid && issued <= h + nst - 1 && copy_next()) { // refill the stage of block h - 1
+        }
         ++h;
         scur_next(mc, net, tc, tiles);
     }
-    if (h > 0) swait(wdone + (h - 1) % nst, (uint32_t)((h - 1) / nst) & 1u, err);
+    // copies issued but never observed (aborting CTA), then the last products
+    for (int q = consumed; q < issued; ++q) umma::mbar_wait(wfull + q % nst, (uint32_t)(q / nst) & 1u, kWaitIters);
+    if (consumed > 0 &&
+        !umma::mbar_wait(wdone + (consumed - 1) % nst, (uint32_t)((consumed - 1) / nst) & 1u, kWaitIters))
+        atomicOr(err, kErrWait);
 }
 
 __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, TcNet tc, RegionsDev reg, ChunkDev ch,
@@ -734,6 +786,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
     // wfull[3], wdone[3] (weight ring), xfull[2], xdone[2] (operand ring), accdone
     __shared__ uint64_t bars[11];
     __shared__ uint32_t tslot;
+    __shared__ int s_abort; // a wait ran out: nothing more is issued, epilogues are skipped
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     long long head;
     int count;
@@ -767,7 +820,9 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
     float *fsum = reinterpret_cast<float *>(reinterpret_cast<uintptr_t>(wls + net.nodes[net.n_lin - 1] + 3) & ~(uintptr_t)15);
     uint64_t *wfull = bars, *wdone = bars + 3, *xfull = bars + 6, *xdone = bars + 8, *accdone = bars + 10;
 
+    volatile int *abort = &s_abort;
     if (tid == 0) {
+        s_abort = 0;
         for (int b = 0; b < 6; ++b) umma::mbar_init(bars + b, 1);
         umma::mbar_init(xfull, kSBuild);
         umma::mbar_init(xfull + 1, kSBuild);
@@ -792,7 +847,8 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
     const uint32_t tmem = tslot;
 
     if (warp == kSBuild / 32) {
-        if (lane == 0) issue_streamed(net, tc, ws, wfull, wdone, XS, xfull, xdone, accdone, tmem, ncols, tiles, err);
+        if (lane == 0)
+            issue_streamed(net, tc, ws, wfull, wdone, XS, xfull, xdone, accdone, tmem, ncols, tiles, err, abort);
         __syncwarp(); // the warp reaches the block barrier below converged
     } else {
         // epilogue: warp w reads TMEM lanes 32 (w % 4).. and every fourth column block
@@ -834,11 +890,12 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                     const int K = net.nodes[src], rows0 = net.hoff[src];
                     for (int kb = 0; kb < mat.Kp / 64; ++kb) {
                         const int xs = xb & 1, fill = xb >> 1;
-                        if (fill >= 1) swait(xdone + xs, (uint32_t)((fill - 1) & 1), err); // stage free
+                        // stage free (an aborting CTA builds nothing but still arrives)
+                        const bool ok = fill < 1 ? !*abort : swait(xdone + xs, (uint32_t)((fill - 1) & 1), err, abort);
                         const XOp &X = XS[xs];
                         // X[4r + c][k] = s_k(r) ? -C[r][k][c] : 0 for the block's 64 rows k,
                         // regions fastest across the lanes; two loads in flight per thread
-                        for (int q0 = tid; q0 < R * 64; q0 += 2 * kSBuild) {
+                        for (int q0 = tid; ok && q0 < R * 64; q0 += 2 * kSBuild) {
                             float x[2][4];
 #pragma unroll
                             for (int u = 0; u < 2; ++u) {
@@ -868,11 +925,14 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                 }
                 const float *bias = (const float *)net.bias[i];
                 float bnext = q4 * 32 + lane < M ? bias[q4 * 32 + lane] : 0.f; // loaded while the products run
-                swait(accdone, (uint32_t)(accph & 1), err); // the layer's products are in TMEM
+                // the layer's products are in TMEM; the TMEM loads below are
+                // warp-collective, so the warp decides as one
+                bool acc_ok = swait(accdone, (uint32_t)(accph & 1), err, abort);
+                acc_ok = __all_sync(0xffffffffu, acc_ok) && !__any_sync(0xffffffffu, *abort != 0);
                 ++accph;
                 umma::fence_after();
                 // epilogue: accumulators -> constraint rows of hidden layer i + 1
-                for (int mt = 0; mt < mtiles; ++mt) {
+                for (int mt = 0; acc_ok && mt < mtiles; ++mt) {
                     const int m = mt * 128 + q4 * 32 + lane;
                     const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
                     const float bm = bnext;
@@ -930,10 +990,11 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                 const int K = net.nodes[i], rows0 = net.hoff[i];
                 const float bl = ((const float *)net.bias[i])[0];
                 constexpr int kWarps = kSBuild / 32;
+                const bool live = !*abort; // per thread: the barriers below are kept either way
                 for (int r0 = 0; r0 < R; r0 += 32) {
                     const int r = r0 + lane;
                     float acc[4] = {0.f, 0.f, 0.f, 0.f};
-                    if (r < nreg)
+                    if (live && r < nreg)
                         for (int k = warp; k < K; k += kWarps) {
                             const float w = wls[k];
                             float x[4] = {0.f, 0.f, 0.f, 0.f};
@@ -946,7 +1007,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                         }
                     reinterpret_cast<float4 *>(fsum)[warp * 32 + lane] = make_float4(acc[0], acc[1], acc[2], acc[3]);
                     bar_builders();
-                    if (tid < 128) {
+                    if (live && tid < 128) {
                         const int rr = tid >> 2, c = tid & 3, rg = r0 + rr;
                         float a = 0.f;
                         for (int w = 0; w < kWarps; ++w) a += fsum[(w * 32 + rr) * 4 + c];

@@ -168,6 +168,11 @@ struct am_engine {
     // network
     DevBuf wt[kMaxLayers], bias[kMaxLayers], w0, tmt[64], wext, bext, scratch;
     NetDev net{};
+    int ntm = 0;                // transforms in tmt
+    long long tm_count[64] = {}; // elements of each
+    // error report: FP64 copies of the parameters (FP32 engines), sample buffers
+    DevBuf wt64[kMaxLayers], bias64[kMaxLayers], w0_64, tmt64[64], wext64, bext64;
+    DevBuf v_ids, v_keys, v_rows, v_eq, v_out;
     // tensor-core composition (mixed form): bf16 hi/lo weights
     DevBuf tc_lin[kMaxLayers], tc_skip[kMaxLayers][kMaxSkips];
     TcNet tcnet{};
@@ -207,6 +212,8 @@ struct am_engine {
     long long max_regions = 0; // AM_OPT_MAX_REGIONS (0: no limit)
     int compose_tile = 0;      // AM_OPT_COMPOSE_TILE: 0 automatic, 1 resident operand, 2 streamed operand
     int face_warps = 0;        // AM_OPT_FACE_WARPS: warps per face polygon, 0 automatic
+    long long table_slots = 0; // AM_OPT_TABLE_SLOTS: fixed region hash table size, 0 automatic
+    int inject_err = 0;        // AM_OPT_INJECT_ERROR: error bits set in the control block after the seeds
     bool limit_hit = false;    // the last run stopped at the region limit
     bool over_limit(long long tail)
     {
@@ -275,13 +282,21 @@ struct am_engine {
         cap = nc;
     }
 
-    // keep the load factor of the region table <= 1/2
+    // keep the load factor of the region table <= 1/2; with a fixed size
+    // (AM_OPT_TABLE_SLOTS) the table never grows, and a run that outgrows it
+    // ends with AM_ERR_TABLE_FULL when an insert reaches the probe bound
     void ensure_table(long long entries, bool rehash)
     {
         unsigned long long need = 1;
-        while (need < (unsigned long long)std::max<long long>(entries, 1) * 2ull) need <<= 1;
-        need = std::max<unsigned long long>(need, 1ull << 16);
-        if (need <= hcap) return;
+        if (table_slots > 0) {
+            while (need < (unsigned long long)table_slots) need <<= 1;
+            if (need == hcap) return;
+            rehash = rehash && need > hcap;
+        } else {
+            while (need < (unsigned long long)std::max<long long>(entries, 1) * 2ull) need <<= 1;
+            need = std::max<unsigned long long>(need, 1ull << 16);
+            if (need <= hcap) return;
+        }
         AM_CUDA(table.reserve(sizeof(unsigned long long) * need));
         hcap = need;
         AM_CUDA(cudaMemsetAsync(table.p, 0xff, sizeof(unsigned long long) * need, st));
@@ -316,10 +331,19 @@ struct am_engine {
     {
         AM_CUDA(cudaMemcpyAsync(h_ctl, d_tail.p, bytes, cudaMemcpyDeviceToHost, st));
         AM_CUDA(cudaStreamSynchronize(st));
-        const int e = h_ctl->err;
+        raise_device_errors(h_ctl->err);
+        return h_ctl->tail;
+    }
+    // the control block's error bits as a status (the first that applies)
+    static void raise_device_errors(int e)
+    {
+        if (e & kErrNonFinite)
+            throw Failure{AM_ERR_INVALID_ARGUMENT, "weights, biases, transforms or extra constraints hold NaN or infinity"};
+        if (e & kErrWait)
+            throw Failure{AM_ERR_CUDA, "device wait limit reached: a tensor-core pipeline barrier wait ran out, "
+                                       "the kernel stopped issuing work and the run's results are not valid"};
         if (e & kErrTableFull) throw Failure{AM_ERR_TABLE_FULL, "hash probe bound reached"};
         if (e & kErrCapacity) throw Failure{AM_ERR_CAPACITY, "region store capacity exceeded"};
-        return h_ctl->tail;
     }
     WaveCtl *ctl() const { return (WaveCtl *)d_tail.p; }
 
@@ -513,6 +537,7 @@ void run_begin(am_engine *e, const RunArgs &a)
         }
     }
     int ntm = 0;
+    long long *tm_count = e->tm_count;
     for (int i = 1; i < e->n_lin; ++i) {
         const int *row = e->arc.data() + (size_t)(i - 1) * e->arc_cols;
         net.nskip[i] = row[0];
@@ -535,16 +560,39 @@ void run_begin(am_engine *e, const RunArgs &a)
                 sk.kind = 1;
                 sk.tmt = e->tmt[ntm].p;
                 sk.Mp = Mp;
+                tm_count[ntm] = (long long)w * Mp;
                 ntm++;
             }
         }
     }
+    e->ntm = ntm;
     if (e->E) {
         upload(e->wext, w_extra, tc * 3 * (size_t)e->E, st);
         upload(e->bext, b_extra, tc * (size_t)e->E, st);
     }
     net.w_extra = e->wext.p;
     net.b_extra = e->bext.p;
+    {
+        // every parameter finite (checked on the device copies, one launch;
+        // decoded as AM_ERR_INVALID_ARGUMENT by the first poll)
+        FiniteList fl{};
+        auto add = [&](const void *p, long long n) {
+            if (p && n > 0 && fl.count < 64) {
+                fl.p[fl.count] = p;
+                fl.n[fl.count++] = n;
+            }
+        };
+        AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
+        for (int i = 0; i < e->n_lin; ++i) add(e->bias[i].p, e->nodes[i + 1]);
+        add(e->w0.p, 3ll * e->nodes[1]);
+        for (int i = 1; i < e->n_lin; ++i) add(e->wt[i].p, (long long)e->nodes[i] * net.Mp[i]);
+        for (int t = 0; t < ntm; ++t) add(e->tmt[t].p, tm_count[t]);
+        if (e->E) {
+            add(e->wext.p, 3ll * e->E);
+            add(e->bext.p, e->E);
+        }
+        launch_check_finite(prec == kFloat64 ? kFloat64 : kFloat32, fl, e->d_err.as<int>(), st);
+    }
     if (prec == kMixed) {
         // three bf16 terms per weight, stored as 128 x 64 shared-memory block images
         TcNet &tc = e->tcnet;
@@ -648,7 +696,6 @@ void run_begin(am_engine *e, const RunArgs &a)
     e->hcap = 0;
     e->stats = am_stats{};
     AM_CUDA(cudaMemsetAsync(e->d_tail.p, 0, sizeof(long long), st));
-    AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
     const int chunk = e->default_chunk();
     e->ensure_chunk(std::min(chunk, std::max(S, 1024)));
     const long long first_wave = e->lean ? std::min<long long>(chunk, 4ll * S + 1024) : chunk;
@@ -669,11 +716,18 @@ void run_begin(am_engine *e, const RunArgs &a)
                       e->s_hash.as<uint64_t>(), e->s_pts.p, S, e->d_tail.as<long long>(), e->blocksum.as<int>(),
                       (int)(e->blocksum.bytes / sizeof(int)), e->d_err.as<int>(), st);
     }
-    e->run.launches += 4;
+    e->run.launches += 5; // + the parameter check
     AM_CUDA(cudaGetLastError());
     const long long tail = e->poll();
     e->num_regions = tail;
     e->stats.num_seeds = tail;
+    if (e->inject_err) {
+        // test hook: error bits as a kernel would leave them, for the wave
+        // loop's error decoding to find
+        e->h_ctl->err = e->inject_err;
+        AM_CUDA(cudaMemcpyAsync(e->d_err.p, &e->h_ctl->err, sizeof(int), cudaMemcpyHostToDevice, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+    }
 
     am_engine::Run &r = e->run;
     r.prec = prec;
@@ -703,7 +757,7 @@ void run_graph_launch(am_engine *e, int max_waves)
     h->head = r.head;
     h->count = count;
     h->waves = 0;
-    h->limit = std::min<long long>(e->cap, (long long)(e->hcap / 2));
+    h->limit = e->table_slots > 0 ? e->cap : std::min<long long>(e->cap, (long long)(e->hcap / 2));
     h->chunk_cap = r.chunk;
     h->work = 0u;
     h->max_waves = max_waves;
@@ -720,8 +774,7 @@ bool run_graph_done(am_engine *e)
 {
     am_engine::Run &r = e->run;
     const WaveCtl *h = e->h_ctl;
-    if (h->err & kErrTableFull) throw Failure{AM_ERR_TABLE_FULL, "hash probe bound reached"};
-    if (h->err & kErrCapacity) throw Failure{AM_ERR_CAPACITY, "region store capacity exceeded"};
+    am_engine::raise_device_errors(h->err);
     AM_CHECK(h->waves < kMaxWaves, "wave bound reached");
     r.tail = h->tail;
     r.chunks += h->waves;
@@ -966,6 +1019,17 @@ int am_set_option(am_engine *e, int option, int64_t value)
         e->compose_tile = (int)value;
         return AM_OK;
     }
+    if (option == AM_OPT_TABLE_SLOTS) {
+        if (value < 0 || value > (int64_t(1) << 40)) return AM_ERR_INVALID_ARGUMENT;
+        e->table_slots = value;
+        e->hcap = 0; // the next run sizes the table afresh
+        return AM_OK;
+    }
+    if (option == AM_OPT_INJECT_ERROR) {
+        if (value < 0 || value > (kErrTableFull | kErrWait | kErrCapacity | kErrNonFinite)) return AM_ERR_INVALID_ARGUMENT;
+        e->inject_err = (int)value;
+        return AM_OK;
+    }
     return AM_ERR_INVALID_ARGUMENT;
 }
 
@@ -1158,6 +1222,100 @@ int am_run_batch(am_engine *const *engines, const am_run_args *args, int count, 
     }
     if (wall_ms) *wall_ms = wall;
     return AM_OK;
+}
+
+// FP64 view of the engine's network for the error report: the engine's own
+// parameter copies, converted exactly to double (FP32 engines), same layouts
+static NetDev network_fp64(am_engine *e)
+{
+    if (e->prec == kFloat64) return e->net;
+    cudaStream_t st = e->st;
+    NetDev n = e->net;
+    auto conv = [&](DevBuf &dst, const void *src, long long count) -> const void * {
+        if (!src || count <= 0) return src;
+        AM_CUDA(dst.reserve(sizeof(double) * (size_t)count));
+        launch_to_double(src, count, dst.p, st);
+        return dst.p;
+    };
+    n.W0 = conv(e->w0_64, e->net.W0, 3ll * e->nodes[1]);
+    for (int i = 0; i < e->n_lin; ++i) n.bias[i] = conv(e->bias64[i], e->net.bias[i], e->nodes[i + 1]);
+    for (int i = 1; i < e->n_lin; ++i) n.Wt[i] = conv(e->wt64[i], e->net.Wt[i], (long long)e->nodes[i] * e->net.Mp[i]);
+    int t = 0;
+    for (int i = 1; i < e->n_lin; ++i)
+        for (int c = 0; c < e->net.nskip[i]; ++c)
+            if (e->net.skip[i][c].kind == 1) {
+                n.skip[i][c].tmt = conv(e->tmt64[t], e->net.skip[i][c].tmt, e->tm_count[t]);
+                ++t;
+            }
+    if (e->E) {
+        n.w_extra = conv(e->wext64, e->net.w_extra, 3ll * e->E);
+        n.b_extra = conv(e->bext64, e->net.b_extra, e->E);
+    }
+    AM_CUDA(cudaGetLastError());
+    return n;
+}
+
+int am_error_report(am_engine *e, int64_t sample_regions, am_error_report_t *out)
+{
+    if (!e) return AM_ERR_NOT_INITIALIZED;
+    if (!e->has_am) return AM_ERR_NO_RESULT;
+    if (!out || sample_regions < 0) return AM_ERR_INVALID_ARGUMENT;
+    return guarded(e, [&] {
+        cudaStream_t st = e->st;
+        const long long R = e->num_regions;
+        const long long k = (sample_regions == 0 || sample_regions > R) ? R : sample_regions;
+        *out = am_error_report_t{};
+        if (k <= 0) return;
+        // evenly spaced region ids
+        std::vector<long long> ids((size_t)k);
+        for (long long j = 0; j < k; ++j) ids[(size_t)j] = (long long)((double)j * (double)R / (double)k);
+        for (long long j = 1; j < k; ++j) ids[(size_t)j] = std::max(ids[(size_t)j], ids[(size_t)j - 1] + 1);
+        for (long long j = k - 1; j >= 0 && ids[(size_t)j] >= R; --j) ids[(size_t)j] = R - 1 - (k - 1 - j);
+        AM_CUDA(e->v_ids.reserve(sizeof(long long) * (size_t)k));
+        AM_CUDA(cudaMemcpyAsync(e->v_ids.p, ids.data(), sizeof(long long) * (size_t)k, cudaMemcpyHostToDevice, st));
+        const NetDev n64 = network_fp64(e);
+        // FP64 rows in slices of at most 1 GiB
+        const long long per = (long long)e->ALLP * 4 * (long long)sizeof(double);
+        const int slice = (int)std::max<long long>(1, std::min<long long>(k, ((long long)1 << 30) / per));
+        AM_CUDA(e->v_keys.reserve(sizeof(uint32_t) * (size_t)slice * e->W));
+        AM_CUDA(e->v_rows.reserve((size_t)per * slice));
+        AM_CUDA(e->v_eq.reserve(sizeof(double) * 4 * (size_t)slice));
+        AM_CUDA(e->v_out.reserve(sizeof(unsigned long long) * 5));
+        AM_CUDA(cudaMemsetAsync(e->v_out.p, 0, sizeof(unsigned long long) * 5, st));
+        const RegionsDev reg = e->regions();
+        for (long long off = 0; off < k; off += slice) {
+            const int cnt = (int)std::min<long long>(slice, k - off);
+            const long long *dids = e->v_ids.as<long long>() + off;
+            launch_gather_keys(e->keys.as<uint32_t>(), e->W, dids, cnt, e->v_keys.as<uint32_t>(), st);
+            RegionsDev rr{};
+            rr.keys = e->v_keys.as<uint32_t>();
+            rr.cap = cnt;
+            ChunkDev ch;
+            ch.head = 0;
+            ch.count = cnt;
+            ch.cons = e->v_rows.p;
+            ch.eq = e->v_eq.p;
+            ch.rec = nullptr;
+            launch_compose(kFloat64, n64, rr, ch, e->iso, st);
+            launch_verify((int)e->ts, reg, dids, cnt, e->v_rows.as<double>(), e->v_eq.as<double>(), e->ALLP, e->ALL,
+                          e->v_out.as<unsigned long long>(), st);
+            AM_CUDA(cudaGetLastError());
+        }
+        unsigned long long h[5];
+        AM_CUDA(cudaMemcpyAsync(h, e->v_out.p, sizeof(h), cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        double f, v;
+        memcpy(&f, &h[0], sizeof(double));
+        memcpy(&v, &h[1], sizeof(double));
+        out->faces = (int64_t)h[4];
+        out->vertices = (int64_t)h[2];
+        out->vertices_singular = (int64_t)h[3];
+        out->max_abs_f = f;
+        out->max_vertex_err = v;
+        e->stats.max_abs_f = f;
+        e->stats.max_vertex_err = v;
+        e->stats.error_faces = (int64_t)h[4];
+    });
 }
 
 int am_get_stats(const am_engine *e, am_stats *out)

@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
 }
 
 // graph-driven loop: retire the wave, take the next one from the queue and
-// go on while it is non-empty, no fatal error is set and its children fit
+// go on while it is non-empty, no error bit is set and its children fit
 __global__ void wave_step_kernel(WaveCtl *ctl, cudaGraphConditionalHandle cond)
 {
     WaveCtl &c = *ctl;
@@ -266,7 +266,7 @@ __global__ void wave_step_kernel(WaveCtl *ctl, cudaGraphConditionalHandle cond)
     const long long rem = c.tail - c.head;
     c.count = (int)(rem < (long long)c.chunk_cap ? (rem > 0 ? rem : 0) : (long long)c.chunk_cap);
     c.work = 0u;
-    const bool go = c.count > 0 && (c.err & (kErrTableFull | kErrCapacity)) == 0 &&
+    const bool go = c.count > 0 && c.err == 0 &&
                     c.tail + (long long)c.count * kVMax <= c.limit && c.waves < c.max_waves &&
                     c.tail <= c.stop_tail;
     cudaGraphSetConditional(cond, go ? 1u : 0u);

@@ -21,8 +21,11 @@ enum Precision : int { kFloat32 = 0, kFloat64 = 1, kMixed = 2 };
 // Region status codes (poly_status)
 enum : int8_t { kOk = 0, kNoStart = 1, kOpen = 2, kTruncated = 3, kSingular = 4 };
 
-// Device error bits
-enum : int { kErrTableFull = 1, kErrWalk = 2, kErrCapacity = 4 };
+// Device error bits.  kErrWait: a bounded wait inside a kernel (a
+// tensor-core pipeline barrier) ran out; the kernel stopped issuing work and
+// returned, and its results are not valid.  kErrNonFinite: a weight, bias,
+// transform or extra constraint is NaN or infinite.
+enum : int { kErrTableFull = 1, kErrWait = 2, kErrCapacity = 4, kErrNonFinite = 8 };
 
 struct SkipDev {
     int from;        // 0 = network input, h >= 1 = hidden layer h
@@ -139,7 +142,21 @@ void launch_region_stats(const int32_t *nv, const int8_t *status, long long n, u
                          cudaStream_t st);
 void launch_wave_step(WaveCtl *ctl, cudaGraphConditionalHandle cond, cudaStream_t st);
 int device_sms();
+// the network's parameter buffers, checked for NaN / infinity in one launch
+struct FiniteList {
+    const void *p[64];
+    long long n[64];
+    int count;
+};
+void launch_check_finite(int prec, const FiniteList &list, int *d_err, cudaStream_t st);
 void launch_prepare_weights(int prec, const void *src, int M, int K, int Mp, void *dst, cudaStream_t st);
+
+// error report (am_verify.cu): out[0] max |f(v)| bits, out[1] max vertex
+// error bits, out[2] vertices, out[3] vertices left out (singular), out[4] faces
+void launch_gather_keys(const uint32_t *keys, int W, const long long *ids, int count, uint32_t *out, cudaStream_t st);
+void launch_to_double(const void *src, long long n, void *dst, cudaStream_t st);
+void launch_verify(int ts_bytes, const RegionsDev &reg, const long long *ids, int count, const double *rows,
+                   const double *eq, int ALLP, int ALL, unsigned long long *out, cudaStream_t st);
 
 // mesh weld (CombineMesh)
 struct MeshDev {

@@ -16,7 +16,15 @@
 // All calls share the array and it keeps the last call's contents; nothing in
 // it has to start at zero (each call writes every scratch byte it reads).
 // Calls whose work overlaps on the GPU (other streams, or the same stream
-// from other threads without ordering) race on the array.
+// from other threads without ordering) race on the array.  The looked-up
+// address belongs to the device's current context: after cudaDeviceReset
+// (or anything else that destroys the primary context) it is stale, and the
+// entry point must not be called again in that process.
+//
+// Errors: a CUDA error already pending on the calling thread is reported as
+// AM_ERR_CUDA without launching anything and is left pending for its owner;
+// otherwise the status covers this call's launches only.  A non-null stream
+// must belong to the current device (AM_ERR_INVALID_ARGUMENT otherwise).
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -74,8 +82,15 @@ extern "C" int am_compose_rows_noalloc(const int32_t *nodesnum, int num_nodes, c
     used += align256(sizeof(uint64_t) * (size_t)count);
     if (used > kScratchBytes) return AM_ERR_CAPACITY; // network + states larger than the 8 MiB scratch
 
+    // an error left pending by earlier work is not ours to report or to clear
+    if (cudaPeekAtLastError() != cudaSuccess) return AM_ERR_CUDA;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return AM_ERR_CUDA;
+    if (stream) {
+        int sdev = -1;
+        if (cudaStreamGetDevice((cudaStream_t)stream, &sdev) != cudaSuccess) return AM_ERR_INVALID_ARGUMENT;
+        if (sdev != dev) return AM_ERR_INVALID_ARGUMENT;
+    }
     unsigned char *scratch = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_scratch_mu);
@@ -123,5 +138,6 @@ extern "C" int am_compose_rows_noalloc(const int32_t *nodesnum, int num_nodes, c
     ch.eq = eq;
     ch.rec = nullptr;
     launch_compose(kFloat32, net, reg, ch, iso, st);
+    // nothing was pending at entry: an error now comes from these launches
     return cudaGetLastError() == cudaSuccess ? AM_OK : AM_ERR_CUDA;
 }

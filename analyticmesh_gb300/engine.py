@@ -156,6 +156,14 @@ class Engine:
         _lib.check(_lib.lib().am_get_stats(self.h, C.byref(s)), self.h)
         return s.as_dict()
 
+    def error_report(self, sample_regions: int = 4096) -> dict:
+        """am_error_report: max |f(v)| and the largest vertex error of the
+        last result against FP64, over ``sample_regions`` evenly spaced
+        regions (0: all)."""
+        r = _lib.AmErrorReport()
+        _lib.check(_lib.lib().am_error_report(self.h, int(sample_regions), C.byref(r)), self.h)
+        return r.as_dict()
+
     def combine(self, scale=1.0, center=(0.0, 0.0, 0.0)) -> Mesh:
         c3 = (C.c_double * 3)(*[float(x) for x in center])
         L = _lib.lib()

@@ -90,9 +90,35 @@ typedef struct {
     double polygon_ms;
     double frontier_ms;
     int64_t kernel_launches;  /* launches inside the marching loop */
+    /* error report: set by am_error_report, zero until it has run on this result */
+    double max_abs_f;         /* max |f(v)| over the checked faces' vertices, f in FP64 */
+    double max_vertex_err;    /* max |v - v64| (largest coordinate) against FP64 re-solves */
+    int64_t error_faces;      /* faces checked */
+    /* mixed form: walk predicates near zero re-taken in FP64 (a constraint
+     * value within 1e-6 |w| of zero, or two hit candidates that close) */
+    int64_t num_fp64_predicates;
 } am_stats;
 
 int am_get_stats(const am_engine *engine, am_stats *out);
+
+/* Error report of the last result (no counterpart in the reference, which
+ * reports timings only, backend/main.py:368-373): sample_regions regions,
+ * evenly spaced over the region store (0 or more than there are: all), are
+ * composed again in FP64 from the engine's parameters (converted exactly to
+ * double), and every vertex of their faces is checked: |f(v)| with f the FP64
+ * face plane (the network's value at v minus the level), and the distance
+ * (largest coordinate) from v to the FP64 solve of the three planes it lies
+ * on.  Also stored in the am_stats fields max_abs_f, max_vertex_err and
+ * error_faces.
+ * Runs on the engine's stream after the marching, outside its am_time. */
+typedef struct {
+    int64_t faces;            /* faces checked (regions of the sample with >= 3 vertices, closed walk) */
+    int64_t vertices;         /* their vertices */
+    int64_t vertices_singular;/* vertices whose FP64 system is singular (left out of max_vertex_err) */
+    double max_abs_f;
+    double max_vertex_err;
+} am_error_report_t;
+int am_error_report(am_engine *engine, int64_t sample_regions, am_error_report_t *out);
 
 /* Welded mesh after am_combine_mesh: verts mesh_num_verts x 3, face_sizes
  * mesh_num_faces, face_indices mesh_num_indices (host memory). */
@@ -160,9 +186,20 @@ typedef enum {
                                  operand of a tile stays in shared memory for all layers, 2 it is rebuilt
                                  per 64-deep block from the rows just written (wider tiles for layers of
                                  256 units and more).  Both give the same bits. */
-    AM_OPT_FACE_WARPS = 7     /* warps per face polygon: 0 (default) automatic (one for narrow networks,
+    AM_OPT_FACE_WARPS = 7,    /* warps per face polygon: 0 (default) automatic (one for narrow networks,
                                  up to eight for wide ones, whose rows leave room for few faces per SM),
                                  or 1, 2, 4, 8.  The warps of a face split the walk's scan over the rows. */
+    AM_OPT_TABLE_SLOTS = 8,   /* region hash table: 0 (default) sized by the engine (load factor <= 1/2,
+                                 grown as regions are found); n > 0: fixed at n slots rounded up to a
+                                 power of two, never grown.  A run that outgrows a fixed table returns
+                                 AM_ERR_TABLE_FULL when an insert reaches the probe bound, where the
+                                 reference's try_insert spins forever (backend/inc/hash.h:56-64); the
+                                 engine stays usable. */
+    AM_OPT_INJECT_ERROR = 9   /* test hook: device error bits (1 table full, 2 device wait limit,
+                                 4 capacity, 8 non-finite parameters) written into the run's control
+                                 block after the seed phase, as a kernel would leave them, so that the
+                                 wave loop's error decoding can be tested without a device fault.
+                                 0 (default) off; stays set until set to 0. */
 } am_option;
 int am_set_option(am_engine *engine, int option, int64_t value);
 
@@ -201,8 +238,13 @@ int am_selftest_umma_bmn(const void *A, const void *B, void *D, int N, int K);
  * Scratch (transposed weights, packed keys) is one static 8 MiB device array
  * in the library, held by every GPU that loads it until exit; the first call
  * on each device looks its address up and should come before any stream
- * capture.  Calls share that array, so calls that overlap on the GPU race.
- * A network plus states larger than the array returns AM_ERR_CAPACITY. */
+ * capture, and a device reset (cudaDeviceReset) makes that address stale, so
+ * the entry point must not be used after one.  Calls share that array, so
+ * calls that overlap on the GPU race.  A network plus states larger than the
+ * array returns AM_ERR_CAPACITY; rows or eq not 16-byte aligned, or a stream
+ * of another device, AM_ERR_INVALID_ARGUMENT.  A CUDA error already pending on
+ * the calling thread is returned as AM_ERR_CUDA before anything is launched
+ * and is not cleared. */
 int am_compose_rows_noalloc(const int32_t *nodesnum, int num_nodes, const float *const *weights,
                             const float *const *biases, const uint8_t *states, int count, double iso,
                             float *rows, float *eq, void *stream);

@@ -153,6 +153,11 @@ def _key_sets(a, b):
             np.setdiff1d(ub, ua, assume_unique=True).size)
 
 
+def region_keys(r):
+    """The set of activation states a run visited (bytes of the packed bits)."""
+    return frozenset(bytes(k) for k in np.unique(_row_keys(r.bits)))
+
+
 def canonical(a_regions, b_regions, tol=1e-5):
     """Order-free comparison.  Returns a dict of counts."""
     na_, nb_, only_a, only_b = _key_sets(a_regions, b_regions)

@@ -9,8 +9,10 @@ import pytest
 import torch
 
 from analyticmesh_gb300 import load_model, onnx_io, save_model, workloads as wl
+from oracle import build_ref
 
-CHAIR = "/root/reference/examples/chair.onnx"
+# the reference checkout (AM_REFERENCE_ROOT): its shipped network, when present
+CHAIR = os.path.join(build_ref.REF_ROOT, "examples", "chair.onnx")
 
 
 @pytest.mark.parametrize("factory", [
