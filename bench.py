@@ -1,13 +1,19 @@
 """Analytic Marching throughput on GB300: analytic faces / second.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--form mixed|float32|float64] [--workload sphere|deep|large_skip|polytope]
+                    [--form mixed|float32|float64]
+                    [--workload large_skip|sphere|deep|polytope|batched]
 
-Workload (default): the sphere network 3 -> [128] x 4 -> 1 (geometric init,
-seed 1, fp32 weights) with 1024 dichotomy seed points (seed 1); synthetic,
-seeded.  One step = one complete Analytic Marching of that network (every
-region visited, every face polygon built), the window of the reference's
-am_time (backend/main.py:455-465): seed init and mesh export are outside.
+Workload (default): the largest single-GPU configuration, the skip-connected
+network 3 -> [512] x 8 -> 1 with the 3-D input added into layer 4 (geometric
+init r = 0.6 + N(0, 0.01), seed 3, fp32 weights; 4096 constraint rows per
+region, ~6.8 M regions), with 1024 dichotomy seed points (seed 1); synthetic,
+seeded.  Chosen form: mixed precision.  One step = one complete Analytic
+Marching of that network (every region visited, every face polygon built),
+the window of the reference's am_time (backend/main.py:455-465): seed init
+and mesh export are outside.  ``--workload sphere`` (3 -> [128] x 4 -> 1),
+``deep`` (3 -> [256] x 6 -> 1 at level 0.35) and ``batched`` (the networks of
+the batched configuration marched at once) select the other configurations.
 
 ``value``: faces / second with inputs resident in HBM, CUDA-event timed on
 the launching stream, L2 flushed (256 MiB write) before every timed step.
@@ -18,8 +24,14 @@ am_get_mesh).
 
 ``--impl reference`` times the reference's own marching loop compiled for the
 host cores (oracle/_ref, all host threads) on a bounded sample of the same
-workload (the first 65536 regions).  Under torchrun every rank runs an
-independent replica (the path does not shard); rank 0 prints one JSON line.
+workload (its first regions: 4096 of the skip network, 16384 of the deep one,
+65536 of the sphere).  Under torchrun every rank runs an independent replica
+(the path does not shard); rank 0 prints one JSON line.
+
+The line also carries the chosen result's error report against FP64
+(``errors``: max |f(v)| and the largest vertex error over an evenly spaced
+sample of its faces, am_error_report) and the plain FP32 form's outcome on the
+same workload (``plain_fp32_value`` or ``plain_note``), its error report too.
 """
 from __future__ import annotations
 
@@ -35,7 +47,11 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# the reference arm's bounded sample (regions per step): about 10-30 s of the
+# host cores per step
+REF_SAMPLE = {"sphere": 65536, "deep": 16384, "large_skip": 4096, "polytope": 65536}
 REF_SAMPLE_REGIONS = 65536
+ERROR_SAMPLE = 4096  # regions of the error report
 # DRAM bytes (read + write) per region of the two heavy kernels in the mixed
 # form, from one ncu capture each (--set full, dram__bytes_read.sum +
 # dram__bytes_write.sum): the sphere workload's wave of 12,672 regions and the
@@ -53,7 +69,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--form", default="mixed", choices=["mixed", "float32", "float64"])
-    p.add_argument("--workload", default="sphere", choices=["sphere", "deep", "large_skip", "polytope", "batched"])
+    p.add_argument("--workload", default="large_skip",
+                   choices=["large_skip", "sphere", "deep", "polytope", "batched"])
     p.add_argument("--nets", type=int, default=16,
                    help="batched workload: the first NETS of the 64 networks (all 64 take minutes per step)")
     p.add_argument("--seeds", type=int, default=1024)
@@ -197,7 +214,7 @@ def reference_workload(args):
     backend/main.py:437-446), the sample split evenly between them."""
     if args.workload != "batched":
         net, states, points, desc = workload(args.workload, args.seeds)
-        return [(net, states, points, REF_SAMPLE_REGIONS)], desc
+        return [(net, states, points, REF_SAMPLE[args.workload])], desc
     from analyticmesh_gb300 import workloads as wl
 
     items = []
@@ -281,20 +298,20 @@ def run_reference(args, rank, ws):
     print(json.dumps(line), flush=True)
 
 
-def cpu_baseline(net, states, points, dtype):
+def cpu_baseline(net, states, points, dtype, budget):
     """The cpu_baseline object of the bench line: the reference's loop built
-    for the host (all threads) on the first REF_SAMPLE_REGIONS regions of the
+    for the host (all threads) on the first ``budget`` regions of the
     workload, or the oracle restatement on the same sample."""
     threads = os.cpu_count() or 1
     kind = reference_kind()
     try:
-        faces, secs = reference_step([(net, states, points, REF_SAMPLE_REGIONS)], dtype, threads, kind)
+        faces, secs = reference_step([(net, states, points, budget)], dtype, threads, kind)
     except Exception:  # a reference build that loads but cannot run: the restatement instead
         kind = "port"
-        faces, secs = reference_step([(net, states, points, REF_SAMPLE_REGIONS)], dtype, threads, kind)
+        faces, secs = reference_step([(net, states, points, budget)], dtype, threads, kind)
     return {"value": faces / secs, "unit": "faces/s", "cores": threads, "kind": kind,
             "sample": "first %d regions of the workload, %s (OpenMP, %d threads)" % (
-                REF_SAMPLE_REGIONS, "reference loop built for the host" if kind == "reference"
+                budget, "reference loop built for the host" if kind == "reference"
                 else "oracle restatement", threads)}
 
 
@@ -522,14 +539,23 @@ def main():
     if roof["traffic"] is not None:
         roof["traffic_note"] = "ncu dram bytes per region of one captured wave x regions per step"
 
+    # the chosen result's error report against FP64 (an evenly spaced sample
+    # of the faces of the phase-timed run above; outside every timed region)
+    errors = eng.error_report(ERROR_SAMPLE)
+    errors["sample_regions"] = ERROR_SAMPLE
+
     # the chosen engine's stores go back before the plain form's are built
     # (large networks hold tens of GB of regions)
     eng.close()
     torch.cuda.empty_cache()
     plain = None
     plain_note = None
+    plain_errors = None
     if form != "float32":
         ep = engine.Engine("float32", net.nodes, net.arc_table, net.num_extra)
+        # a plain run that passes twice the chosen form's regions is stopped
+        # there (AM_ERR_CAPACITY) and reported as not converging
+        ep.set_option(_lib.AM_OPT_MAX_REGIONS, 2 * regions)
         try:
             W32 = [w.float() for w in W]
             B32 = [b.float() for b in B]
@@ -548,8 +574,19 @@ def main():
                 e1.synchronize()
                 pt.append(s2["num_faces"] / (e0.elapsed_time(e1) / 1e3))
             plain = statistics.mean(pt) * ws
+            plain_errors = ep.error_report(ERROR_SAMPLE)
+            plain_note = "plain FP32: %d regions, %d faces per step" % (s2["num_regions"], s2["num_faces"])
         except _lib.AmError as exc:  # e.g. the FP32 form's store outgrowing the GPU
-            plain_note = "plain FP32 run failed: %s" % str(exc)[:160]
+            if exc.status == _lib.AM_ERR_CAPACITY:
+                st2 = ep.stats()
+                plain_note = ("plain FP32 run does not converge: stopped after %d regions (the chosen form's "
+                              "march has %d); %s" % (st2["num_regions"], regions, str(exc)[:120]))
+                try:
+                    plain_errors = ep.error_report(ERROR_SAMPLE)
+                except _lib.AmError:
+                    plain_errors = None
+            else:
+                plain_note = "plain FP32 run failed: %s" % str(exc)[:160]
         finally:
             ep.close()
 
@@ -557,7 +594,8 @@ def main():
         return
     cpu = None
     if ws == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(net, states, points, "float64" if form == "float64" else "float32")
+        cpu = cpu_baseline(net, states, points, "float64" if form == "float64" else "float32",
+                           REF_SAMPLE.get(args.workload, REF_SAMPLE_REGIONS))
     line = {
         "metric": "analytic_faces_per_sec", "value": value, "unit": "faces/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
@@ -568,7 +606,8 @@ def main():
                    "regions_per_step": regions, "l2": "256 MiB flush before every timed step",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "faces/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "roofline": roof, "phases_ms": phases, "plain_fp32_value": plain, "plain_note": plain_note,
+        "roofline": roof, "phases_ms": phases, "errors": errors, "plain_fp32_value": plain,
+        "plain_note": plain_note, "plain_errors": plain_errors,
         "chosen_vs_plain": (value / plain) if plain else None, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": launches,
     }
