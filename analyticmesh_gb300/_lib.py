@@ -57,6 +57,7 @@ AM_OPT_COMPOSE_TILE = 6
 AM_OPT_FACE_WARPS = 7
 AM_OPT_TABLE_SLOTS = 8
 AM_OPT_INJECT_ERROR = 9
+AM_OPT_PRUNE_ROWS = 10
 
 # device error bits (AM_OPT_INJECT_ERROR)
 ERR_TABLE_FULL, ERR_WAIT, ERR_CAPACITY, ERR_NONFINITE = 1, 2, 4, 8

@@ -214,6 +214,7 @@ struct am_engine {
     int face_warps = 0;        // AM_OPT_FACE_WARPS: warps per face polygon, 0 automatic
     long long table_slots = 0; // AM_OPT_TABLE_SLOTS: fixed region hash table size, 0 automatic
     int inject_err = 0;        // AM_OPT_INJECT_ERROR: error bits set in the control block after the seeds
+    int prune = 1;             // AM_OPT_PRUNE_ROWS: the walk scans only the rows that can bound the face
     bool limit_hit = false;    // the last run stopped at the region limit
     bool over_limit(long long tail)
     {
@@ -374,6 +375,7 @@ struct am_engine {
         add(&prec, sizeof(prec));
         add(&chunk, sizeof(chunk));
         add(&face_warps, sizeof(face_warps));
+        add(&prune, sizeof(prune));
         add(&iso, sizeof(iso));
         add(&tol, sizeof(tol));
         add(&net, sizeof(net));
@@ -407,7 +409,7 @@ struct am_engine {
                     launch_compose_tc(net, tcnet, reg, ch, iso, d_err.as<int>(), st);
                 else
                     launch_compose(prec, net, reg, ch, iso, st);
-                launch_polygon(prec, net, reg, ch, hs, tol, face_warps, d_err.as<int>(), st);
+                launch_polygon(prec, net, reg, ch, hs, tol, face_warps, prune, d_err.as<int>(), st);
                 launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, chunk * kVMax,
                               d_tail.as<long long>(), blocksum.as<int>(), (int)(blocksum.bytes / sizeof(int)),
                               d_err.as<int>(), st);
@@ -825,7 +827,7 @@ void run_host_loop(am_engine *e)
             t_comp += ms;
             AM_CUDA(cudaEventRecord(pa, st));
         }
-        launch_polygon(prec, net, reg, ch, hs, tol, e->face_warps, e->d_err.as<int>(), st);
+        launch_polygon(prec, net, reg, ch, hs, tol, e->face_warps, e->prune, e->d_err.as<int>(), st);
         if (e->phase_timing) {
             AM_CUDA(cudaEventRecord(pb, st));
             AM_CUDA(cudaEventSynchronize(pb));
@@ -1023,6 +1025,11 @@ int am_set_option(am_engine *e, int option, int64_t value)
         if (value < 0 || value > (int64_t(1) << 40)) return AM_ERR_INVALID_ARGUMENT;
         e->table_slots = value;
         e->hcap = 0; // the next run sizes the table afresh
+        return AM_OK;
+    }
+    if (option == AM_OPT_PRUNE_ROWS) {
+        if (value != 0 && value != 1) return AM_ERR_INVALID_ARGUMENT;
+        e->prune = (int)value;
         return AM_OK;
     }
     if (option == AM_OPT_INJECT_ERROR) {

@@ -126,8 +126,10 @@ struct Tolerances {
 // launchers (stream-ordered, no synchronisation)
 void launch_compose(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, double iso,
                     cudaStream_t st);
+// prune: 1 = the walk scans only the rows that can bound the face (see
+// prune_rows), 0 = every row (the same faces)
 void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs,
-                    const Tolerances &tol, int face_warps, int *d_err, cudaStream_t st);
+                    const Tolerances &tol, int face_warps, int prune, int *d_err, cudaStream_t st);
 int polygon_face_warps(int prec, int ALLP);
 void launch_seed_pack(const uint8_t *states, int S, int N, int W, uint32_t *keys, uint64_t *hash, cudaStream_t st);
 void launch_seed_insert(const uint32_t *keys, const uint64_t *hash, int S, int W, const HashDev &hs, int32_t *rec,

@@ -171,12 +171,25 @@ __device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long 
 // step without further messages.  Warp 0 (the leader) alone re-solves the
 // vertices in the solve precision and writes the outputs.  G = 1 is the plain
 // warp per face with no barrier.
+constexpr int kListCap = 384;  // rows the pruned walk keeps at most (more: the walk scans every row)
+constexpr int kPruneMin = 96;  // fewer rows than this: no pruning
+
 template <typename TC>
 struct GroupShared {
     long long rl;   // the group's region (chunk-local)
     int done, pad;  // the leader's refinement outcome
     TC bt[2][8];    // partial minima per step parity and warp
     int bk[2][8];
+    int nlist;      // rows kept by the pruning
+    // row pruning: first the sample's extreme rows per warp and direction,
+    // then (once every warp has read those) the list of the rows kept
+    union {
+        struct {
+            TC v[8][8];
+            int16_t i[8][8];
+        } ext;
+        uint16_t list[kListCap];
+    };
 };
 
 template <typename TC>
@@ -208,8 +221,9 @@ __host__ __device__ constexpr size_t group_shared_bytes()
 // (two interleaved candidates per lane halve the compare chain), then across
 // the warp; every lane returns the warp's (t, plane), plane 0x7fffffff if none
 template <typename TC>
-__device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, int k0, int kstep, TC d0, TC d1, TC d2,
-                                         TC thr, TC c0, TC c1, TC c2, int e, int prev, TC &bt_out, int &bk_out)
+__device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, int k0,
+                                         int kstep, TC d0, TC d1, TC d2, TC thr, TC c0, TC c1, TC c2, int e, int prev,
+                                         TC &bt_out, int &bk_out)
 {
     TC bnum = TC(1), bden = TC(0), bnum1 = TC(1), bden1 = TC(0);
     int bk = 0x7fffffff, bk1 = 0x7fffffff;
@@ -226,12 +240,21 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, int k0
             bi = k;
         }
     };
-    int k = k0;
-    for (; k + kstep < ALL; k += 2 * kstep) {
-        consider(k, bnum, bden, bk);
-        consider(k + kstep, bnum1, bden1, bk1);
+    if (list) { // the rows that survived pruning
+        int j = k0;
+        for (; j + kstep < nlist; j += 2 * kstep) {
+            consider(list[j], bnum, bden, bk);
+            consider(list[j + kstep], bnum1, bden1, bk1);
+        }
+        if (j < nlist) consider(list[j], bnum, bden, bk);
+    } else {
+        int k = k0;
+        for (; k + kstep < ALL; k += 2 * kstep) {
+            consider(k, bnum, bden, bk);
+            consider(k + kstep, bnum1, bden1, bk1);
+        }
+        if (k < ALL) consider(k, bnum, bden, bk);
     }
-    if (k < ALL) consider(k, bnum, bden, bk);
     {
         const TC lhs = bnum1 * bden, rhs = bnum * bden1;
         if (bk1 != 0x7fffffff && (lhs < rhs || (lhs == rhs && bk1 < bk))) {
@@ -260,9 +283,9 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, int k0
 // step j's hit plane (sbk) and merge decision (sdec, 0 append, 1 merge with
 // the previous vertex, 2 merge with the first), nsteps the steps taken.
 template <typename TC, typename TS, bool kGroup>
-__device__ void walk(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TS *eqv, const TS *p, int s, TC par_eps,
-                     TS same_eps, int lane, TS &vx, TS &vy, TS &vz, int &ve, int &n, bool &closed, int8_t &status,
-                     int &sbk, int &sdec, int &nsteps, const Grp<TC> &g)
+__device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
+                     const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy, TS &vz,
+                     int &ve, int &n, bool &closed, int8_t &status, int &sbk, int &sdec, int &nsteps, const Grp<TC> &g)
 {
     TC cx = 0, cy = 0, cz = 0; // the vertex rounded to the scan precision
     vx = vy = vz = TS(0);
@@ -286,8 +309,8 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, con
         // first hit along the edge line, the scan split over the group
         TC bt;
         int bk;
-        hit_scan<TC>(rows, ALL, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1, d2, thr, c0, c1, c2, e,
-                     prev, bt, bk);
+        hit_scan<TC>(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1, d2, thr,
+                     c0, c1, c2, e, prev, bt, bk);
         if (kGroup) {
             const int par = step & 1;
             if (lane == 0) {
@@ -394,9 +417,9 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, con
 // than 32 steps, met a vertex that is not finite in TS, or a decision comes
 // out differently in TS.
 template <typename TC, typename TS, bool kGroup>
-__device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TS *eqv, const TS *p, int s,
-                             TC par_eps, TS same_eps, int lane, TS &vx, TS &vy, TS &vz, int &ve, int &n, bool &closed,
-                             int8_t &status, const Grp<TC> &g)
+__device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
+                             const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy,
+                             TS &vz, int &ve, int &n, bool &closed, int8_t &status, const Grp<TC> &g)
 {
     const unsigned full = 0xffffffffu;
     const TC eqf[4] = {eqc.x, eqc.y, eqc.z, eqc.w};
@@ -405,8 +428,8 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &
     int fve, fn, sbk, sdec, nsteps;
     bool fclosed;
     int8_t fst = kOk;
-    walk<TC, TC, kGroup>(rows, ALL, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz, fve, fn, fclosed, fst,
-                         sbk, sdec, nsteps, g);
+    walk<TC, TC, kGroup>(rows, ALL, list, nlist, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz, fve, fn,
+                         fclosed, fst, sbk, sdec, nsteps, g);
     if (fst != kOk || !fclosed || nsteps < 1 || nsteps > 32) return false;
     if (kGroup && g.gw != 0) return true; // the leader refines; the caller shares its outcome
 
@@ -491,13 +514,183 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &
     return true;
 }
 
+// Row pruning before the walk.  The face polygon is the intersection of the
+// half-planes the rows cut out of the face plane.  In coordinates u of that
+// plane centred on the start point p, row k reads m_k . u <= c_k, with
+// c_k = -(w_k . p + b_k) the distance from p to the row's plane (the rows are
+// normalised) and m_k the in-plane part of w_k.  For c_k > 0 the row's dual
+// point q_k = m_k / c_k lies strictly inside the convex hull of the other dual
+// points and the origin exactly when the row's line misses the polygon (the
+// polar of a polygon around p): such a row is never the first plane the walk
+// hits on an edge.  A sample of the rows (every eighth) gives, for eight
+// directions, the extreme dual points; their convex polygon lies inside that
+// hull, and so does the circle of radius r around the origin inscribed in it.
+// Every row whose dual point lies inside 0.98 r -- computed with c_k lowered
+// by a bound on its rounding -- is dropped, and the walk scans the kept rows
+// only, so its decisions (the first hit, ties to the lower row) are those of
+// the scan over every row.  Rows through or near p and rows that are not
+// finite are always kept; the sample uses only rows with c_k well above the
+// rounding bound, so that its dual points are accurate.  Returns the number
+// of kept rows (their indices in sh->list), or -1 -- the walk scans every
+// row -- when the sample gives no circle or more than kListCap rows are kept.
+template <typename TC, bool kGroup>
+__device__ int prune_rows(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TC *pc, int lane,
+                          const Grp<TC> &g)
+{
+    const unsigned full = 0xffffffffu;
+    GroupShared<TC> *sh = g.sh;
+    const int w = kGroup ? g.gw : 0, G = kGroup ? g.G : 1;
+    // orthonormal basis (e1, e2) of the face plane
+    TC nx = eqc.x, ny = eqc.y, nz = eqc.z;
+    const TC nn = nx * nx + ny * ny + nz * nz;
+    if (!(nn > TC(0)) || !finite_bits(nn)) return -1; // uniform: every lane reads the same plane
+    const TC inv = rsqrt(nn);
+    nx *= inv;
+    ny *= inv;
+    nz *= inv;
+    const TC ax = (fabs(nx) <= fabs(ny) && fabs(nx) <= fabs(nz)) ? TC(1) : TC(0);
+    const TC ay = (ax == TC(0) && fabs(ny) <= fabs(nz)) ? TC(1) : TC(0);
+    const TC az = (ax == TC(0) && ay == TC(0)) ? TC(1) : TC(0);
+    TC e1x = ay * nz - az * ny, e1y = az * nx - ax * nz, e1z = ax * ny - ay * nx;
+    const TC i1 = rsqrt(e1x * e1x + e1y * e1y + e1z * e1z);
+    e1x *= i1;
+    e1y *= i1;
+    e1z *= i1;
+    const TC e2x = ny * e1z - nz * e1y, e2y = nz * e1x - nx * e1z, e2z = nx * e1y - ny * e1x;
+    const TC p0 = pc[0], p1 = pc[1], p2 = pc[2];
+    // rounding of c_k in TC, and the sample's floor on c_k
+    const TC dc = (sizeof(TC) == 4 ? TC(1e-6) : TC(1e-14)) * (TC(1) + fabs(p0) + fabs(p1) + fabs(p2));
+    const TC cmin = TC(1000) * dc;
+    if (w == 0 && lane == 0) sh->nlist = 0;
+
+    // sample: the extreme dual point in directions 0, 45, ..., 315 degrees
+    TC bv[8];
+    int bi[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+        bv[m] = TC(-INFINITY);
+        bi[m] = 0x7fffffff;
+    }
+    for (int k = 8 * (32 * w + lane); k < ALL; k += 8 * 32 * G) {
+        const vec4_t<TC> r = rows[k];
+        const TC c = -(r.x * p0 + r.y * p1 + r.z * p2 + r.w);
+        if (!(c >= cmin) || !finite_bits(c)) continue;
+        const TC ic = TC(1) / c;
+        const TC qx = (r.x * e1x + r.y * e1y + r.z * e1z) * ic;
+        const TC qy = (r.x * e2x + r.y * e2y + r.z * e2z) * ic;
+        const TC v[8] = {qx, qx + qy, qy, qy - qx, -qx, -qx - qy, -qy, qx - qy};
+#pragma unroll
+        for (int m = 0; m < 8; ++m)
+            if (v[m] > bv[m]) {
+                bv[m] = v[m];
+                bi[m] = k;
+            }
+    }
+#pragma unroll
+    for (int m = 0; m < 8; ++m)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const TC ov = __shfl_xor_sync(full, bv[m], o);
+            const int oi = __shfl_xor_sync(full, bi[m], o);
+            if (ov > bv[m] || (ov == bv[m] && oi < bi[m])) {
+                bv[m] = ov;
+                bi[m] = oi;
+            }
+        }
+    if (kGroup) {
+        if (lane < 8) {
+            TC v = bv[0];
+            int i = bi[0];
+#pragma unroll
+            for (int m = 1; m < 8; ++m)
+                if (lane == m) v = bv[m], i = bi[m];
+            sh->ext.v[w][lane] = v;
+            sh->ext.i[w][lane] = (int16_t)(i == 0x7fffffff ? -1 : i);
+        }
+        g.sync();
+#pragma unroll
+        for (int m = 0; m < 8; ++m) {
+            bv[m] = TC(-INFINITY);
+            bi[m] = 0x7fffffff;
+            for (int u = 0; u < G; ++u) {
+                const TC ov = sh->ext.v[u][m];
+                const int oi = sh->ext.i[u][m] < 0 ? 0x7fffffff : (int)sh->ext.i[u][m];
+                if (ov > bv[m] || (ov == bv[m] && oi < bi[m])) {
+                    bv[m] = ov;
+                    bi[m] = oi;
+                }
+            }
+        }
+        g.sync(); // every warp has read the extremes: the list may overwrite them
+    }
+    // the extreme points in counter-clockwise order (lane m < 8: direction
+    // m), and the radius of the circle around the origin inscribed in their
+    // polygon: the smallest distance from the origin to an edge, which must
+    // have the origin strictly on its left
+    bool ok = true;
+#pragma unroll
+    for (int m = 0; m < 8; ++m) ok = ok && bi[m] != 0x7fffffff;
+    if (!ok) return -1; // a direction without a sampled row: the polygon may be open that way
+    int mine = bi[0];
+#pragma unroll
+    for (int m = 1; m < 8; ++m)
+        if ((lane & 7) == m) mine = bi[m];
+    const vec4_t<TC> er = rows[mine];
+    const TC eic = TC(1) / -(er.x * p0 + er.y * p1 + er.z * p2 + er.w);
+    const TC qx = (er.x * e1x + er.y * e1y + er.z * e1z) * eic;
+    const TC qy = (er.x * e2x + er.y * e2y + er.z * e2z) * eic;
+    const int nxt = (lane + 1) & 7;
+    const TC qx1 = __shfl_sync(full, qx, nxt), qy1 = __shfl_sync(full, qy, nxt);
+    const int bi1 = __shfl_sync(full, mine, nxt);
+    const bool edge = lane < 8 && bi1 != mine;
+    const TC dx = qx1 - qx, dy = qy1 - qy;
+    const TC cr = dy * qx - dx * qy; // (E1 - E0) x (O - E0)
+    const TC len = sqrt(dx * dx + dy * dy);
+    const bool bad = edge && !(cr > TC(0) && len > TC(0));
+    TC rad = edge && !bad ? cr / len : TC(INFINITY);
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) rad = fmin(rad, __shfl_xor_sync(full, rad, o));
+    rad = __shfl_sync(full, rad, 0);
+    const int edges = __popc(__ballot_sync(full, edge));
+    if (__any_sync(full, bad) || edges < 3 || !(rad > TC(0)) || !finite_bits(rad)) return -1;
+    const TC re = TC(0.98) * rad;
+    const TC re2 = re * re;
+
+    // every row: keep those whose dual point may lie outside the circle
+    for (int k0 = 32 * w; k0 < ALL; k0 += 32 * G) {
+        const int k = k0 + lane;
+        bool keep = false;
+        if (k < ALL) {
+            const vec4_t<TC> r = rows[k];
+            const TC c = -(r.x * p0 + r.y * p1 + r.z * p2 + r.w) - dc;
+            const TC m1 = r.x * e1x + r.y * e1y + r.z * e1z;
+            const TC m2 = r.x * e2x + r.y * e2y + r.z * e2z;
+            keep = !(c > TC(0)) || !(m1 * m1 + m2 * m2 < re2 * c * c);
+        }
+        const unsigned b = __ballot_sync(full, keep);
+        if (b) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(&sh->nlist, __popc(b));
+            base = __shfl_sync(full, base, 0);
+            const int pos = base + __popc(b & ((1u << lane) - 1u));
+            if (keep && pos < kListCap) sh->list[pos] = (uint16_t)k;
+        }
+    }
+    if (kGroup)
+        g.sync();
+    else
+        __syncwarp();
+    const int nl = sh->nlist;
+    return nl <= kListCap ? nl : -1;
+}
+
 // Rows are staged normalised (|w| = 1, zero rows become 0.x + sign(b) inf):
 // signed geometric distances are then plain dot products, the same quantity
 // the reference's feasibility test computes as (w.x + b) * rsqrt(|w|^2)
 // (kernel.h:729-795).  TC is the scan precision, TS the solve precision.
 template <typename TC, typename TS, bool kGroup>
 __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
-                                                      int G_, int *err)
+                                                      int G_, int prune, int *err)
 {
     const int G = kGroup ? G_ : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -515,6 +708,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
     g.bar = 1 + gid;
     g.sh = reinterpret_cast<GroupShared<TC> *>(smem_raw + (size_t)F * net.ALLP * sizeof(vec4_t<TC>) +
                                                (size_t)gid * group_shared_bytes<TC>());
+    // (the group's shared block also holds the pruning list: one per face)
     const TC eps = (TC)tol.eps, par_eps = (TC)tol.par_eps;
     const TS same_eps = (TS)tol.same_eps;
 
@@ -638,6 +832,15 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             if (s < 0) status = kNoStart;
         }
 
+        // ---------------------------------------------------- row pruning
+        int nlist = -1;
+        const uint16_t *list = nullptr;
+        if (s >= 0 && prune && ALL >= kPruneMin) {
+            const TC pc3[3] = {(TC)p[0], (TC)p[1], (TC)p[2]};
+            nlist = prune_rows<TC, kGroup>(rows, ALL, eqc, pc3, lane, g);
+            if (nlist >= 0) list = g.sh->list;
+        }
+
         // ---------------------------------------------------- walk
         // lane i holds vertex i and the plane of the edge leaving it
         TS vx = 0, vy = 0, vz = 0;
@@ -648,8 +851,8 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             bool done = false;
             if (sizeof(TS) > sizeof(TC)) // scan-precision walk, vertices refined in the solve precision
             {
-                done = walk_refined<TC, TS, kGroup>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve,
-                                                    n, closed, status, g);
+                done = walk_refined<TC, TS, kGroup>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx,
+                                                    vy, vz, ve, n, closed, status, g);
                 if (kGroup) { // the leader's outcome for the group
                     if (g.gw == 0 && lane == 0) g.sh->done = done ? 1 : 0;
                     g.sync();
@@ -658,8 +861,8 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             }
             if (!done) {
                 int sbk, sdec, nsteps;
-                walk<TC, TS, kGroup>(rows, ALL, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n, closed,
-                                     status, sbk, sdec, nsteps, g);
+                walk<TC, TS, kGroup>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n,
+                                     closed, status, sbk, sdec, nsteps, g);
             }
         }
         if (kGroup && g.gw != 0) continue; // the leader writes the face
@@ -718,11 +921,12 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
 } // namespace
 
 // Faces per block for G warps per face: as many as keep a block's rows
-// within 72 KB (three blocks per SM), at most 8 / G, a power of two.
-int polygon_faces_per_block(size_t row_bytes, int G)
+// (and each face's shared block) within 73 KB (three blocks per SM), at most
+// 8 / G, a power of two.
+int polygon_faces_per_block(size_t face_bytes, int G)
 {
     int F = 1;
-    while (2 * F * G <= 8 && (size_t)(2 * F) * row_bytes <= 72u * 1024u) F *= 2;
+    while (2 * F * G <= 8 && (size_t)(2 * F) * face_bytes <= 73u * 1024u) F *= 2;
     return F;
 }
 
@@ -730,18 +934,19 @@ int polygon_faces_per_block(size_t row_bytes, int G)
 // and the warps of a face as the rows allow.
 int polygon_face_warps(int prec, int ALLP)
 {
-    const size_t row_bytes = (prec == kFloat64 ? sizeof(double4) : sizeof(float4)) * (size_t)ALLP;
-    const int F = polygon_faces_per_block(row_bytes, 1);
+    const size_t face_bytes = prec == kFloat64 ? sizeof(double4) * (size_t)ALLP + group_shared_bytes<double>()
+                                               : sizeof(float4) * (size_t)ALLP + group_shared_bytes<float>();
+    const int F = polygon_faces_per_block(face_bytes, 1);
     return 8 / F;
 }
 
 template <typename TC, typename TS>
 void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs, const Tolerances &tol,
-                int *d_err, int G, cudaStream_t st)
+                int *d_err, int G, int prune, cudaStream_t st)
 {
     const size_t row_bytes = sizeof(vec4_t<TC>) * (size_t)net.ALLP;
-    const int F = polygon_faces_per_block(row_bytes, G);
-    const size_t smem = row_bytes * F + (G > 1 ? group_shared_bytes<TC>() * F : 0);
+    const int F = polygon_faces_per_block(row_bytes + group_shared_bytes<TC>(), G);
+    const size_t smem = (row_bytes + group_shared_bytes<TC>()) * F;
     auto k = G > 1 ? polygon_kernel<TC, TS, true> : polygon_kernel<TC, TS, false>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int sms = device_sms();
@@ -755,20 +960,20 @@ void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, co
         const long long need = (ch.count + F - 1) / F;
         grid = (int)std::min<long long>(need, (long long)sms * 16);
     }
-    k<<<grid, threads, smem, st>>>(net, reg, ch, hs, tol, G, d_err);
+    k<<<grid, threads, smem, st>>>(net, reg, ch, hs, tol, G, prune, d_err);
 }
 
 void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs,
-                    const Tolerances &tol, int face_warps, int *d_err, cudaStream_t st)
+                    const Tolerances &tol, int face_warps, int prune, int *d_err, cudaStream_t st)
 {
     if (!ch.ctl && ch.count <= 0) return;
     const int G = face_warps > 0 ? face_warps : polygon_face_warps(prec, net.ALLP);
     if (prec == kFloat64)
-        launch_one<double, double>(net, reg, ch, hs, tol, d_err, G, st);
+        launch_one<double, double>(net, reg, ch, hs, tol, d_err, G, prune, st);
     else if (prec == kMixed)
-        launch_one<float, double>(net, reg, ch, hs, tol, d_err, G, st);
+        launch_one<float, double>(net, reg, ch, hs, tol, d_err, G, prune, st);
     else
-        launch_one<float, float>(net, reg, ch, hs, tol, d_err, G, st);
+        launch_one<float, float>(net, reg, ch, hs, tol, d_err, G, prune, st);
 }
 
 } // namespace am

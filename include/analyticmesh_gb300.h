@@ -195,11 +195,15 @@ typedef enum {
                                  AM_ERR_TABLE_FULL when an insert reaches the probe bound, where the
                                  reference's try_insert spins forever (backend/inc/hash.h:56-64); the
                                  engine stays usable. */
-    AM_OPT_INJECT_ERROR = 9   /* test hook: device error bits (1 table full, 2 device wait limit,
+    AM_OPT_INJECT_ERROR = 9,  /* test hook: device error bits (1 table full, 2 device wait limit,
                                  4 capacity, 8 non-finite parameters) written into the run's control
                                  block after the seed phase, as a kernel would leave them, so that the
                                  wave loop's error decoding can be tested without a device fault.
                                  0 (default) off; stays set until set to 0. */
+    AM_OPT_PRUNE_ROWS = 10    /* 1 (default): before walking a face, drop the constraint rows whose line
+                                 provably misses the polygon (a dual-space test against a sample of the
+                                 rows), so that the walk scans a few dozen rows per step instead of all;
+                                 0: every row.  Both give the same faces. */
 } am_option;
 int am_set_option(am_engine *engine, int option, int64_t value);
 
