@@ -23,7 +23,7 @@ class AmStats(C.Structure):
         ("am_time_ms", C.c_double), ("compose_ms", C.c_double), ("polygon_ms", C.c_double),
         ("frontier_ms", C.c_double), ("kernel_launches", C.c_int64),
         ("max_abs_f", C.c_double), ("max_vertex_err", C.c_double), ("error_faces", C.c_int64),
-        ("num_fp64_predicates", C.c_int64),
+        ("num_fp64_walks", C.c_int64),
     ]
 
     def as_dict(self):

@@ -347,6 +347,10 @@ struct am_engine {
         if (e & kErrCapacity) throw Failure{AM_ERR_CAPACITY, "region store capacity exceeded"};
     }
     WaveCtl *ctl() const { return (WaveCtl *)d_tail.p; }
+    unsigned long long *fp64_counter() const
+    {
+        return (unsigned long long *)((char *)d_tail.p + kStatsOff) + kFp64Slot;
+    }
 
     void drop_graph()
     {
@@ -409,7 +413,7 @@ struct am_engine {
                     launch_compose_tc(net, tcnet, reg, ch, iso, d_err.as<int>(), st);
                 else
                     launch_compose(prec, net, reg, ch, iso, st);
-                launch_polygon(prec, net, reg, ch, hs, tol, face_warps, prune, d_err.as<int>(), st);
+                launch_polygon(prec, net, reg, ch, hs, tol, face_warps, prune, fp64_counter(), d_err.as<int>(), st);
                 launch_append(0, prec, net, reg, ch, hs, nullptr, nullptr, nullptr, chunk * kVMax,
                               d_tail.as<long long>(), blocksum.as<int>(), (int)(blocksum.bytes / sizeof(int)),
                               d_err.as<int>(), st);
@@ -698,6 +702,7 @@ void run_begin(am_engine *e, const RunArgs &a)
     e->hcap = 0;
     e->stats = am_stats{};
     AM_CUDA(cudaMemsetAsync(e->d_tail.p, 0, sizeof(long long), st));
+    AM_CUDA(cudaMemsetAsync(e->fp64_counter(), 0, sizeof(unsigned long long), st));
     const int chunk = e->default_chunk();
     e->ensure_chunk(std::min(chunk, std::max(S, 1024)));
     const long long first_wave = e->lean ? std::min<long long>(chunk, 4ll * S + 1024) : chunk;
@@ -827,7 +832,8 @@ void run_host_loop(am_engine *e)
             t_comp += ms;
             AM_CUDA(cudaEventRecord(pa, st));
         }
-        launch_polygon(prec, net, reg, ch, hs, tol, e->face_warps, e->prune, e->d_err.as<int>(), st);
+        launch_polygon(prec, net, reg, ch, hs, tol, e->face_warps, e->prune, e->fp64_counter(), e->d_err.as<int>(),
+                       st);
         if (e->phase_timing) {
             AM_CUDA(cudaEventRecord(pb, st));
             AM_CUDA(cudaEventSynchronize(pb));
@@ -892,7 +898,7 @@ void run_end(am_engine *e)
         const unsigned long long *h = (const unsigned long long *)((const char *)e->h_ctl + kStatsOff);
         AM_CUDA(cudaMemsetAsync(d, 0, kStatsCount * sizeof(unsigned long long), st));
         launch_region_stats(e->nv.as<int32_t>(), e->status.as<int8_t>(), tail, d, st);
-        AM_CUDA(cudaMemcpyAsync((char *)e->h_ctl + kStatsOff, d, kStatsCount * sizeof(unsigned long long),
+        AM_CUDA(cudaMemcpyAsync((char *)e->h_ctl + kStatsOff, d, (kStatsCount + 1) * sizeof(unsigned long long),
                                 cudaMemcpyDeviceToHost, st));
         AM_CUDA(cudaStreamSynchronize(st));
         sx.num_faces = (int64_t)h[0];
@@ -901,6 +907,7 @@ void run_end(am_engine *e)
         sx.num_open = (int64_t)h[2 + kOpen - 1];
         sx.num_truncated = (int64_t)h[2 + kTruncated - 1];
         sx.num_singular = (int64_t)h[2 + kSingular - 1];
+        sx.num_fp64_walks = (int64_t)h[kFp64Slot];
     }
     e->flip = flip_insideout ? 1 : 0;
     e->iso = iso;

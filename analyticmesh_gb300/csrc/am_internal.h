@@ -89,10 +89,12 @@ struct WaveCtl {
 
 // the control block's device / pinned allocation: WaveCtl, then the run's
 // statistics counters (faces, largest polygon, then one count per status
-// kNoStart .. kSingular)
+// kNoStart .. kSingular, reduced at the end of a run), then the count of
+// faces walked again with FP64 predicates (accumulated during the run)
 constexpr int kStatsCount = 6;
+constexpr int kFp64Slot = kStatsCount;
 constexpr size_t kStatsOff = (sizeof(WaveCtl) + 15) / 16 * 16;
-constexpr size_t kCtlBytes = kStatsOff + kStatsCount * sizeof(unsigned long long);
+constexpr size_t kCtlBytes = kStatsOff + (kStatsCount + 1) * sizeof(unsigned long long);
 
 struct ChunkDev {
     long long head;     // first rid of the chunk
@@ -128,8 +130,10 @@ void launch_compose(int prec, const NetDev &net, const RegionsDev &reg, const Ch
                     cudaStream_t st);
 // prune: 1 = the walk scans only the rows that can bound the face (see
 // prune_rows), 0 = every row (the same faces)
+// nfp64: counts the faces the mixed form walks again with FP64 predicates
 void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs,
-                    const Tolerances &tol, int face_warps, int prune, int *d_err, cudaStream_t st);
+                    const Tolerances &tol, int face_warps, int prune, unsigned long long *nfp64, int *d_err,
+                    cudaStream_t st);
 int polygon_face_warps(int prec, int ALLP);
 void launch_seed_pack(const uint8_t *states, int S, int N, int W, uint32_t *keys, uint64_t *hash, cudaStream_t st);
 void launch_seed_insert(const uint32_t *keys, const uint64_t *hash, int S, int W, const HashDev &hs, int32_t *rec,

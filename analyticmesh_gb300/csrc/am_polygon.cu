@@ -177,8 +177,9 @@ constexpr int kPruneMin = 96;  // fewer rows than this: no pruning
 template <typename TC>
 struct GroupShared {
     long long rl;   // the group's region (chunk-local)
-    int done, pad;  // the leader's refinement outcome
+    int done, near; // the leader's refinement outcome; a warp met a row near a vertex
     TC bt[2][8];    // partial minima per step parity and warp
+    double btd[2][8]; // the same for a scan in FP64 over FP32 rows
     int bk[2][8];
     int nlist;      // rows kept by the pruning
     // row pruning: first the sample's extreme rows per warp and direction,
@@ -216,24 +217,39 @@ __host__ __device__ constexpr size_t group_shared_bytes()
     return (sizeof(GroupShared<TC>) + 15) / 16 * 16;
 }
 
-// first hit along the edge line over rows k0, k0 + kstep, ...: min over
-// crossing planes of t = max(0, -g) / a, compared as fractions within a lane
-// (two interleaved candidates per lane halve the compare chain), then across
-// the warp; every lane returns the warp's (t, plane), plane 0x7fffffff if none
-template <typename TC>
-__device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, int k0,
-                                         int kstep, TC d0, TC d1, TC d2, TC thr, TC c0, TC c1, TC c2, int e, int prev,
-                                         TC &bt_out, int &bk_out)
+// first hit along the edge line over rows k0, k0 + kstep, ... (of the kept
+// list, when the rows were pruned): min over crossing planes of
+// t = max(0, -g) / a, compared as fractions within a lane (two interleaved
+// candidates per lane halve the compare chain), then across the warp; every
+// lane returns the warp's (t, plane), plane 0x7fffffff if none.  The rows are
+// TR, the arithmetic TA (FP64 over FP32 rows for the mixed form's FP64
+// predicates).  kNear: `near` is set when a row other than the two the
+// current point lies on has |g| < 1e-6 there (the rows are normalised, so g
+// is a distance): a predicate near zero, which the mixed form takes again in
+// FP64.
+template <typename TR, typename TA, bool kNear>
+__device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const uint16_t *list, int nlist, int k0,
+                                         int kstep, TA d0, TA d1, TA d2, TA thr, TA c0, TA c1, TA c2, int e, int prev,
+                                         TA &bt_out, int &bk_out, bool &near)
 {
-    TC bnum = TC(1), bden = TC(0), bnum1 = TC(1), bden1 = TC(0);
+    TA bnum = TA(1), bden = TA(0), bnum1 = TA(1), bden1 = TA(0);
     int bk = 0x7fffffff, bk1 = 0x7fffffff;
-    auto consider = [&](int k, TC &bn, TC &bd, int &bi) {
-        const vec4_t<TC> r = rows[k];
-        const TC a = r.x * d0 + r.y * d1 + r.z * d2;
-        if (!(a > thr) || k == e || k == prev) return;
-        TC num = -(r.x * c0 + r.y * c1 + r.z * c2 + r.w);
-        num = num > TC(0) ? num : TC(0);
-        const TC lhs = num * bd, rhs = bn * a;
+    bool nr = false;
+    auto consider = [&](int k, TA &bn, TA &bd, int &bi) {
+        const vec4_t<TR> r = rows[k];
+        const TA rx = (TA)r.x, ry = (TA)r.y, rz = (TA)r.z, rw = (TA)r.w;
+        const TA a = rx * d0 + ry * d1 + rz * d2;
+        TA num;
+        if (kNear) {
+            num = -(rx * c0 + ry * c1 + rz * c2 + rw);
+            nr = nr || (fabs(num) < TA(1e-6) && k != e && k != prev);
+            if (!(a > thr) || k == e || k == prev) return;
+        } else {
+            if (!(a > thr) || k == e || k == prev) return;
+            num = -(rx * c0 + ry * c1 + rz * c2 + rw);
+        }
+        num = num > TA(0) ? num : TA(0);
+        const TA lhs = num * bd, rhs = bn * a;
         if (lhs < rhs || (lhs == rhs && k < bi)) {
             bn = num;
             bd = a;
@@ -256,17 +272,17 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, const 
         if (k < ALL) consider(k, bnum, bden, bk);
     }
     {
-        const TC lhs = bnum1 * bden, rhs = bnum * bden1;
+        const TA lhs = bnum1 * bden, rhs = bnum * bden1;
         if (bk1 != 0x7fffffff && (lhs < rhs || (lhs == rhs && bk1 < bk))) {
             bnum = bnum1;
             bden = bden1;
             bk = bk1;
         }
     }
-    TC bt = bk == 0x7fffffff ? TC(INFINITY) : bnum / bden;
+    TA bt = bk == 0x7fffffff ? TA(INFINITY) : bnum / bden;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const TC ot = __shfl_xor_sync(0xffffffffu, bt, o);
+        const TA ot = __shfl_xor_sync(0xffffffffu, bt, o);
         const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
         if (ot < bt || (ot == bt && ok < bk)) {
             bt = ot;
@@ -275,18 +291,23 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TC> *rows, int ALL, const 
     }
     bt_out = bt;
     bk_out = bk;
+    if (kNear) near = __any_sync(0xffffffffu, nr);
 }
 
-// One face walk: from the start plane s, ray shooting along each edge line
-// in the scan precision TC, vertices solved in TS.  Lane i ends with vertex
-// i (vx, vy, vz) and the plane of the edge leaving it (ve); lane j records
-// step j's hit plane (sbk) and merge decision (sdec, 0 append, 1 merge with
-// the previous vertex, 2 merge with the first), nsteps the steps taken.
-template <typename TC, typename TS, bool kGroup>
+// One face walk: from the start plane s, ray shooting along each edge line,
+// the scan in TA (TC, or TS for the mixed form's FP64 predicates), vertices
+// solved in TS.  Lane i ends with vertex i (vx, vy, vz) and the plane of the
+// edge leaving it (ve); lane j records step j's hit plane (sbk) and merge
+// decision (sdec, 0 append, 1 merge with the previous vertex, 2 merge with
+// the first), nsteps the steps taken.  kNear: `near` (this warp) is set when
+// some step's scan met a row within 1e-6 of the current point.
+template <typename TC, typename TS, bool kGroup, typename TA = TC, bool kNear = false>
 __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
                      const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy, TS &vz,
-                     int &ve, int &n, bool &closed, int8_t &status, int &sbk, int &sdec, int &nsteps, const Grp<TC> &g)
+                     int &ve, int &n, bool &closed, int8_t &status, int &sbk, int &sdec, int &nsteps, const Grp<TC> &g,
+                     bool *near = nullptr)
 {
+    constexpr bool kWide = sizeof(TA) > sizeof(TC); // FP64 scan over FP32 rows
     TC cx = 0, cy = 0, cz = 0; // the vertex rounded to the scan precision
     vx = vy = vz = TS(0);
     ve = -1;
@@ -296,32 +317,42 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
     sdec = 0;
     nsteps = 0;
     int e = s, prev = -1;
-    TC curc[3] = {(TC)p[0], (TC)p[1], (TC)p[2]}; // current point, scan precision
+    bool any_near = false;
+    TA cur[3] = {(TA)p[0], (TA)p[1], (TA)p[2]}; // current point, scan arithmetic
     for (int step = 0; step < kWalkSteps; ++step) {
         nsteps = step + 1;
         // direction of the edge line: w_eq x w_e (counter-clockwise about w_eq)
         const vec4_t<TC> ref_ = rows[e];
-        const TC d0 = eqc.y * ref_.z - eqc.z * ref_.y;
-        const TC d1 = eqc.z * ref_.x - eqc.x * ref_.z;
-        const TC d2 = eqc.x * ref_.y - eqc.y * ref_.x;
-        const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
-        const TC c0 = curc[0], c1 = curc[1], c2 = curc[2];
+        TA q0, q1, q2;
+        if (kWide) {
+            q0 = (TA)eqv[0], q1 = (TA)eqv[1], q2 = (TA)eqv[2];
+        } else {
+            q0 = (TA)eqc.x, q1 = (TA)eqc.y, q2 = (TA)eqc.z;
+        }
+        const TA rx = (TA)ref_.x, ry = (TA)ref_.y, rz = (TA)ref_.z;
+        const TA d0 = q1 * rz - q2 * ry;
+        const TA d1 = q2 * rx - q0 * rz;
+        const TA d2 = q0 * ry - q1 * rx;
+        const TA thr = (TA)par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
         // first hit along the edge line, the scan split over the group
-        TC bt;
+        TA bt;
         int bk;
-        hit_scan<TC>(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1, d2, thr,
-                     c0, c1, c2, e, prev, bt, bk);
+        bool nr = false;
+        hit_scan<TC, TA, kNear>(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1,
+                                d2, thr, cur[0], cur[1], cur[2], e, prev, bt, bk, nr);
+        any_near = any_near || nr;
         if (kGroup) {
             const int par = step & 1;
+            TA *sbt = kWide ? (TA *)&g.sh->btd[par][0] : (TA *)&g.sh->bt[par][0];
             if (lane == 0) {
-                g.sh->bt[par][g.gw] = bt;
+                sbt[g.gw] = bt;
                 g.sh->bk[par][g.gw] = bk;
             }
             g.sync();
-            bt = g.sh->bt[par][0];
+            bt = sbt[0];
             bk = g.sh->bk[par][0];
             for (int w = 1; w < g.G; ++w) {
-                const TC ot = g.sh->bt[par][w];
+                const TA ot = sbt[w];
                 const int ok = g.sh->bk[par][w];
                 if (ot < bt || (ot == bt && ok < bk)) {
                     bt = ot;
@@ -400,11 +431,18 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
         }
         prev = e;
         e = bk;
-        curc[0] = Vc[0];
-        curc[1] = Vc[1];
-        curc[2] = Vc[2];
+        if (kWide) {
+            cur[0] = (TA)V[0];
+            cur[1] = (TA)V[1];
+            cur[2] = (TA)V[2];
+        } else {
+            cur[0] = (TA)Vc[0];
+            cur[1] = (TA)Vc[1];
+            cur[2] = (TA)Vc[2];
+        }
     }
     if (!closed && status == kOk) status = kTruncated;
+    if (near) *near = any_near;
 }
 
 // Mixed form: the walk runs in the scan precision TC (solves included, as the
@@ -412,9 +450,11 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
 // vertex (the four Cramer determinants), eight vertices per warp instruction
 // -- and every merge decision is taken again on the TS vertices.  When all
 // decisions agree, the face is the TS walk's face: the same hit planes, the
-// same TS vertices.  Returns false, and the caller walks again with a TS
-// solve at every step, when the TC walk did not close normally, took more
-// than 32 steps, met a vertex that is not finite in TS, or a decision comes
+// same TS vertices.  Returns false, and the caller walks again with every
+// predicate and every solve in TS, when a scan met a row within 1e-6 of the
+// current point other than the two it lies on (a sign or feasibility test
+// near zero), when the TC walk did not close normally, took more than 32
+// steps or met a vertex that is not finite in TS, or when a decision comes
 // out differently in TS.
 template <typename TC, typename TS, bool kGroup>
 __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
@@ -428,9 +468,16 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *li
     int fve, fn, sbk, sdec, nsteps;
     bool fclosed;
     int8_t fst = kOk;
-    walk<TC, TC, kGroup>(rows, ALL, list, nlist, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz, fve, fn,
-                         fclosed, fst, sbk, sdec, nsteps, g);
-    if (fst != kOk || !fclosed || nsteps < 1 || nsteps > 32) return false;
+    bool near = false;
+    walk<TC, TC, kGroup, TC, true>(rows, ALL, list, nlist, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz,
+                                   fve, fn, fclosed, fst, sbk, sdec, nsteps, g, &near);
+    if (kGroup) { // a row near a vertex in any warp's share of the scan
+        if (near && lane == 0) atomicOr(&g.sh->near, 1);
+        g.sync();
+        near = g.sh->near != 0;
+    }
+    // a predicate near zero: the caller walks again with FP64 predicates
+    if (near || fst != kOk || !fclosed || nsteps < 1 || nsteps > 32) return false;
     if (kGroup && g.gw != 0) return true; // the leader refines; the caller shares its outcome
 
     // step j's vertex in TS, into lane j
@@ -690,7 +737,7 @@ __device__ int prune_rows(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc
 // (kernel.h:729-795).  TC is the scan precision, TS the solve precision.
 template <typename TC, typename TS, bool kGroup>
 __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
-                                                      int G_, int prune, int *err)
+                                                      int G_, int prune, unsigned long long *nfp64, int *err)
 {
     const int G = kGroup ? G_ : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -723,7 +770,10 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         long long rl;
         if (g.gw == 0) {
             rl = ch.ctl ? next_work(ch.ctl, lane) : rl_next;
-            if (kGroup && lane == 0) g.sh->rl = rl;
+            if (kGroup && lane == 0) {
+                g.sh->rl = rl;
+                g.sh->near = 0;
+            }
         }
         rl_next += (long long)gridDim.x * F;
         if (kGroup) {
@@ -861,8 +911,14 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             }
             if (!done) {
                 int sbk, sdec, nsteps;
-                walk<TC, TS, kGroup>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve, n,
-                                     closed, status, sbk, sdec, nsteps, g);
+                if (sizeof(TS) > sizeof(TC)) { // mixed form: FP64 predicates and FP64 solves
+                    if (g.gw == 0 && lane == 0) atomicAdd(nfp64, 1ull);
+                    walk<TC, TS, kGroup, TS, false>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx,
+                                                    vy, vz, ve, n, closed, status, sbk, sdec, nsteps, g);
+                } else {
+                    walk<TC, TS, kGroup>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve,
+                                         n, closed, status, sbk, sdec, nsteps, g);
+                }
             }
         }
         if (kGroup && g.gw != 0) continue; // the leader writes the face
@@ -942,7 +998,7 @@ int polygon_face_warps(int prec, int ALLP)
 
 template <typename TC, typename TS>
 void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs, const Tolerances &tol,
-                int *d_err, int G, int prune, cudaStream_t st)
+                int *d_err, int G, int prune, unsigned long long *nfp64, cudaStream_t st)
 {
     const size_t row_bytes = sizeof(vec4_t<TC>) * (size_t)net.ALLP;
     const int F = polygon_faces_per_block(row_bytes + group_shared_bytes<TC>(), G);
@@ -960,20 +1016,21 @@ void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, co
         const long long need = (ch.count + F - 1) / F;
         grid = (int)std::min<long long>(need, (long long)sms * 16);
     }
-    k<<<grid, threads, smem, st>>>(net, reg, ch, hs, tol, G, prune, d_err);
+    k<<<grid, threads, smem, st>>>(net, reg, ch, hs, tol, G, prune, nfp64, d_err);
 }
 
 void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs,
-                    const Tolerances &tol, int face_warps, int prune, int *d_err, cudaStream_t st)
+                    const Tolerances &tol, int face_warps, int prune, unsigned long long *nfp64, int *d_err,
+                    cudaStream_t st)
 {
     if (!ch.ctl && ch.count <= 0) return;
     const int G = face_warps > 0 ? face_warps : polygon_face_warps(prec, net.ALLP);
     if (prec == kFloat64)
-        launch_one<double, double>(net, reg, ch, hs, tol, d_err, G, prune, st);
+        launch_one<double, double>(net, reg, ch, hs, tol, d_err, G, prune, nfp64, st);
     else if (prec == kMixed)
-        launch_one<float, double>(net, reg, ch, hs, tol, d_err, G, prune, st);
+        launch_one<float, double>(net, reg, ch, hs, tol, d_err, G, prune, nfp64, st);
     else
-        launch_one<float, float>(net, reg, ch, hs, tol, d_err, G, prune, st);
+        launch_one<float, float>(net, reg, ch, hs, tol, d_err, G, prune, nfp64, st);
 }
 
 } // namespace am

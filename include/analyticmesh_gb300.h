@@ -94,9 +94,10 @@ typedef struct {
     double max_abs_f;         /* max |f(v)| over the checked faces' vertices, f in FP64 */
     double max_vertex_err;    /* max |v - v64| (largest coordinate) against FP64 re-solves */
     int64_t error_faces;      /* faces checked */
-    /* mixed form: walk predicates near zero re-taken in FP64 (a constraint
-     * value within 1e-6 |w| of zero, or two hit candidates that close) */
-    int64_t num_fp64_predicates;
+    /* mixed form: faces walked again with every sign and feasibility
+     * predicate in FP64, because a constraint value came within 1e-6 |w| of
+     * zero at a vertex (or a decision differed between FP32 and FP64) */
+    int64_t num_fp64_walks;
 } am_stats;
 
 int am_get_stats(const am_engine *engine, am_stats *out);
