@@ -136,9 +136,10 @@ __device__ __forceinline__ unsigned long long load_slot(const unsigned long long
 
 // Does the key stored behind slot value `cur` equal parent_key ^ flip(k)?
 // Region entries (tag 0) point at the region store; candidate entries (tag 1)
-// carry (chunk-local parent, plane) and point at the parent's key.
-__device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long long head, int ALL, int W,
-                            const uint32_t *pkey, int k)
+// carry (chunk-local parent, plane) and point at the parent's key.  The whole
+// warp compares: lane l takes words l, l + 32, ..., all loads issued at once.
+__device__ bool warp_key_matches(unsigned long long cur, const RegionsDev &reg, long long head, int ALL, int W,
+                                 const uint32_t *pkey, int k, int lane)
 {
     const uint32_t id = (uint32_t)cur & 0x7fffffffu;
     const bool cand = (cur >> 31) & 1ull;
@@ -154,12 +155,54 @@ __device__ bool key_matches(unsigned long long cur, const RegionsDev &reg, long 
     const uint32_t kb = 1u << (k & 31);
     const int ow = ok2 >= 0 ? (ok2 >> 5) : -1;
     const uint32_t ob = ok2 >= 0 ? (1u << (ok2 & 31)) : 0u;
-    for (int w = 0; w < W; ++w) {
-        uint32_t a = pkey[w] ^ (w == kw ? kb : 0u);
-        uint32_t b = other[w] ^ (w == ow ? ob : 0u);
-        if (a != b) return false;
+    bool differ = false;
+    for (int w = lane; w < W; w += 32) {
+        const uint32_t a = pkey[w] ^ (w == kw ? kb : 0u);
+        const uint32_t b = other[w] ^ (w == ow ? ob : 0u);
+        differ = differ || a != b;
     }
-    return true;
+    return !__any_sync(0xffffffffu, differ);
+}
+
+// Insert the neighbour across plane k (parent key pkey with bit k flipped)
+// into the region hash set; the whole warp works on it, lane 0 owning the
+// slot operations.  Returns the slot claimed for a new candidate (or the
+// candidate slot this one now shares), -1 when the key is a committed
+// region already.  Among equal candidate keys the smallest (parent, plane)
+// id stays in the slot, so the result does not depend on timing.
+__device__ int warp_insert(const RegionsDev &reg, const HashDev &hs, long long head, int ALL, int W, const uint32_t *pkey,
+                           uint64_t phash, long long rl, int k, int lane, int *err)
+{
+    const unsigned full = 0xffffffffu;
+    const uint64_t h = flip_hash(phash, pkey[k >> 5], k);
+    const uint32_t fp = fp_of(h);
+    const uint32_t myid = (uint32_t)(rl * ALL + k);
+    const unsigned long long mine = slot_value(fp, 1, myid);
+    unsigned long long slot = h & hs.mask;
+    for (int probe = 0; probe < kMaxProbes; ++probe) {
+        unsigned long long cur = 0ull;
+        int claimed = 0;
+        if (lane == 0) {
+            cur = load_slot(hs.slots + slot);
+            if (cur == kEmpty) {
+                const unsigned long long old = atomicCAS(hs.slots + slot, kEmpty, mine);
+                claimed = old == kEmpty;
+                cur = old;
+            }
+        }
+        cur = __shfl_sync(full, cur, 0);
+        if (__shfl_sync(full, claimed, 0)) return (int)slot;
+        if ((uint32_t)(cur >> 32) == fp && warp_key_matches(cur, reg, head, ALL, W, pkey, k, lane)) {
+            if ((cur >> 31) & 1ull) {
+                if (lane == 0) atomicMin(hs.slots + slot, mine);
+                return (int)slot;
+            }
+            return -1;
+        }
+        slot = (slot + (unsigned long long)probe + 1ull) & hs.mask;
+    }
+    if (lane == 0) atomicOr(err, kErrTableFull);
+    return -1;
 }
 
 // A face belongs to a group of G warps (G = 1, 2, 4 or 8; wide networks use
@@ -294,6 +337,70 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const 
     if (kNear) near = __any_sync(0xffffffffu, nr);
 }
 
+// The mixed form's scan with FP64 predicates (over FP32 rows): every row is
+// evaluated in FP32 from the FP32 copy of the current point, and again in
+// FP64 from the FP64 current point when that value is within 2e-6 of zero --
+// a sign or feasibility decision near zero, taken in FP64.  The first hit is
+// the smaller of the FP32 candidates' best and the FP64 candidates' best,
+// compared in FP64, ties to the lower row.
+__device__ __forceinline__ void hit_scan_wide(const float4 *rows, int ALL, const uint16_t *list, int nlist, int k0,
+                                              int kstep, float d0, float d1, float d2, float thr, float c0, float c1,
+                                              float c2, double D0, double D1, double D2, double thr64, double C0,
+                                              double C1, double C2, int e, int prev, double &bt_out, int &bk_out)
+{
+    float bnum = 1.f, bden = 0.f;
+    int bk = 0x7fffffff;
+    double tn = INFINITY;
+    int tk = 0x7fffffff;
+    auto consider = [&](int k) {
+        if (k == e || k == prev) return;
+        const float4 r = rows[k];
+        const float g = r.x * c0 + r.y * c1 + r.z * c2 + r.w;
+        if (fabsf(g) < 2e-6f) {
+            const double a = (double)r.x * D0 + (double)r.y * D1 + (double)r.z * D2;
+            if (!(a > thr64)) return;
+            double num = -((double)r.x * C0 + (double)r.y * C1 + (double)r.z * C2 + (double)r.w);
+            num = num > 0.0 ? num : 0.0;
+            const double t = num / a;
+            if (t < tn || (t == tn && k < tk)) {
+                tn = t;
+                tk = k;
+            }
+            return;
+        }
+        const float a = r.x * d0 + r.y * d1 + r.z * d2;
+        if (!(a > thr)) return;
+        const float num = -g > 0.f ? -g : 0.f;
+        const float lhs = num * bden, rhs = bnum * a;
+        if (lhs < rhs || (lhs == rhs && k < bk)) {
+            bnum = num;
+            bden = a;
+            bk = k;
+        }
+    };
+    if (list) {
+        for (int j = k0; j < nlist; j += kstep) consider(list[j]);
+    } else {
+        for (int k = k0; k < ALL; k += kstep) consider(k);
+    }
+    double bt = bk == 0x7fffffff ? INFINITY : (double)bnum / (double)bden;
+    if (tk != 0x7fffffff && (tn < bt || (tn == bt && tk < bk))) {
+        bt = tn;
+        bk = tk;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ot = __shfl_xor_sync(0xffffffffu, bt, o);
+        const int ok = __shfl_xor_sync(0xffffffffu, bk, o);
+        if (ot < bt || (ot == bt && ok < bk)) {
+            bt = ot;
+            bk = ok;
+        }
+    }
+    bt_out = bt;
+    bk_out = bk;
+}
+
 // One face walk: from the start plane s, ray shooting along each edge line,
 // the scan in TA (TC, or TS for the mixed form's FP64 predicates), vertices
 // solved in TS.  Lane i ends with vertex i (vx, vy, vz) and the plane of the
@@ -318,29 +425,32 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
     nsteps = 0;
     int e = s, prev = -1;
     bool any_near = false;
-    TA cur[3] = {(TA)p[0], (TA)p[1], (TA)p[2]}; // current point, scan arithmetic
+    TC curc[3] = {(TC)p[0], (TC)p[1], (TC)p[2]}; // current point, scan precision
+    TA cur[3] = {(TA)p[0], (TA)p[1], (TA)p[2]};  // and in FP64 for the wide scan
     for (int step = 0; step < kWalkSteps; ++step) {
         nsteps = step + 1;
         // direction of the edge line: w_eq x w_e (counter-clockwise about w_eq)
         const vec4_t<TC> ref_ = rows[e];
-        TA q0, q1, q2;
-        if (kWide) {
-            q0 = (TA)eqv[0], q1 = (TA)eqv[1], q2 = (TA)eqv[2];
-        } else {
-            q0 = (TA)eqc.x, q1 = (TA)eqc.y, q2 = (TA)eqc.z;
-        }
-        const TA rx = (TA)ref_.x, ry = (TA)ref_.y, rz = (TA)ref_.z;
-        const TA d0 = q1 * rz - q2 * ry;
-        const TA d1 = q2 * rx - q0 * rz;
-        const TA d2 = q0 * ry - q1 * rx;
-        const TA thr = (TA)par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        const TC d0 = eqc.y * ref_.z - eqc.z * ref_.y;
+        const TC d1 = eqc.z * ref_.x - eqc.x * ref_.z;
+        const TC d2 = eqc.x * ref_.y - eqc.y * ref_.x;
+        const TC thr = par_eps * sqrt(d0 * d0 + d1 * d1 + d2 * d2);
         // first hit along the edge line, the scan split over the group
         TA bt;
         int bk;
-        bool nr = false;
-        hit_scan<TC, TA, kNear>(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1,
-                                d2, thr, cur[0], cur[1], cur[2], e, prev, bt, bk, nr);
-        any_near = any_near || nr;
+        if constexpr (kWide) {
+            const TA q0 = (TA)eqv[0], q1 = (TA)eqv[1], q2 = (TA)eqv[2];
+            const TA rx = (TA)ref_.x, ry = (TA)ref_.y, rz = (TA)ref_.z;
+            const TA D0 = q1 * rz - q2 * ry, D1 = q2 * rx - q0 * rz, D2 = q0 * ry - q1 * rx;
+            const TA thr64 = (TA)par_eps * sqrt(D0 * D0 + D1 * D1 + D2 * D2);
+            hit_scan_wide(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1, d2,
+                          thr, curc[0], curc[1], curc[2], D0, D1, D2, thr64, cur[0], cur[1], cur[2], e, prev, bt, bk);
+        } else {
+            bool nr = false;
+            hit_scan<TC, TC, kNear>(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0,
+                                    d1, d2, thr, curc[0], curc[1], curc[2], e, prev, bt, bk, nr);
+            any_near = any_near || nr;
+        }
         if (kGroup) {
             const int par = step & 1;
             TA *sbt = kWide ? (TA *)&g.sh->btd[par][0] : (TA *)&g.sh->bt[par][0];
@@ -431,14 +541,13 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
         }
         prev = e;
         e = bk;
+        curc[0] = Vc[0];
+        curc[1] = Vc[1];
+        curc[2] = Vc[2];
         if (kWide) {
             cur[0] = (TA)V[0];
             cur[1] = (TA)V[1];
             cur[2] = (TA)V[2];
-        } else {
-            cur[0] = (TA)Vc[0];
-            cur[1] = (TA)Vc[1];
-            cur[2] = (TA)Vc[2];
         }
     }
     if (!closed && status == kOk) status = kTruncated;
@@ -937,37 +1046,18 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         }
 
         // ---------------------------------------------------- neighbours
+        // one neighbour after the other, each inserted by the whole warp
         int rec = -1;
         const uint32_t *pkey = reg.keys + (size_t)rid * W;
         const bool spawn = lane < n && ve >= 0 && ve < N && (closed || lane < n - 1) && !(!is_seed && ve == s);
-        if (spawn) {
-            const int k = ve;
-            const uint64_t h = flip_hash(reg.hash[rid], pkey[k >> 5], k);
-            const uint32_t fp = fp_of(h);
-            const uint32_t myid = (uint32_t)(rl * ALL + k);
-            const unsigned long long mine = slot_value(fp, 1, myid);
-            unsigned long long slot = h & hs.mask;
-            int probe = 0;
-            for (; probe < kMaxProbes; ++probe) {
-                unsigned long long cur = load_slot(hs.slots + slot);
-                if (cur == kEmpty) {
-                    const unsigned long long old = atomicCAS(hs.slots + slot, kEmpty, mine);
-                    if (old == kEmpty) {
-                        rec = (int)slot;
-                        break;
-                    }
-                    cur = old;
-                }
-                if ((uint32_t)(cur >> 32) == fp && key_matches(cur, reg, head, ALL, W, pkey, k)) {
-                    if ((cur >> 31) & 1ull) {
-                        atomicMin(hs.slots + slot, mine);
-                        rec = (int)slot;
-                    }
-                    break;
-                }
-                slot = (slot + (unsigned long long)probe + 1ull) & hs.mask;
-            }
-            if (probe == kMaxProbes) atomicOr(err, kErrTableFull);
+        unsigned todo = __ballot_sync(0xffffffffu, spawn);
+        const uint64_t phash = reg.hash[rid];
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1u;
+            const int k = __shfl_sync(0xffffffffu, ve, src);
+            const int got = warp_insert(reg, hs, head, ALL, W, pkey, phash, rl, k, lane, err);
+            if (lane == src) rec = got;
         }
         if (lane < kVMax) ch.rec[(size_t)rl * kVMax + lane] = rec;
         __syncwarp();
