@@ -209,25 +209,31 @@ __device__ int total_blocks(const NetDev &net, const TcNet &tc)
     return n;
 }
 
-// Weight-block pipeline, driven by thread 0: stage h % nstage receives block
-// h once block h - nstage's products have completed (done barrier); block
-// h's products wait for its bytes (full barrier).  Phase parity of either
-// barrier for block h is (h / nstage) & 1.  h counts on across the CTA's
-// tiles, so the next tile's first blocks load during this tile's last layer.
+// Weight-block pipeline.  A copy warp (its lane 0) streams every weight block
+// of the CTA's tiles, in the order the products consume them: block h goes
+// into stage h % nstage once block h - nstage's products have completed (done
+// barrier).  Thread 0 issues the products of block h once its bytes have
+// landed (full barrier).  Phase parity of either barrier for block h is
+// (h / nstage) & 1.  h counts on across the CTA's tiles, so the next tile's
+// first blocks load during this tile's last layer and every layer's first
+// blocks during the previous layer's epilogue.  (Measured on GB300: with the
+// copies issued by thread 0 between its products, each block cost it a wait
+// for the previous block's products before the refill, and the tensor pipe
+// stood idle most of the time.)
 //
 // Every wait is bounded.  A wait that runs out sets the error bit kErrWait
-// and the CTA's abort flag: from then on thread 0 issues no copy and no
-// product, the other threads skip the epilogues, and before the CTA returns
-// thread 0 waits (again bounded) for the copies and products already in
-// flight, so that nothing lands in shared memory or TMEM after the CTA has
-// released them.  The host reports kErrWait as a failed run.
+// and the CTA's abort flag: from then on no copy and no product is issued,
+// the other threads skip the epilogues, and before the CTA returns the copy
+// warp waits (again bounded) for its copies in flight and thread 0 for the
+// products in flight, so that nothing lands in shared memory or TMEM after
+// the CTA has released them.  The host reports kErrWait as a failed run.
 struct WPipe {
     uint64_t *full, *done;
     uint8_t *ws;
-    int nstage, total, issued;
+    int nstage, total;
     int *err;
     int per_tile;          // blocks one tile consumes; the sequence repeats per tile
-    int consumed;          // blocks whose bytes were observed and whose products were issued
+    int consumed;          // (thread 0) blocks whose products were issued
     volatile int *abort;   // the CTA's abort flag (shared memory)
 };
 
@@ -239,24 +245,28 @@ __device__ __forceinline__ bool wp_wait(WPipe &p, uint64_t *bar, uint32_t parity
     return false;
 }
 
-// copy the next weight block into its stage; false (nothing issued) once the
-// CTA is aborting
-__device__ bool wp_issue(WPipe &p, const NetDev &net, const TcNet &tc)
+// (the copy warp's lane 0) every weight block of the CTA's tiles, nstage
+// blocks ahead of the products at most
+__device__ void wp_produce(WPipe &p, const NetDev &net, const TcNet &tc)
 {
-    if (*p.abort) return false;
-    const int h = p.issued, s = h % p.nstage;
-    if (h >= p.nstage && !wp_wait(p, p.done + s, (uint32_t)((h - p.nstage) / p.nstage) & 1u)) return false;
-    umma::mbar_expect_tx(p.full + s, (uint32_t)kWBlockBytes);
-    umma::bulk_g2s(p.ws + (size_t)s * kWBlockBytes, block_ptr(net, tc, h % p.per_tile), (uint32_t)kWBlockBytes,
-                   p.full + s);
-    p.issued = h + 1;
-    return true;
+    int last[4] = {-1, -1, -1, -1}; // the last block copied into each stage
+    for (int h = 0; h < p.total; ++h) {
+        const int s = h % p.nstage;
+        if (*p.abort) break;
+        if (h >= p.nstage && !wp_wait(p, p.done + s, (uint32_t)((h - p.nstage) / p.nstage) & 1u)) break;
+        umma::mbar_expect_tx(p.full + s, (uint32_t)kWBlockBytes);
+        umma::bulk_g2s(p.ws + (size_t)s * kWBlockBytes, block_ptr(net, tc, h % p.per_tile), (uint32_t)kWBlockBytes,
+                       p.full + s);
+        last[s] = h;
+    }
+    // nothing lands in shared memory after the CTA has left (bounded)
+    for (int s = 0; s < p.nstage; ++s)
+        if (last[s] >= 0) umma::mbar_wait(p.full + s, (uint32_t)(last[s] / p.nstage) & 1u, kWaitIters);
 }
 
 // (thread 0) D[mt] (+)= M . X over all K blocks of the operand in shared
 // memory: six products per K step (terms t, u of weight 2^-8(t+u), t + u <= 2)
-__device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const TcMat &m, int mtiles, const XOp &X,
-                           uint32_t tmem, bool first, int &g)
+__device__ void gemm_issue(WPipe &p, const TcMat &m, int mtiles, const XOp &X, uint32_t tmem, bool first, int &g)
 {
     const int ncols = X.ncols;
     const uint32_t idesc = X.idesc();
@@ -264,7 +274,7 @@ __device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const T
     const int kblocks = m.Kp / 64;
     for (int mt = 0; mt < mtiles; ++mt) {
         for (int kb = 0; kb < kblocks; ++kb) {
-            if (p.issued <= g && !wp_issue(p, net, tc)) return;
+            if (*p.abort) return;
             const int s = g % p.nstage;
             if (!wp_wait(p, p.full + s, (uint32_t)(g / p.nstage) & 1u)) return;
             umma::fence_after();
@@ -288,26 +298,20 @@ __device__ void gemm_issue(WPipe &p, const NetDev &net, const TcNet &tc, const T
                         ++q;
                     }
             }
-            umma::commit(umma::smem_addr(p.done + s));
+            umma::commit(umma::smem_addr(p.done + s)); // frees the stage for the copy warp
             p.consumed = g + 1;
-            // refill the stage freed by the previous block
-            while (p.issued < p.total && p.issued <= g + p.nstage - 1 && wp_issue(p, net, tc)) {
-            }
             ++g;
         }
     }
 }
 
-// (thread 0) after the last block of a layer: wait until its products are in
-// TMEM, then start the next layer's blocks so they land during the epilogue
-__device__ void gemm_finish(WPipe &p, const NetDev &net, const TcNet &tc, int g)
+// (thread 0) after the last block of a layer: wait until its products are in TMEM
+__device__ void gemm_finish(WPipe &p, int g)
 {
     if (*p.abort) return;
     const int last = g - 1;
     if (!wp_wait(p, p.done + last % p.nstage, (uint32_t)(last / p.nstage) & 1u)) return;
     umma::fence_before();
-    while (p.issued < p.total && p.issued <= last + p.nstage && wp_issue(p, net, tc)) {
-    }
 }
 
 // (every thread, after the block barrier that follows gemm_finish) observe
@@ -318,15 +322,16 @@ __device__ __forceinline__ void gemm_observe(const WPipe &p, int last)
     umma::fence_after();
 }
 
-// (thread 0, aborting CTA) wait, bounded, for the copies issued but never
-// observed and for the products of the last committed block
+// (thread 0, aborting CTA) wait, bounded, for the products of the last
+// committed block
 __device__ void wp_drain(WPipe &p)
 {
-    for (int h = p.consumed; h < p.issued; ++h)
-        umma::mbar_wait(p.full + h % p.nstage, (uint32_t)(h / p.nstage) & 1u, kWaitIters);
     if (p.consumed > 0)
         umma::mbar_wait(p.done + (p.consumed - 1) % p.nstage, (uint32_t)((p.consumed - 1) / p.nstage) & 1u, kWaitIters);
 }
+
+// the 512 threads of the resident tile (not the copy warp)
+__device__ __forceinline__ void bar_main() { asm volatile("bar.sync 2, %0;" ::"r"(kThreads) : "memory"); }
 
 // words between two regions' keys in shared memory: odd, so that lanes
 // reading consecutive regions' bits hit distinct banks
@@ -341,14 +346,15 @@ __host__ __device__ __forceinline__ int tile_cols(int count, int slots, int ncol
     return ncols < 16 ? 16 : (ncols > ncols_max ? ncols_max : ncols);
 }
 
-__global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcNet tc, RegionsDev reg, ChunkDev ch,
+__global__ void __launch_bounds__(kThreads + 32, 1) compose_tc_kernel(NetDev net, TcNet tc, RegionsDev reg, ChunkDev ch,
                                                                   float iso, int slots, int *err)
 {
     extern __shared__ uint8_t smem_raw[];
     __shared__ uint64_t bars[4];
     __shared__ uint32_t tslot;
     __shared__ int s_last;
-    __shared__ int s_abort; // set by thread 0 when a pipeline wait runs out
+    __shared__ int s_abort; // a pipeline wait ran out (thread 0 or the copy warp)
+    __shared__ int s_stop;  // thread 0's view of it, published before a tile barrier: uniform
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     long long head;
     int count;
@@ -379,26 +385,31 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
     float *wls = reinterpret_cast<float *>(w0s + net.nodes[1]);
     float *fsum = reinterpret_cast<float *>(reinterpret_cast<uintptr_t>(wls + net.nodes[net.n_lin - 1] + 3) & ~(uintptr_t)15);
 
-    WPipe pp{bars, bars + 2, ws, tc.nstage, 0, 0, err, 1, 0, &s_abort};
+    WPipe pp{bars, bars + 2, ws, tc.nstage, 0, err, 1, 0, &s_abort};
+    pp.per_tile = total_blocks(net, tc);
+    pp.total = pp.per_tile * mytiles;
     if (tid == 0) {
         s_abort = 0;
+        s_stop = 0;
         for (int b = 0; b < 4; ++b) umma::mbar_init(bars + b, 1);
         umma::fence_mbar_init();
-        pp.per_tile = total_blocks(net, tc);
-        pp.total = pp.per_tile * mytiles;
-        // the first weight blocks do not depend on the tile: start them now
-        while (pp.issued < pp.total && pp.issued < pp.nstage && wp_issue(pp, net, tc)) {
-        }
     }
     if (warp == 0) umma::tmem_alloc(&tslot, (uint32_t)tmem_cols);
     {
         const float *W0 = (const float *)net.W0;
         const float *b0 = (const float *)net.bias[0];
-        for (int m = tid; m < net.nodes[1]; m += kThreads)
+        for (int m = tid; tid < kThreads && m < net.nodes[1]; m += kThreads)
             w0s[m] = make_float4(W0[3 * m], W0[3 * m + 1], W0[3 * m + 2], b0[m]);
         const int il = net.n_lin - 1;
         const float *wl = (const float *)net.Wt[il]; // [K][Mp], column 0
-        for (int k = tid; k < net.nodes[il]; k += kThreads) wls[k] = wl[(size_t)k * net.Mp[il]];
+        for (int k = tid; tid < kThreads && k < net.nodes[il]; k += kThreads) wls[k] = wl[(size_t)k * net.Mp[il]];
+    }
+    __syncthreads(); // barriers initialised, for the copy warp too
+    if (warp == kThreads / 32) { // the copy warp: the weight blocks of every tile
+        if (lane == 0) wp_produce(pp, net, tc);
+        __syncwarp();
+        __syncthreads(); // the tile threads' last barrier
+        return;
     }
     int g = 0; // next weight block (thread 0)
     // epilogue: warp w reads TMEM lanes 32 (w % 4).. and every (kThreads / 128)-th column block
@@ -409,10 +420,10 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         const int nreg = (int)min((long long)R, (long long)count - rl0);
         float *cons = (float *)ch.cons + (size_t)rl0 * rstride;
         const uint32_t *gkeys = reg.keys + (size_t)(head + rl0) * net.W;
-        __syncthreads(); // the previous tile is done with the keys and the operand
+        bar_main(); // the previous tile is done with the keys and the operand
         for (int q = tid; q < R * net.W; q += kThreads)
             keys[(q / net.W) * KW + q % net.W] = q < nreg * net.W ? gkeys[q] : 0u;
-        __syncthreads(); // every thread reads every region's bits below
+        bar_main(); // every thread reads every region's bits below
 
         // hidden layer 1 = linear 0 rows (sign-flipped) and the extra constraints
         {
@@ -448,38 +459,42 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
         }
         umma::fence_proxy_async();
         umma::fence_before();
-        __syncthreads();
+        bar_main();
         umma::fence_after();
         const uint32_t tmem = tslot;
 
         for (int i = 1; i <= net.n_lin - 2; ++i) {
             const int M = net.nodes[i + 1];
             const int mtiles = (M + 127) / 128;
-            if (tid == 0) gemm_issue(pp, net, tc, tc.lin[i], mtiles, X, tmem, true, g);
+            if (tid == 0) gemm_issue(pp, tc.lin[i], mtiles, X, tmem, true, g);
             for (int s = 0; s < net.nskip[i]; ++s) {
                 const SkipDev &sk = net.skip[i][s];
                 if (tc_skip(sk)) {
                     // the operand is about to be overwritten: the products so far must be done
-                    if (tid == 0) gemm_finish(pp, net, tc, g);
-                    __syncthreads();
-                    if (s_abort) break; // written by thread 0 before the barrier: uniform
+                    if (tid == 0) {
+                        gemm_finish(pp, g);
+                        if (*pp.abort) s_stop = 1;
+                    }
+                    bar_main();
+                    if (s_stop) break; // written by thread 0 before the barrier: uniform
                     stage_x_from_rows(X, cons, rstride, keys, KW, nreg, net.hoff[sk.from],
                                       net.nodes[sk.from], tc.skip[i][s].Kp);
                     umma::fence_proxy_async();
-                    __syncthreads();
-                    if (tid == 0) gemm_issue(pp, net, tc, tc.skip[i][s], mtiles, X, tmem, false, g);
+                    bar_main();
+                    if (tid == 0) gemm_issue(pp, tc.skip[i][s], mtiles, X, tmem, false, g);
                 }
             }
             // the first M tile's bias, loaded while the products run
             const float *bias = (const float *)net.bias[i];
             float bnext = q4 * 32 + lane < M ? bias[q4 * 32 + lane] : 0.f;
             if (tid == 0) {
-                gemm_finish(pp, net, tc, g);
+                gemm_finish(pp, g);
+                if (*pp.abort) s_stop = 1;
                 s_last = g - 1;
             }
             __syncwarp();
-            __syncthreads();
-            if (s_abort) break; // no epilogue: the accumulators are not complete
+            bar_main();
+            if (s_stop) break; // no epilogue: the accumulators are not complete
             gemm_observe(pp, s_last);
             // epilogue: accumulators -> constraint rows (HBM) and the next operand (smem)
             const int Kn = (M + 63) / 64 * 64; // next operand's padded K (the face plane reads it too)
@@ -548,11 +563,11 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
             }
             umma::fence_proxy_async();
             umma::fence_before();
-            __syncthreads();
+            bar_main();
             umma::fence_after();
         }
 
-        if (s_abort) break;
+        if (s_stop) break;
         // face plane: w_eq = W_L . X_L (+ b_L, + connections into the output layer)
         // in fp32 from the operand in shared memory (hi + mid + lo is exact):
         // lanes take regions (consecutive regions share operand rows), the
@@ -575,7 +590,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                     }
                 // partial sums: [warp][lane][4]
                 reinterpret_cast<float4 *>(fsum)[warp * 32 + lane] = make_float4(acc[0], acc[1], acc[2], acc[3]);
-                __syncthreads();
+                bar_main();
                 if (tid < 128) {
                     const int rr = tid >> 2, c = tid & 3, rg = r0 + rr;
                     float a = 0.f;
@@ -601,13 +616,13 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
                         ((float *)ch.eq)[(size_t)(rl0 + rg) * 4 + c] = a;
                     }
                 }
-                __syncthreads();
+                bar_main();
             }
         }
     } // tiles
-    if (tid == 0 && s_abort) wp_drain(pp);
+    if (tid == 0 && *pp.abort) wp_drain(pp);
     umma::fence_before();
-    __syncthreads();
+    __syncthreads(); // with the copy warp
     if (warp == 0) umma::tmem_dealloc(tslot, (uint32_t)tmem_cols);
 }
 
@@ -625,7 +640,7 @@ __global__ void __launch_bounds__(kThreads, 1) compose_tc_kernel(NetDev net, TcN
 // and face-plane arithmetic are those of compose_tc_kernel, so both kernels
 // give the same bits.
 constexpr int kSBuild = 512;            // builder threads (16 warps)
-constexpr int kSThreads = kSBuild + 32; // + the issuing warp
+constexpr int kSThreads = kSBuild + 64; // + the issuing warp and the weight-copy warp
 constexpr int kSFaceSumBytes = kSBuild * 16;
 
 __device__ __forceinline__ int jobs_of(const NetDev &net, int i)
@@ -672,108 +687,106 @@ __device__ __forceinline__ bool swait(uint64_t *bar, uint32_t parity, int *err, 
     return false;
 }
 
-// position in the product sequence: tile, layer, job, K block, M tile (innermost)
-struct SCur {
-    int t, i, job, kb, mt;
-    bool valid;
-};
-
-__device__ void scur_next(SCur &c, const NetDev &net, const TcNet &tc, int tiles)
+// (one thread of its own warp) the weight blocks through the nstage ring, in
+// the order the products consume them -- tile, layer, job, K block, M tile --
+// running ahead of the products by up to nstage blocks: block h goes into
+// stage h % nstage once the products of block h - nstage have completed.
+// Measured on GB300: with the copies issued from the same thread as the
+// products, every block cost that thread a wait for the previous block's
+// products before its refill (about as long as the 24 products themselves),
+// so the tensor pipe was idle most of the time.
+__device__ void produce_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, uint64_t *wfull, uint64_t *wdone,
+                                 int tiles, int *err, volatile int *abort)
 {
-    int src;
-    const TcMat &m = job_mat(net, tc, c.i, c.job, src);
-    if (++c.mt < m.Mp / 128) return;
-    c.mt = 0;
-    if (++c.kb < m.Kp / 64) return;
-    c.kb = 0;
-    if (++c.job < jobs_of(net, c.i)) return;
-    c.job = 0;
-    if (++c.i <= net.n_lin - 2) return;
-    c.i = 1;
-    if (++c.t < tiles) return;
-    c.valid = false;
+    const int nst = tc.nstage;
+    int h = 0;
+    int last[4] = {-1, -1, -1, -1}; // the last block copied into each stage
+    for (int t = 0; t < tiles; ++t)
+        for (int i = 1; i <= net.n_lin - 2; ++i) {
+            const int njobs = jobs_of(net, i);
+            for (int job = 0; job < njobs; ++job) {
+                int src;
+                const TcMat &m = job_mat(net, tc, i, job, src);
+                const int mtiles = m.Mp / 128, kblocks = m.Kp / 64;
+                for (int kb = 0; kb < kblocks; ++kb)
+                    for (int mt = 0; mt < mtiles; ++mt, ++h) {
+                        const int s = h % nst;
+                        if (h >= nst && !swait(wdone + s, (uint32_t)((h - nst) / nst) & 1u, err, abort)) continue;
+                        if (*abort) continue;
+                        umma::mbar_expect_tx(wfull + s, (uint32_t)kWBlockBytes);
+                        umma::bulk_g2s(ws + (size_t)s * kWBlockBytes,
+                                       m.blocks + (size_t)(mt * kblocks + kb) * kWBlockBytes, (uint32_t)kWBlockBytes,
+                                       wfull + s);
+                        last[s] = h;
+                    }
+            }
+        }
+    // nothing lands in shared memory after the CTA has left: the last copy of
+    // every stage (bounded)
+    for (int s = 0; s < nst; ++s)
+        if (last[s] >= 0) umma::mbar_wait(wfull + s, (uint32_t)(last[s] / nst) & 1u, kWaitIters);
 }
 
-// (one thread) weight blocks through the nstage ring, operand blocks through
-// the two-stage ring: six products per K step into the main (hi.hi) and the
-// correction accumulator of each M tile
+// (one thread) the products: operand blocks through the two-stage ring,
+// weight blocks from the producer's ring, six products per K step into the
+// main (hi.hi) and the correction accumulator of each M tile.  The commits
+// that free the operand stages and publish the layer's accumulators are
+// made whatever happens, so that the builders never wait on a partner that
+// gave up.
 __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, uint64_t *wfull, uint64_t *wdone,
                                const XOp *XS, uint64_t *xfull, uint64_t *xdone, uint64_t *accdone, uint32_t tmem,
                                int ncols, int tiles, int *err, volatile int *abort)
 {
     const int nst = tc.nstage;
-    SCur cc{0, 1, 0, 0, 0, net.n_lin - 2 >= 1}; // next weight block to copy
-    SCur mc = cc;                                // next weight block to multiply
-    int issued = 0, consumed = 0;
-    auto copy_next = [&]() -> bool {
-        const int s = issued % nst;
-        if (issued >= nst && !swait(wdone + s, (uint32_t)((issued - nst) / nst) & 1u, err, abort)) return false;
-        int src;
-        const TcMat &m = job_mat(net, tc, cc.i, cc.job, src);
-        umma::mbar_expect_tx(wfull + s, (uint32_t)kWBlockBytes);
-        umma::bulk_g2s(ws + (size_t)s * kWBlockBytes,
-                       m.blocks + (size_t)(cc.mt * (m.Kp / 64) + cc.kb) * kWBlockBytes, (uint32_t)kWBlockBytes,
-                       wfull + s);
-        ++issued;
-        scur_next(cc, net, tc, tiles);
-        return true;
-    };
-    while (cc.valid && issued < nst && copy_next()) {
-    }
-    int h = 0, xb = 0;
+    int h = 0, xb = 0, consumed = 0;
     // operand descriptors of the two stages; term and K step add constant offsets
     const uint64_t xd0 = XS[0].desc(0, 0, 0), xd1 = XS[1].desc(0, 0, 0);
     const uint64_t xu = XS[0].ustep(), xj = XS[0].jstep();
     const uint32_t idesc = XS[0].idesc();
-    while (mc.valid) {
-        int src;
-        const TcMat &m = job_mat(net, tc, mc.i, mc.job, src);
-        const int mtiles = m.Mp / 128, kblocks = m.Kp / 64;
-        const int xs = xb & 1;
-        const uint64_t xd = xs ? xd1 : xd0;
-        bool ok = mc.mt != 0 || swait(xfull + xs, (uint32_t)(xb >> 1) & 1u, err, abort); // operand block built
-        while (ok && cc.valid && issued <= h && copy_next()) {
-        }
-        const int s = h % nst;
-        ok = ok && issued > h && swait(wfull + s, (uint32_t)(h / nst) & 1u, err, abort);
-        if (ok) {
-            umma::fence_after();
-            const uint32_t a0 = umma::smem_addr(ws + (size_t)s * kWBlockBytes);
-            const uint32_t d_main = tmem + (uint32_t)(mc.mt * ncols);
-            const uint32_t d_corr = tmem + (uint32_t)((mtiles + mc.mt) * ncols);
-            const bool fresh = mc.job == 0 && mc.kb == 0;
-            const uint64_t ad = umma::desc_sw128(a0); // term t at +16 KB, K step j at +32 B
+    for (int t = 0; t < tiles; ++t)
+        for (int i = 1; i <= net.n_lin - 2; ++i) {
+            const int njobs = jobs_of(net, i);
+            for (int job = 0; job < njobs; ++job) {
+                int src;
+                const TcMat &m = job_mat(net, tc, i, job, src);
+                const int mtiles = m.Mp / 128, kblocks = m.Kp / 64;
+                for (int kb = 0; kb < kblocks; ++kb) {
+                    const int xs = xb & 1;
+                    const uint64_t xd = xs ? xd1 : xd0;
+                    const bool xok = swait(xfull + xs, (uint32_t)(xb >> 1) & 1u, err, abort); // operand block built
+                    const bool fresh = job == 0 && kb == 0;
+                    for (int mt = 0; mt < mtiles; ++mt, ++h) {
+                        const int s = h % nst;
+                        if (!xok || !swait(wfull + s, (uint32_t)(h / nst) & 1u, err, abort)) continue;
+                        umma::fence_after();
+                        const uint32_t a0 = umma::smem_addr(ws + (size_t)s * kWBlockBytes);
+                        const uint32_t d_main = tmem + (uint32_t)(mt * ncols);
+                        const uint32_t d_corr = tmem + (uint32_t)((mtiles + mt) * ncols);
+                        const uint64_t ad = umma::desc_sw128(a0); // term t at +16 KB, K step j at +32 B
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                umma::mma_bf16(d_main, ad + 2u * j, xd + xj * j, idesc, (fresh && j == 0) ? 0u : 1u);
-                int q = 0;
+                        for (int j = 0; j < 4; ++j) {
+                            umma::mma_bf16(d_main, ad + 2u * j, xd + xj * j, idesc, (fresh && j == 0) ? 0u : 1u);
+                            int q = 0;
 #pragma unroll
-                for (int t = 0; t < 3; ++t)
+                            for (int tt = 0; tt < 3; ++tt)
 #pragma unroll
-                    for (int u = 0; u + t < 3; ++u) {
-                        if (t == 0 && u == 0) continue;
-                        umma::mma_bf16(d_corr, ad + 1024u * t + 2u * j, xd + xu * u + xj * j, idesc,
-                                       (fresh && j == 0 && q == 0) ? 0u : 1u);
-                        ++q;
+                                for (int u = 0; u + tt < 3; ++u) {
+                                    if (tt == 0 && u == 0) continue;
+                                    umma::mma_bf16(d_corr, ad + 1024u * tt + 2u * j, xd + xu * u + xj * j, idesc,
+                                                   (fresh && j == 0 && q == 0) ? 0u : 1u);
+                                    ++q;
+                                }
+                        }
+                        umma::commit(umma::smem_addr(wdone + s)); // the producer may refill the stage
+                        consumed = h + 1;
                     }
+                    umma::commit(umma::smem_addr(xdone + xs)); // the operand stage is free once these complete
+                    ++xb;
+                }
             }
-            umma::commit(umma::smem_addr(wdone + s));
-            consumed = h + 1;
+            umma::commit(umma::smem_addr(accdone)); // the layer's accumulators are complete
         }
-        // the builders' barriers are served in every case
-        if (mc.mt == mtiles - 1) {
-            umma::commit(umma::smem_addr(xdone + xs)); // the operand stage is free once these complete
-            ++xb;
-            if (mc.kb == kblocks - 1 && mc.job == jobs_of(net, mc.i) - 1)
-                umma::commit(umma::smem_addr(accdone)); // the layer's accumulators are complete
-        }
-        while (ok && cc.valid && issued <= h + nst - 1 && copy_next()) { // refill the stage of block h - 1
-        }
-        ++h;
-        scur_next(mc, net, tc, tiles);
-    }
-    // copies issued but never observed (aborting CTA), then the last products
-    for (int q = consumed; q < issued; ++q) umma::mbar_wait(wfull + q % nst, (uint32_t)(q / nst) & 1u, kWaitIters);
+    // the last products have completed before TMEM is released
     if (consumed > 0 &&
         !umma::mbar_wait(wdone + (consumed - 1) % nst, (uint32_t)((consumed - 1) / nst) & 1u, kWaitIters))
         atomicOr(err, kErrWait);
@@ -850,6 +863,9 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
         if (lane == 0)
             issue_streamed(net, tc, ws, wfull, wdone, XS, xfull, xdone, accdone, tmem, ncols, tiles, err, abort);
         __syncwarp(); // the warp reaches the block barrier below converged
+    } else if (warp == kSBuild / 32 + 1) {
+        if (lane == 0) produce_streamed(net, tc, ws, wfull, wdone, tiles, err, abort);
+        __syncwarp();
     } else {
         // epilogue: warp w reads TMEM lanes 32 (w % 4).. and every fourth column block
         const int q4 = warp & 3, cgrp = warp >> 2, ngrp = kSBuild / 128;
@@ -1113,13 +1129,13 @@ void launch_compose_tc(const NetDev &net, const TcNet &tc, const RegionsDev &reg
     }
     cudaFuncSetAttribute(compose_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
     if (ch.ctl) { // wave size known on the device only: every resident tile slot, tiles strided
-        compose_tc_kernel<<<slots, kThreads, smem_max, st>>>(net, tc, reg, ch, (float)iso, slots, d_err);
+        compose_tc_kernel<<<slots, kThreads + 32, smem_max, st>>>(net, tc, reg, ch, (float)iso, slots, d_err);
         return;
     }
     const int ncols = tile_cols(ch.count, slots, tc.ncols_max);
     const int R = ncols / 4;
     const int grid = (ch.count + R - 1) / R;
-    compose_tc_kernel<<<grid, kThreads, tc_smem_bytes(tc, ncols, net.W), st>>>(net, tc, reg, ch, (float)iso, slots,
+    compose_tc_kernel<<<grid, kThreads + 32, tc_smem_bytes(tc, ncols, net.W), st>>>(net, tc, reg, ch, (float)iso, slots,
                                                                               d_err);
 }
 
