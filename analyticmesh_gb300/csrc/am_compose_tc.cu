@@ -703,13 +703,15 @@ __device__ void produce_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws
     int last[4] = {-1, -1, -1, -1}; // the last block copied into each stage
     for (int t = 0; t < tiles; ++t)
         for (int i = 1; i <= net.n_lin - 2; ++i) {
+            const int mtl = (net.nodes[i + 1] + 127) / 128, mper = (mtl + tc.mgroups - 1) / tc.mgroups;
+            for (int mt0 = 0; mt0 < mtl; mt0 += mper) {
             const int njobs = jobs_of(net, i);
             for (int job = 0; job < njobs; ++job) {
                 int src;
                 const TcMat &m = job_mat(net, tc, i, job, src);
                 const int mtiles = m.Mp / 128, kblocks = m.Kp / 64;
                 for (int kb = 0; kb < kblocks; ++kb)
-                    for (int mt = 0; mt < mtiles; ++mt, ++h) {
+                    for (int mt = mt0; mt < min(mtiles, mt0 + mper); ++mt, ++h) {
                         const int s = h % nst;
                         if (h >= nst && !swait(wdone + s, (uint32_t)((h - nst) / nst) & 1u, err, abort)) continue;
                         if (*abort) continue;
@@ -719,6 +721,7 @@ __device__ void produce_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws
                                        wfull + s);
                         last[s] = h;
                     }
+            }
             }
         }
     // nothing lands in shared memory after the CTA has left: the last copy of
@@ -745,6 +748,8 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
     const uint32_t idesc = XS[0].idesc();
     for (int t = 0; t < tiles; ++t)
         for (int i = 1; i <= net.n_lin - 2; ++i) {
+            const int mtl = (net.nodes[i + 1] + 127) / 128, mper = (mtl + tc.mgroups - 1) / tc.mgroups;
+            for (int mt0 = 0; mt0 < mtl; mt0 += mper) { // a group of M tiles, its own accumulators
             const int njobs = jobs_of(net, i);
             for (int job = 0; job < njobs; ++job) {
                 int src;
@@ -755,13 +760,13 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
                     const uint64_t xd = xs ? xd1 : xd0;
                     const bool xok = swait(xfull + xs, (uint32_t)(xb >> 1) & 1u, err, abort); // operand block built
                     const bool fresh = job == 0 && kb == 0;
-                    for (int mt = 0; mt < mtiles; ++mt, ++h) {
+                    for (int mt = mt0; mt < min(mtiles, mt0 + mper); ++mt, ++h) {
                         const int s = h % nst;
                         if (!xok || !swait(wfull + s, (uint32_t)(h / nst) & 1u, err, abort)) continue;
                         umma::fence_after();
                         const uint32_t a0 = umma::smem_addr(ws + (size_t)s * kWBlockBytes);
-                        const uint32_t d_main = tmem + (uint32_t)(mt * ncols);
-                        const uint32_t d_corr = tmem + (uint32_t)((mtiles + mt) * ncols);
+                        const uint32_t d_main = tmem + (uint32_t)((mt - mt0) * ncols);
+                        const uint32_t d_corr = tmem + (uint32_t)((mper + mt - mt0) * ncols);
                         const uint64_t ad = umma::desc_sw128(a0); // term t at +16 KB, K step j at +32 B
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
@@ -784,7 +789,8 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
                     ++xb;
                 }
             }
-            umma::commit(umma::smem_addr(accdone)); // the layer's accumulators are complete
+            umma::commit(umma::smem_addr(accdone)); // the group's accumulators are complete
+            }
         }
     // the last products have completed before TMEM is released
     if (consumed > 0 &&
@@ -811,7 +817,8 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
     const int tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (tiles == 0) return;
     int tmem_cols = 32;
-    while (tmem_cols < 2 * tc.mtiles_max * ncols) tmem_cols <<= 1;
+    const int mper_max = (tc.mtiles_max + tc.mgroups - 1) / tc.mgroups;
+    while (tmem_cols < 2 * mper_max * ncols) tmem_cols <<= 1;
     const size_t rstride = (size_t)net.ALLP * 4;
     const int KW = key_stride(net.W); // odd: lanes on consecutive regions read distinct banks
 
@@ -830,7 +837,9 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
     uint32_t *keys = reinterpret_cast<uint32_t *>(ws + (size_t)tc.nstage * kWBlockBytes);
     float4 *w0s = reinterpret_cast<float4 *>(keys + (size_t)(tc.ncols_max / 4) * key_stride(net.W));
     float *wls = reinterpret_cast<float *>(w0s + net.nodes[1]);
-    float *fsum = reinterpret_cast<float *>(reinterpret_cast<uintptr_t>(wls + net.nodes[net.n_lin - 1] + 3) & ~(uintptr_t)15);
+    // the face plane's partial sums use the operand ring: it is idle then
+    // (the tile's products are complete, the next tile's operand not begun)
+    float *fsum = reinterpret_cast<float *>(base);
     uint64_t *wfull = bars, *wdone = bars + 3, *xfull = bars + 6, *xdone = bars + 8, *accdone = bars + 10;
 
     volatile int *abort = &s_abort;
@@ -899,6 +908,9 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
             for (int i = 1; i <= net.n_lin - 2; ++i) {
                 const int M = net.nodes[i + 1];
                 const int mtiles = (M + 127) / 128;
+                const int mper = (mtiles + tc.mgroups - 1) / tc.mgroups;
+                for (int mt0 = 0; mt0 < mtiles; mt0 += mper) { // the products of this group of M tiles
+                const int mt1 = min(mtiles, mt0 + mper);
                 const int njobs = jobs_of(net, i);
                 for (int job = 0; job < njobs; ++job) {
                     int src;
@@ -940,7 +952,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                     }
                 }
                 const float *bias = (const float *)net.bias[i];
-                float bnext = q4 * 32 + lane < M ? bias[q4 * 32 + lane] : 0.f; // loaded while the products run
+                float bnext = mt0 * 128 + q4 * 32 + lane < M ? bias[mt0 * 128 + q4 * 32 + lane] : 0.f; // loaded while the products run
                 // the layer's products are in TMEM; the TMEM loads below are
                 // warp-collective, so the warp decides as one
                 bool acc_ok = swait(accdone, (uint32_t)(accph & 1), err, abort);
@@ -948,16 +960,16 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                 ++accph;
                 umma::fence_after();
                 // epilogue: accumulators -> constraint rows of hidden layer i + 1
-                for (int mt = 0; acc_ok && mt < mtiles; ++mt) {
+                for (int mt = mt0; acc_ok && mt < mt1; ++mt) {
                     const int m = mt * 128 + q4 * 32 + lane;
                     const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
                     const float bm = bnext;
-                    if (mt + 1 < mtiles) bnext = m + 128 < M ? bias[m + 128] : 0.f;
+                    if (mt + 1 < mt1) bnext = m + 128 < M ? bias[m + 128] : 0.f;
                     const int row = net.hoff[i + 1] + m;
                     for (int cb = cgrp; cb < ncols / 16; cb += ngrp) {
                         float v[16], vc[16];
-                        umma::tmem_ld16x2(lane_base + (uint32_t)(mt * ncols + cb * 16),
-                                          lane_base + (uint32_t)((mtiles + mt) * ncols + cb * 16), v, vc);
+                        umma::tmem_ld16x2(lane_base + (uint32_t)((mt - mt0) * ncols + cb * 16),
+                                          lane_base + (uint32_t)((mper + mt - mt0) * ncols + cb * 16), v, vc);
                         if (m >= M) continue;
 #pragma unroll
                         for (int qq = 0; qq < 4; ++qq) {
@@ -996,6 +1008,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                 }
                 umma::fence_before(); // TMEM read out before the next products overwrite it
                 bar_builders();       // rows of hidden layer i + 1 written by every builder
+                }
             }
 
             // face plane: w_eq = W_L . X_L, X_L = -C of the last hidden layer
@@ -1098,10 +1111,10 @@ int device_sms()
 
 size_t tc_smem_bytes(const TcNet &tc, int ncols, int W)
 {
-    if (tc.streamed) { // two operand stages of one K block each
+    if (tc.streamed) { // two operand stages of one K block each (the face-plane sums reuse them)
         const size_t cols = tc.mn ? (size_t)(ncols + 63) / 64 * 64 : (size_t)ncols;
-        return 1024 + 6 * cols * 64 * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * key_stride(W) * 4 +
-               16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last + 16 + (size_t)kSFaceSumBytes;
+        return 1024 + std::max<size_t>(6 * cols * 64 * 2, (size_t)kSFaceSumBytes) + (size_t)tc.nstage * kWBlockBytes +
+               (size_t)(tc.ncols_max / 4) * key_stride(W) * 4 + 16 * (size_t)tc.n1 + 4 * (size_t)tc.k_last + 16;
     }
     const size_t cols = tc.mn ? (size_t)(ncols + 63) / 64 * 64 : (size_t)ncols;
     return 1024 + 3 * cols * tc.kp_max * 2 + (size_t)tc.nstage * kWBlockBytes + (size_t)(tc.ncols_max / 4) * key_stride(W) * 4 +

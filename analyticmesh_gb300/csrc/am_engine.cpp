@@ -214,7 +214,7 @@ struct am_engine {
     int face_warps = 0;        // AM_OPT_FACE_WARPS: warps per face polygon, 0 automatic
     long long table_slots = 0; // AM_OPT_TABLE_SLOTS: fixed region hash table size, 0 automatic
     int inject_err = 0;        // AM_OPT_INJECT_ERROR: error bits set in the control block after the seeds
-    int prune = 1;             // AM_OPT_PRUNE_ROWS: the walk scans only the rows that can bound the face
+    int prune = 0;             // AM_OPT_PRUNE_ROWS: the walk scans only the rows that can bound the face
     bool limit_hit = false;    // the last run stopped at the region limit
     bool over_limit(long long tail)
     {
@@ -604,6 +604,7 @@ void run_begin(am_engine *e, const RunArgs &a)
         TcNet &tc = e->tcnet;
         memset(&tc, 0, sizeof(tc));
         tc.mtiles_max = 1;
+        tc.mgroups = 1;
         auto split = [&](DevBuf &buf, const void *src_fp32, int M, int K, TcMat &m) {
             const int Mp = (M + 127) / 128 * 128, Kp = (K + 63) / 64 * 64;
             upload(e->scratch, src_fp32, sizeof(float) * (size_t)M * K, st);
@@ -651,21 +652,34 @@ void run_begin(am_engine *e, const RunArgs &a)
         // streamed operand (wide layers): two 64-deep operand blocks, so the
         // tile is as wide as TMEM allows; taken when that is wider
         // (the widest tile first, then the most weight stages in flight)
-        TcNet ts = tc;
-        ts.streamed = 1;
-        ts.ncols_max = 0;
-        for (int mn = 1; mn >= 0 && ts.ncols_max < 16; --mn) {
-            ts.mn = mn;
-            for (int ncols = std::min(256, 256 / ts.mtiles_max) / 16 * 16; ncols >= 16 && ts.ncols_max < 16;
-                 ncols -= 16)
-                for (int ns = 3; ns >= 1; --ns) {
-                    ts.ncols_max = ncols;
-                    ts.nstage = ns;
-                    if (tc_smem_bytes(ts, ncols, e->W) <= smem_cap) break;
-                    ts.ncols_max = 0;
-                }
+        // With mgroups > 1 a layer's M tiles are multiplied in that many
+        // passes, each with its own accumulators, so that the tile can be
+        // wider than two accumulators per M tile of the widest layer allow
+        // (the operand is rebuilt once per pass).
+        auto streamed_tile = [&](int mgroups) {
+            TcNet ts = tc;
+            ts.streamed = 1;
+            ts.mgroups = mgroups;
+            ts.ncols_max = 0;
+            const int mper = (ts.mtiles_max + mgroups - 1) / mgroups;
+            for (int mn = 1; mn >= 0 && ts.ncols_max < 16; --mn) {
+                ts.mn = mn;
+                for (int ncols = std::min(256, 256 / mper) / 16 * 16; ncols >= 16 && ts.ncols_max < 16; ncols -= 16)
+                    for (int ns = 3; ns >= 1; --ns) {
+                        ts.ncols_max = ncols;
+                        ts.nstage = ns;
+                        if (tc_smem_bytes(ts, ncols, e->W) <= smem_cap) break;
+                        ts.ncols_max = 0;
+                    }
+            }
+            return ts;
+        };
+        TcNet ts = streamed_tile(1);
+        if (tc.mtiles_max >= 2 && e->compose_tile != 2) {
+            const TcNet t2 = streamed_tile(2);
+            if (e->compose_tile == 3 || t2.ncols_max > ts.ncols_max) ts = t2;
         }
-        const bool want_streamed = e->compose_tile == 2 ||
+        const bool want_streamed = e->compose_tile >= 2 ||
                                    (e->compose_tile == 0 && tc.kp_max >= 256 && ts.ncols_max > tc.ncols_max);
         if (ts.ncols_max >= 16 && (want_streamed || tc.ncols_max < 16)) tc = ts;
         AM_CHECK(e->compose_tile != 1 || !tc.streamed, "resident operand tile does not fit");
@@ -1024,7 +1038,7 @@ int am_set_option(am_engine *e, int option, int64_t value)
         return AM_OK;
     }
     if (option == AM_OPT_COMPOSE_TILE) {
-        if (value < 0 || value > 2) return AM_ERR_INVALID_ARGUMENT;
+        if (value < 0 || value > 3) return AM_ERR_INVALID_ARGUMENT;
         e->compose_tile = (int)value;
         return AM_OK;
     }
@@ -1135,7 +1149,7 @@ int am_autotune(am_engine *e, const am_run_args *x, int64_t sample_regions, int3
         return rc == AM_OK;
     };
     std::vector<int> cts = {0};
-    if (e->prec == kMixed) cts = {1, 2};
+    if (e->prec == kMixed) cts = {1, 2, 3};
     const int fws[] = {1, 2, 4, 8};
     double c = 0, p = 0;
     for (int ct : cts) sample(ct, 0, c, p); // untimed pass

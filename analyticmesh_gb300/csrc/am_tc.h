@@ -31,6 +31,8 @@ struct TcNet {
     int mn;                             // operand layout: 1 MN-major (64-column atoms), 0 K-major
     int n1, k_last;                     // widths of hidden layer 1 and of the last hidden layer
     int streamed;                       // operand rebuilt per 64-wide K block from the rows (wide layers)
+    int mgroups;                        // streamed: a layer's M tiles in this many passes, each with its own
+                                        // accumulators (TMEM holds 2 x ceil(mtiles / mgroups) x ncols columns)
 };
 
 size_t tc_smem_bytes(const TcNet &tc, int ncols, int W);

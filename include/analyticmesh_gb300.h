@@ -186,7 +186,9 @@ typedef enum {
     AM_OPT_COMPOSE_TILE = 6,  /* "mixed" composition on the tensor cores: 0 (default) automatic, 1 the
                                  operand of a tile stays in shared memory for all layers, 2 it is rebuilt
                                  per 64-deep block from the rows just written (wider tiles for layers of
-                                 256 units and more).  Both give the same bits. */
+                                 256 units and more), 3 as 2 with a layer's 128-row tiles multiplied in two
+                                 passes, so that TMEM holds accumulators for twice as many regions (layers
+                                 of 512 units).  All give the same bits. */
     AM_OPT_FACE_WARPS = 7,    /* warps per face polygon: 0 (default) automatic (one for narrow networks,
                                  up to eight for wide ones, whose rows leave room for few faces per SM),
                                  or 1, 2, 4, 8.  The warps of a face split the walk's scan over the rows. */
@@ -201,10 +203,12 @@ typedef enum {
                                  block after the seed phase, as a kernel would leave them, so that the
                                  wave loop's error decoding can be tested without a device fault.
                                  0 (default) off; stays set until set to 0. */
-    AM_OPT_PRUNE_ROWS = 10    /* 1 (default): before walking a face, drop the constraint rows whose line
-                                 provably misses the polygon (a dual-space test against a sample of the
-                                 rows), so that the walk scans a few dozen rows per step instead of all;
-                                 0: every row.  Both give the same faces. */
+    AM_OPT_PRUNE_ROWS = 10    /* 1: before walking a face, drop the constraint rows whose line provably
+                                 misses the polygon (a dual-space test against a sample of the rows), so
+                                 that the walk scans a few dozen rows per step instead of all; 0 (default):
+                                 every row.  Both give the same faces.  Measured on GB300 the two pruning
+                                 passes cost about what they save (+5 % on 3-[128]x4-1 in the mixed form,
+                                 -10 to -25 % on the 1536- and 4096-row networks), hence off. */
 } am_option;
 int am_set_option(am_engine *engine, int option, int64_t value);
 

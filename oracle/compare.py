@@ -200,3 +200,57 @@ def parity_report(a, b, tol=1e-5):
                 common_polygons=int(ra.size), faces_count_mismatch=int(count_differs.sum()),
                 faces_beyond_tol=int((same & (~np.isfinite(d) | (d > tol))).sum()),
                 max_diff=float(d[fin].max()) if fin.any() else 0.0)
+
+
+def region_geometry(r, i, engine_record=True):
+    """(vertex count, polygon area, shortest edge, length of the edge on the
+    region's start plane or nan) of region record i -- the engine's records
+    carry the plane of every edge, the oracle's only the pivot table."""
+    n = int(r.nverts[i])
+    if n < 3:
+        return n, 0.0, 0.0, float("nan")
+    V = np.asarray(r.verts[i, :n], dtype=np.float64)
+    e = np.linalg.norm(np.roll(V, -1, axis=0) - V, axis=1)
+    c = V.mean(0)
+    area = 0.5 * float(np.linalg.norm(np.cross(V - c, np.roll(V, -1, axis=0) - c).sum(0)))
+    sedge = float("nan")
+    st = int(r.start[i])
+    if engine_record and st >= 0:
+        on = np.nonzero(np.asarray(r.edges[i, :n]) == st)[0]
+        if on.size:
+            sedge = float(e[on].min())
+    return n, area, float(e.min()), sedge
+
+
+def classify_regions(r, idx, engine_record=True, length_eps=1e-5, area_eps=1e-10):
+    """Why a region can be found by one run and not by another: counts of
+    the records idx of run r by category -- "no_face" (fewer than 3
+    vertices, or a walk that did not close), "sliver" (area below area_eps or
+    an edge shorter than length_eps: a face at a near-degenerate vertex,
+    whose neighbours depend on merge decisions at FP_SAME_EPS), "entry" (its
+    edge on the start plane, the one its parent shared, is shorter than
+    length_eps), or "other"."""
+    out = {"no_face": 0, "sliver": 0, "entry": 0, "other": 0}
+    others = []
+    for i in idx:
+        n, area, emin, sedge = region_geometry(r, i, engine_record)
+        bad_status = engine_record and hasattr(r, "status") and int(r.status[i]) != 0
+        if n < 3 or bad_status:
+            out["no_face"] += 1
+        elif area < area_eps or emin < length_eps:
+            out["sliver"] += 1
+        elif sedge == sedge and sedge < length_eps:
+            out["entry"] += 1
+        else:
+            out["other"] += 1
+            others.append(int(i))
+    out["other_ids"] = others[:20]
+    return out
+
+
+def region_difference(a, b):
+    """Record indices (one per key) of the regions only a visited and only b visited."""
+    ka, kb = _row_keys(a.bits), _row_keys(b.bits)
+    ua, ia = np.unique(ka, return_index=True)
+    ub, ib = np.unique(kb, return_index=True)
+    return ia[~np.isin(ua, ub)], ib[~np.isin(ub, ua)]

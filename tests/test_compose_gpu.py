@@ -97,13 +97,14 @@ def test_tensor_core_rows_match_fp32_accuracy(factory):
 ], ids=["wide256", "wide512", "odd_widths_tc_skip", "input_skip"])
 def test_streamed_and_resident_operand_tiles_agree(factory):
     """The tensor-core composition with the operand resident in shared memory
-    for all layers and with the operand rebuilt per 64-deep block from the
-    rows just written: same rows, same face planes, same regions, bit for bit."""
+    for all layers, with the operand rebuilt per 64-deep block from the rows
+    just written, and the latter with each layer's M tiles in two passes:
+    same rows, same face planes, same regions, bit for bit."""
     m = factory()
     net = wl.net_arrays(m)
     st, pt = wl.seeds_for(m, init_num=128, seed=7)
     out = {}
-    for tile in (1, 2):
+    for tile in (1, 2, 3):
         try:
             eng = engine.march(net, st, pt, "mixed", options={_lib.AM_OPT_COMPOSE_TILE: tile})
         except RuntimeError as e:  # the resident tile of a 512-wide net may not fit
@@ -114,9 +115,11 @@ def test_streamed_and_resident_operand_tiles_agree(factory):
         rows, eq = eng.region_rows(0, n)
         out[tile] = (s["num_regions"], s["num_faces"], eng.regions().bits[:n], rows, eq)
         eng.close()
-    assert 2 in out
-    if 1 in out:
-        a, b = out[1], out[2]
+    assert 2 in out and 3 in out
+    for other in (1, 3):  # the resident tile, and the streamed tile in two M passes
+        if other not in out:
+            continue
+        a, b = out[other], out[2]
         assert a[0] == b[0] and a[1] == b[1]
         assert np.array_equal(a[2], b[2])
         assert np.array_equal(a[3].view(np.int64), b[3].view(np.int64))
