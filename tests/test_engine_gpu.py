@@ -56,10 +56,13 @@ def test_engine_matches_reference_golden(name):
     # same regions, same polygons combinatorially
     assert c["regions_only_a"] == 0 and c["regions_only_b"] == 0, c
     assert c["faces_count_mismatch"] == 0, c
-    # numerically: within tolerance except ill-conditioned vertices, where
-    # both sides' own rounding exceeds it (bounded at 100 x tol)
-    assert c["faces_beyond_tol"] <= max(1, c["common_polygons"] // 500), c
-    assert c["max_diff"] <= 100 * TOL[g["dtype"]], c
+    # numerically: within the tolerance, or within what the face's
+    # worst-conditioned vertex allows (test_parity_gpu.common_faces_agree)
+    if g["dtype"] == "float32":
+        from test_parity_gpu import common_faces_agree
+        common_faces_agree(reg, g["regions"], True, False, eng)
+    else:
+        assert c["faces_beyond_tol"] == 0, c
     eng.close()
 
 
@@ -86,29 +89,6 @@ def test_engine_matches_oracle(factory, nseed, dtype):
     # every vertex on the zero level set
     v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in range(reg.num) if reg.nverts[i] >= 3])
     assert np.abs(f_at(net, v)).max() <= (1e-5 if dtype == "float32" else 1e-10)
-    eng.close()
-
-
-def test_sphere_config_parity_and_accuracy():
-    """Config 2 (3 -> [128] x 4 -> 1, ~2.6e5 regions): the engine's fp32 run
-    is as close to the FP64 oracle as the oracle's own fp32 run is; both
-    disagree only at near-degenerate vertices."""
-    m = wl.sphere()
-    net = wl.net_arrays(m)
-    st, pt = wl.seeds_for(m, init_num=1024, seed=1)
-    eng = engine.march(net, st, pt, "float32")
-    reg = eng.regions()
-    o64 = O.run_oracle(net, st, pt, dtype="float64")
-    o32 = O.run_oracle(net, st, pt, dtype="float32")
-    ce = CM.parity_report(reg, o64, tol=1e-5)
-    co = CM.parity_report(o32, o64, tol=1e-5)
-    base_r = co["regions_only_a"] + co["regions_only_b"]
-    base_f = co["faces_count_mismatch"] + co["faces_beyond_tol"]
-    assert ce["regions_only_a"] + ce["regions_only_b"] <= 2 * base_r + 10, (ce, co)
-    assert ce["faces_count_mismatch"] + ce["faces_beyond_tol"] <= 2 * base_f + 20, (ce, co)
-    assert (ce["regions_only_a"] + ce["regions_only_b"]) <= 1e-4 * ce["regions_b"], ce
-    v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in range(reg.num) if reg.nverts[i] >= 3])
-    assert np.abs(f_at(net, v)).max() <= 1e-5
     eng.close()
 
 
@@ -171,22 +151,6 @@ def test_mesh_combine_quantised_weld():
     assert mesh.verts.shape == v.shape
     assert mesh.faces == f
     np.testing.assert_allclose(mesh.verts, v * 2.0 + np.array([0.1, -0.2, 0.3]), atol=1e-6)
-    eng.close()
-
-
-def test_watertight_sphere_mesh():
-    m = wl.sphere()
-    net = wl.net_arrays(m)
-    st, pt = wl.seeds_for(m, init_num=1024, seed=1)
-    eng = engine.march(net, st, pt, "float32")
-    mesh = eng.combine()
-    edges = {}
-    for f in mesh.faces:
-        for a, b in zip(f, f[1:] + f[:1]):
-            e = (min(a, b), max(a, b))
-            edges[e] = edges.get(e, 0) + 1
-    counts = np.array(list(edges.values()))
-    assert (counts == 2).mean() > 0.999
     eng.close()
 
 
