@@ -129,9 +129,29 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
                  : "memory");
 }
 
-// bounded wait on phase `parity`; false when the bound is reached
+// has phase `parity` completed?  (non-blocking)
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// bounded wait on phase `parity`; false when the bound is reached.  A phase
+// that has completed already is seen by the non-blocking test (measured on
+// GB300: try_wait took ~300 cycles even then, on the issuing thread's
+// critical path once per weight block)
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int max_iters)
 {
+    if (mbar_test(bar, parity)) return true;
     const uint32_t a = smem_addr(bar);
     for (int i = 0; i < max_iters; ++i) {
         uint32_t done;
