@@ -676,8 +676,13 @@ void run_begin(am_engine *e, const RunArgs &a)
         };
         TcNet ts = streamed_tile(1);
         if (tc.mtiles_max >= 2 && e->compose_tile != 2) {
+            // two passes pay for rebuilding the operand and a second epilogue
+            // per layer: automatically only for twice the tile width with two
+            // weight stages or more (measured on GB300: 3-[512]x8-1 faster
+            // with 128 columns in two passes than 64 in one, 3-[256]x6-1
+            // slower with a wider two-pass tile than 128 columns in one)
             const TcNet t2 = streamed_tile(2);
-            if (e->compose_tile == 3 || t2.ncols_max > ts.ncols_max) ts = t2;
+            if (e->compose_tile == 3 || (t2.ncols_max >= 2 * ts.ncols_max && t2.nstage >= 2)) ts = t2;
         }
         const bool want_streamed = e->compose_tile >= 2 ||
                                    (e->compose_tile == 0 && tc.kp_max >= 256 && ts.ncols_max > tc.ncols_max);

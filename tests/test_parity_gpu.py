@@ -57,9 +57,10 @@ def face_condition(eng, reg, rid):
     return worst
 
 
-def _drop_collinear(P, eps=1e-9):
-    """The polygon without vertices where it does not turn (a vertex on the
-    straight edge between its neighbours)."""
+def _drop_collinear(P, eps=1e-5):
+    """The polygon without vertices where it turns by less than eps radians
+    (a vertex on the straight edge between its neighbours, up to the
+    rounding of FP32 planes)."""
     n = len(P)
     keep = []
     for i in range(n):
