@@ -320,10 +320,17 @@ struct am_engine {
     int default_chunk() const
     {
         if (chunk_opt > 0) return (int)std::min<int64_t>(chunk_opt, (int64_t)(0x7fffffff / std::max(ALL, 1)));
+        // ~2 GiB of constraint rows per wave; a full wave of the tensor-core
+        // composition is a whole number of rounds of one tile per SM (a
+        // partly filled last round idles the other SMs)
         const size_t per = tc * 4 * (size_t)ALLP;
-        long long c = (long long)((1ull << 30) / std::max<size_t>(per, 1));
-        c = std::max<long long>(1024, std::min<long long>(c, 1 << 18));
+        long long c = (long long)((2ull << 30) / std::max<size_t>(per, 1));
+        c = std::max<long long>(1024, std::min<long long>(c, 1 << 19));
         c = std::min<long long>(c, 0x7fffffff / std::max(ALL, 1));
+        if (prec == kMixed && tcnet.ncols_max >= 16) {
+            const long long round = (long long)device_sms() * (tcnet.ncols_max / 4);
+            if (c > round) c = c / round * round;
+        }
         return (int)c;
     }
 

