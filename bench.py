@@ -54,10 +54,14 @@ REF_SAMPLE_REGIONS = 65536
 ERROR_SAMPLE = 4096  # regions of the error report
 # DRAM bytes (read + write) per region of the two heavy kernels in the mixed
 # form, from one ncu capture each (--set full, dram__bytes_read.sum +
-# dram__bytes_write.sum): the sphere workload's wave of 12,672 regions and the
-# deep workload's wave of ~40,150 regions
+# dram__bytes_write.sum): the sphere workload's wave of 12,672 regions, the
+# deep workload's wave of ~40,150 regions and the skip network's wave of ~12,030
 NCU_TRAFFIC_PER_REGION = {("sphere", "mixed"): {"compose": (1.214e6 + 45.631e6) / 12672,
                                                 "polygon": (109.571e6 + 4.067e6) / 12672},
+                          # a wave of ~12,030 regions of a bounded march (the full march is too
+                          # large to capture): per region, scaled to the step's regions
+                          ("large_skip", "mixed"): {"compose": (55.605e6 + 746.199e6) / 12030,
+                                                    "polygon": (805.019e6 + 15.494e6) / 12030},
                           ("deep", "mixed"): {"compose": (27.491e6 + 957.757e6) / 40150,
                                               "polygon": (1018.464e6 + 20.326e6) / 40150}}
 
