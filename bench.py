@@ -86,6 +86,9 @@ def parse():
                         "which cannot see kernels inside conditional graphs")
     p.add_argument("--profile", action="store_true",
                    help="warm-up + timed steps only (for ncu launch lists): no e2e, phase, plain or CPU legs")
+    p.add_argument("--max-regions", type=int, default=0,
+                   help="with --profile: stop every marching after the wave that passes this many regions "
+                        "(a bounded march small enough for a full ncu capture)")
     return p.parse_args()
 
 
@@ -460,8 +463,16 @@ def main():
     if args.host_loop:
         eng.set_option(_lib.AM_OPT_GRAPH, 0)
 
+    if args.profile and args.max_regions > 0:
+        eng.set_option(_lib.AM_OPT_MAX_REGIONS, args.max_regions)
+
     def step():
-        return eng.run(W, B, S, P, TM, None, None, net.iso, False, stream=stream)
+        try:
+            return eng.run(W, B, S, P, TM, None, None, net.iso, False, stream=stream)
+        except _lib.AmError as exc:  # the bounded march of --max-regions
+            if not (args.max_regions > 0 and exc.status == _lib.AM_ERR_CAPACITY):
+                raise
+            return eng.stats()
 
     for _ in range(args.warmup):
         step()
