@@ -52,9 +52,14 @@ class _Corr:
 
 def dichotomy(model, iso, init_num=1024, w_extra_constraints=None, b_extra_constraints=None, try_pts_num=4096,
               init_ball_radius=1.0, iter_max=100, avg_eps=1e-3, time_out=60, provided_surfpts=None,
-              provided_surfstd=None, generator=None, device="cpu", verbose=False):
+              provided_surfstd=None, generator=None, device="cpu", verbose=False, rng=None):
     """Pairs of opposite-sign samples, bisected until the mean |f - iso| is
-    below ``avg_eps`` (backend/main.py:252-326).  Returns (init_num, 3) fp32."""
+    below ``avg_eps`` (backend/main.py:252-326).  Returns (init_num, 3) fp32.
+
+    ``rng`` (a ``random.Random``): draw the pairs as the reference does, by
+    ``rng.sample`` over the n_pos x n_neg products and a float division for
+    the negative index -- with ``generator`` seeded like the reference's
+    global torch RNG, the same points from the same draws."""
     t0 = time.time()
     neg = torch.zeros([0, 3], device=device)
     pos = torch.zeros([0, 3], device=device)
@@ -75,9 +80,15 @@ def dichotomy(model, iso, init_num=1024, w_extra_constraints=None, b_extra_const
         if n_pos and n_neg:
             n_range = n_pos * n_neg
             n_sample = min(init_num - neg.shape[0], n_range)
-            index = torch.randperm(n_range, generator=generator)[:n_sample].to(device)
+            if rng is not None:
+                index = torch.tensor(rng.sample(range(n_range), n_sample))
+                index_neg = (index / n_pos).long().to(device)
+                index = index.to(device)
+            else:
+                index = torch.randperm(n_range, generator=generator)[:n_sample].to(device)
+                index_neg = index // n_pos
             pos = torch.cat([pos, pts[id_pos[index % n_pos]]], dim=0)
-            neg = torch.cat([neg, pts[id_neg[index // n_pos]]], dim=0)
+            neg = torch.cat([neg, pts[id_neg[index_neg]]], dim=0)
             if verbose:
                 print("(am) (dichotomy) n_pos = %d | n_neg = %d" % (n_pos, n_neg))
     mid = (neg + pos) / 2

@@ -11,7 +11,9 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """The marching fixtures (seeds_*.npz hold seed-point fixtures instead)."""
+    all_ = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    return [n for n in all_ if not n.startswith("seeds_")]
 
 
 def load(name):

@@ -51,3 +51,28 @@ def test_dichotomy_is_reproducible_with_a_generator(model):
 def test_gradient_descent_rejects_unknown_loss(model):
     with pytest.raises(ValueError):
         S.gradient_descent(model, 0.0, init_num=8, loss_type="huber")
+
+
+def test_dichotomy_pinned_to_the_reference_draws():
+    """The reference's own dichotomy (backend/main.py:252-326), run with its
+    global RNGs seeded, gave tests/golden/seeds_dichotomy.npz
+    (tests/golden/make_seed_golden.py); with the same draws -- a torch
+    generator seeded like the global one, a random.Random seeded like
+    Python's -- this implementation gives the same points, bit for bit."""
+    import os
+    import random
+
+    import numpy as np
+
+    from analyticmesh_gb300 import seeds, workloads as wl
+
+    here = os.path.dirname(os.path.abspath(__file__))
+    gold = np.load(os.path.join(here, "golden", "seeds_dichotomy.npz"))
+    cases = [(7, [32, 32], 0.0, 256, 1024, 5), (12, [48, 48, 48], 0.05, 200, 2048, 9)]
+    for c, (nseed, widths, iso, n, tries, seed) in enumerate(cases):
+        model = wl.geometric(widths, nseed, perturb=0.05 if len(widths) > 2 else 0.0).float().eval()
+        with torch.no_grad():
+            pts = seeds.dichotomy(model, iso, init_num=n, try_pts_num=tries, init_ball_radius=1.0, iter_max=100,
+                                  avg_eps=1e-3, time_out=60, generator=torch.Generator().manual_seed(seed),
+                                  rng=random.Random(seed))
+        assert np.array_equal(pts.numpy(), gold["points%d" % c]), c
