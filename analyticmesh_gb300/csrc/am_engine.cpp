@@ -206,6 +206,7 @@ struct am_engine {
         int chunks = 0;
         double t_comp = 0, t_poly = 0, t_front = 0;
         bool flip = false;
+        bool lean = false; // batch member: the wave buffers grow with the queue
     } run;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, pa = nullptr, pb = nullptr;
     bool lean = false; // batch member: region store and table start small and grow on demand
@@ -772,6 +773,7 @@ void run_begin(am_engine *e, const RunArgs &a)
     r.chunks = 0;
     r.t_comp = r.t_poly = r.t_front = 0;
     r.flip = a.flip_insideout != 0;
+    r.lean = e->lean;
 }
 
 // graph-driven loop: one graph launch runs up to max_waves waves, until the
@@ -782,8 +784,19 @@ void run_graph_launch(am_engine *e, int max_waves)
 {
     am_engine::Run &r = e->run;
     cudaStream_t st = e->st;
-    e->ensure_chunk(r.chunk);
-    const int count = (int)std::min<long long>(r.tail - r.head, r.chunk);
+    // the largest wave of this launch: the chunk, or for a batch member the
+    // queue's length rounded up to a power of two (at most the chunk), so
+    // that many small networks do not each hold a full chunk of rows; the
+    // loop stops when the queue outgrows it and the next launch grows it
+    const long long pending = r.tail - r.head;
+    int wave = r.chunk;
+    if (r.lean) {
+        long long w = std::max(e->chunk_cap, 1024);
+        while (w < pending && w < r.chunk) w *= 2;
+        wave = (int)std::min<long long>(w, r.chunk);
+    }
+    e->ensure_chunk(wave);
+    const int count = (int)std::min<long long>(pending, wave);
     e->ensure_regions(r.tail + (long long)count * kVMax);
     e->ensure_table(std::max<long long>(r.tail + (long long)count * kVMax, e->cap), true);
     WaveCtl *h = e->h_ctl;
@@ -791,14 +804,15 @@ void run_graph_launch(am_engine *e, int max_waves)
     h->count = count;
     h->waves = 0;
     h->limit = e->table_slots > 0 ? e->cap : std::min<long long>(e->cap, (long long)(e->hcap / 2));
-    h->chunk_cap = r.chunk;
+    h->chunk_cap = wave;
+    h->grow_at = wave < r.chunk ? (int)std::min<long long>(2ll * wave, INT_MAX) : INT_MAX;
     h->work = 0u;
     h->max_waves = max_waves;
     h->stop_tail = e->max_regions > 0 ? e->max_regions : LLONG_MAX;
     // tail and err stay as the device has them
     AM_CUDA(cudaMemcpyAsync((char *)e->d_tail.p + offsetof(WaveCtl, head), (char *)h + offsetof(WaveCtl, head),
                             sizeof(WaveCtl) - offsetof(WaveCtl, head), cudaMemcpyHostToDevice, st));
-    e->run_wave_graph(r.prec, e->net, r.iso, r.tol, r.chunk);
+    e->run_wave_graph(r.prec, e->net, r.iso, r.tol, wave);
     AM_CUDA(cudaMemcpyAsync(h, e->d_tail.p, sizeof(WaveCtl), cudaMemcpyDeviceToHost, st));
 }
 

@@ -257,7 +257,8 @@ __global__ void __launch_bounds__(kScanBlock) append_write_kernel(AppendArgs a)
 }
 
 // graph-driven loop: retire the wave, take the next one from the queue and
-// go on while it is non-empty, no error bit is set and its children fit
+// go on while it is non-empty, no error bit is set, its children fit and the
+// queue has not outgrown the wave buffers of a batch member
 __global__ void wave_step_kernel(WaveCtl *ctl, cudaGraphConditionalHandle cond)
 {
     WaveCtl &c = *ctl;
@@ -268,7 +269,7 @@ __global__ void wave_step_kernel(WaveCtl *ctl, cudaGraphConditionalHandle cond)
     c.work = 0u;
     const bool go = c.count > 0 && c.err == 0 &&
                     c.tail + (long long)c.count * kVMax <= c.limit && c.waves < c.max_waves &&
-                    c.tail <= c.stop_tail;
+                    c.tail <= c.stop_tail && rem <= (long long)c.grow_at;
     cudaGraphSetConditional(cond, go ? 1u : 0u);
 }
 

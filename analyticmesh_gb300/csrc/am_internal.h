@@ -83,7 +83,7 @@ struct WaveCtl {
     int chunk_cap;      // largest wave
     unsigned int work;  // next region of the wave for the polygon warps
     int max_waves;      // waves one graph launch may run
-    int pad1;
+    int grow_at;        // stop while more regions than this wait (a batch member's wave buffers grow with its queue)
     long long stop_tail; // stop after the wave that takes tail past this (a region limit)
 };
 

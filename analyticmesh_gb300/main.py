@@ -59,9 +59,10 @@ def AnalyticMarching(model, save_ply_path="mesh.ply", iso=0.0, scale=1.0, center
 
     Returns ``{"init_point_time", "init_cuda_time", "am_time", "export_time",
     "vertices", "faces", "stats"}``; writes ``save_ply_path`` unless it is None.
-    In voxel mode (``voxel_configs``) every occupied voxel is marched on its
-    own and the sub-meshes are concatenated; ``stats`` then describes the
-    last voxel's marching.
+    In voxel mode (``voxel_configs``) every occupied voxel is marched with its
+    6 faces as extra constraints, all voxels at once (one batched run), and
+    the sub-meshes are concatenated; ``stats`` then sums the voxels' counts
+    and ``voxel_boxes`` holds the occupied voxels' lower corners.
     """
     global _ENVIRONMENT
     init_configs = copy.deepcopy(init_configs if init_configs is not None else DICHOTOMY_DICT)
@@ -129,46 +130,59 @@ def AnalyticMarching(model, save_ply_path="mesh.ply", iso=0.0, scale=1.0, center
         out["stats"] = cuam.engine().stats()
         return out
 
-    # voxel mode (backend/main.py:475-556): one marching per occupied voxel with
-    # the voxel's 6 faces as extra constraints; sub-meshes concatenated
+    # voxel mode (backend/main.py:475-556): every occupied voxel is marched
+    # with the voxel's 6 faces as extra constraints -- here all voxels at
+    # once, one engine each, in one am_run_batch (the reference loops over
+    # the voxels one marching after the other); sub-meshes concatenated
+    from . import engine as _engine
+
     vs = float(voxel_configs["voxel_size"])
     idx3 = torch.floor(points.double() / vs).long()
     imin = idx3.min(0).values
     idx3 = idx3 - imin
     dim = idx3.max(0).values + 1
     idx1 = idx3[:, 0] * dim[1] * dim[2] + idx3[:, 1] * dim[2] + idx3[:, 2]
-    am_t = ex_t = 0.0
-    all_v, all_f, nv = [], [], 0
+    engines, nets, sts, pts, lows = [], [], [], [], []
+    arc_np = arc_table.numpy()
     for cell in torch.unique(idx1).tolist():
         sel = torch.where(idx1 == cell)[0]
         c0 = cell // int(dim[1] * dim[2])
         c1 = (cell % int(dim[1] * dim[2])) // int(dim[2])
         c2 = cell % int(dim[2])
         lo = [(int(imin[0]) + c0) * vs, (int(imin[1]) + c1) * vs, (int(imin[2]) + c2) * vs]
+        lows.append(lo)
         w_b, b_b = get_boundary("cube", min_vert=lo, max_vert=[x + vs for x in lo])
         w_all = torch.cat([w_b.to(dtype=tt, device=dev) + CONSTRAINTS_JITTER, w_extra]).contiguous()
         b_all = torch.cat([b_b.to(dtype=tt, device=dev), b_extra]).contiguous()
-        t0 = time.time()
-        cuam.AnalyticMarching(weights=weights, biases=biases, states=states[sel].contiguous(),
-                              points=points[sel].contiguous(), arc_tm=arc_tm, w_extra_constraints=w_all,
-                              b_extra_constraints=b_all, iso=iso, flip_insideout=flip_insideout)
-        torch.cuda.synchronize()
-        am_t += time.time() - t0
-        t0 = time.time()
-        m = cuam.CombineMesh(scale=scale, center=list(center))
-        ex_t += time.time() - t0
+        nets.append(type("VoxelNet", (), dict(W=weights, b=biases, tms=arc_tm, w_extra=w_all, b_extra=b_all)))
+        sts.append(states[sel].to(torch.uint8).contiguous())
+        pts.append(points[sel].contiguous())
+        engines.append(_engine.Engine(ft, model.nodes, arc_np, num_extra))
+    t0 = time.time()
+    _engine.run_batch(engines, nets, sts, pts, iso, flip_insideout)
+    torch.cuda.synchronize()
+    out["am_time"] = time.time() - t0
+    t0 = time.time()
+    all_v, all_f, nv = [], [], 0
+    stats = {}
+    for e in engines:
+        m = e.combine(scale=scale, center=tuple(center))
         all_v.append(m.verts)
         all_f.extend([[i + nv for i in f] for f in m.faces])
         nv += len(m.verts)
+        for k, v in e.stats().items():
+            if k.startswith("num_") or k.startswith("mesh_num"):
+                stats[k] = stats.get(k, 0) + v
+        e.close()
     verts = np.concatenate(all_v) if all_v else np.zeros((0, 3))
-    t0 = time.time()
     if save_ply_path is not None:
         write_ply(save_ply_path, verts, all_f, save_polymesh, save_float32_verts)
-    out["am_time"] = am_t
-    out["export_time"] = ex_t + time.time() - t0
+    stats["voxels"] = len(engines)
+    out["export_time"] = time.time() - t0
+    out["voxel_boxes"] = np.asarray(lows, np.float64).reshape(-1, 3)  # lower corners; edge voxel_size
     out["vertices"] = verts
     out["faces"] = all_f
-    out["stats"] = cuam.engine().stats()
+    out["stats"] = stats
     return out
 
 

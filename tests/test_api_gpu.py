@@ -59,19 +59,71 @@ def test_saved_and_loaded_network_marches_and_writes_its_mesh(tmp_path, dtype):
     assert [list(map(int, f)) for f in pf] == [list(map(int, f)) for f in faces]
 
 
-def test_voxel_mode_meshes_on_the_level_set():
+def _poly_area(p):
+    """Area of a planar polygon (k, 3)."""
+    if len(p) < 3:
+        return 0.0
+    c = np.cross(p[1:-1] - p[0], p[2:] - p[0])
+    return 0.5 * np.linalg.norm(c.sum(0))
+
+
+def _clip_box(p, lo, hi):
+    """A convex polygon (k, 3) clipped to the box [lo, hi] (Sutherland-Hodgman)."""
+    for ax in range(3):
+        for sgn, lim in ((1.0, hi[ax]), (-1.0, lo[ax])):
+            if len(p) == 0:
+                return p
+            d = sgn * (p[:, ax] - lim)  # <= 0 inside
+            out = []
+            for i in range(len(p)):
+                a, b, da, db = p[i], p[(i + 1) % len(p)], d[i], d[(i + 1) % len(p)]
+                if da <= 0:
+                    out.append(a)
+                if (da < 0 < db) or (db < 0 < da):
+                    out.append(a + (b - a) * (da / (da - db)))
+            p = np.asarray(out).reshape(-1, 3)
+    return p
+
+
+def test_voxel_mode_meshes_the_surface_inside_each_voxel():
+    """Voxel mode marches all occupied voxels in one batched run, each with
+    its 6 faces as extra constraints: every vertex is on the level set, and a
+    voxel's mesh covers the part of the whole surface inside that voxel --
+    its area is the area of the whole marching's mesh clipped to the voxel
+    (a voxel may miss a piece of the surface that holds none of its seeds,
+    and then has less, never more)."""
     model = wl.geometric([32, 32], 7)
     net = wl.net_arrays(model)
-    out = AnalyticMarching(model, None, dtype=torch.float64, voxel_configs={"voxel_size": 0.25},
+    vs = 0.25
+    out = AnalyticMarching(model, None, dtype=torch.float64, voxel_configs={"voxel_size": vs},
                            generator=torch.Generator().manual_seed(2))
     verts, faces = np.asarray(out["vertices"]), out["faces"]
     _check_mesh(verts, faces)
     assert np.abs(_f64(net, verts)).max() <= F_TOL[torch.float64]
-    # every vertex lies on the surface of the unvoxelised network, which a
-    # whole marching of the same network covers: the same bounding box
+    boxes = out["voxel_boxes"]
+    assert out["stats"]["voxels"] == len(boxes) > 1
+    assert out["stats"]["num_faces"] == len(faces)
     whole = AnalyticMarching(model, None, dtype=torch.float64, generator=torch.Generator().manual_seed(2))
     wv = np.asarray(whole["vertices"])
-    assert np.all(verts.min(0) >= wv.min(0) - 1e-9) and np.all(verts.max(0) <= wv.max(0) + 1e-9)
+    wpolys = [wv[np.asarray(f)] for f in whole["faces"]]
+    wlo = np.array([p.min(0) for p in wpolys])
+    whi = np.array([p.max(0) for p in wpolys])
+    vpolys = [verts[np.asarray(f)] for f in faces]
+    cent = np.array([p.mean(0) for p in vpolys])
+    agree, total_v, total_w = 0, 0.0, 0.0
+    for lo in boxes:
+        hi = lo + vs
+        # the voxel's own faces (centroids inside the box)
+        inside = np.all((cent >= lo - 1e-9) & (cent <= hi + 1e-9), axis=1)
+        a_vox = sum(_poly_area(vpolys[i]) for i in np.where(inside)[0])
+        near = np.where(np.all((whi >= lo) & (wlo <= hi), axis=1))[0]
+        a_whole = sum(_poly_area(_clip_box(wpolys[i], lo, hi)) for i in near)
+        assert a_vox <= a_whole * (1 + 1e-6) + 1e-12, (lo, a_vox, a_whole)
+        agree += abs(a_vox - a_whole) <= 1e-6 * max(a_whole, 1e-6)
+        total_v += a_vox
+        total_w += a_whole
+    assert agree >= 0.9 * len(boxes), (agree, len(boxes))
+    assert total_v >= 0.97 * total_w
 
 
 def test_export_triangles_and_double_vertices(tmp_path):
