@@ -267,6 +267,18 @@ struct am_engine {
         return r;
     }
     HashDev hashdev() const { return HashDev{table.as<unsigned long long>(), hcap - 1}; }
+    // the region store, the table and the wave buffers go back to the device
+    // (the next run allocates them afresh); the engine keeps no result
+    void release_run_buffers()
+    {
+        drop_graph();
+        for (DevBuf *b : {&keys, &hash, &mid, &start, &nv, &status, &verts, &edges, &table, &cons, &eq, &rec, &blocksum})
+            b->reset();
+        cap = 0;
+        hcap = 0;
+        chunk_cap = 0;
+        num_regions = 0;
+    }
 
     void ensure_regions(long long need)
     {
@@ -1164,11 +1176,13 @@ int am_autotune(am_engine *e, const am_run_args *x, int64_t sample_regions, int3
         e->has_am = false;
         e->has_mesh = false;
         e->limit_hit = false;
+        e->lean = true; // stores sized to the sample, not to a full chunk
         const int rc = guarded(e, [&] {
             run_begin(e, a);
             run_host_loop(e);
             run_end(e);
         });
+        e->lean = false;
         if (rc != AM_OK) last_rc = rc;
         comp = e->stats.compose_ms;
         poly = e->stats.polygon_ms;
@@ -1193,6 +1207,11 @@ int am_autotune(am_engine *e, const am_run_args *x, int64_t sample_regions, int3
     e->has_am = false; // the samples are not a result
     e->has_mesh = false;
     e->limit_hit = false;
+    // many engines are tuned before a batch: none keeps its sample's stores
+    guarded(e, [&] {
+        AM_CUDA(cudaStreamSynchronize(e->st));
+        e->release_run_buffers();
+    });
     if (best_ct < 0 || best_fw < 0) {
         e->compose_tile = keep_ct;
         e->face_warps = keep_fw;

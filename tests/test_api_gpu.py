@@ -143,3 +143,52 @@ def test_export_triangles_and_double_vertices(tmp_path):
     fans = [[int(f[0]), int(f[j + 1]), int(f[j + 2])] for f in mesh.faces for j in range(len(f) - 2)]
     assert [list(map(int, f)) for f in pf] == fans
     eng.close()
+
+
+def test_reference_call_sequence_through_the_cuam_drop_in(tmp_path):
+    """The reference's own sequence of backend/main.py:376-472 with
+    ``from analyticmesh_gb300 import cuam as cuamlib`` in place of
+    ``build.cuam``: the same tensor preparation (bool states and points moved
+    to the CPU and back, int32 CPU arc table, jittered extra constraints),
+    Destroy at re-initialisation, Init, AnalyticMarching, CombineMesh,
+    ExportMesh; the PLY written is the marching's welded mesh."""
+    from analyticmesh_gb300 import cuam as cuamlib
+    from analyticmesh_gb300.seeds import dichotomy
+
+    model = wl.geometric([32, 32], 7).cuda().eval()
+    net = wl.net_arrays(model)
+    dtype = torch.float64
+    w_ex, b_ex = torch.zeros([0, 3]), torch.zeros([0])
+    points = dichotomy(model, 0.0, init_num=256, generator=torch.Generator().manual_seed(5), device="cuda")
+    with torch.no_grad():
+        model(points, requires_outputs_list=True)
+        states = torch.cat([(s > 0) for s in model.outputs_list], dim=1)
+        model.outputs_list = []
+    info = model.get_info()
+    arc_table = info["arc_table"].to(dtype=torch.int32).cpu()
+    weights = [w.to(dtype=dtype).cuda() for w in info["weights"]]
+    biases = [b.to(dtype=dtype).cuda() for b in info["biases"]]
+    states = states.to(dtype=torch.bool).cpu()
+    points = points.to(dtype=dtype).cpu()
+    arc_tm = [t.to(dtype=dtype).cuda() for t in info["arc_tm"]]
+    w_extra = w_ex.to(dtype=dtype).cuda()
+    b_extra = b_ex.to(dtype=dtype).cuda()
+    w_extra += 1e-8
+    faces = []
+    for rep in range(2):  # the second pass re-initialises as after an architecture change
+        if rep:
+            cuamlib.Destroy()
+        cuamlib.Init(float_type="float64", nodesnum=model.nodes, arc_table=arc_table, num_extra_constraints=0)
+        cuamlib.AnalyticMarching(weights=weights, biases=biases, states=states.cuda(), points=points.cuda(),
+                                 arc_tm=arc_tm, w_extra_constraints=w_extra, b_extra_constraints=b_extra, iso=0.0,
+                                 flip_insideout=False)
+        mesh = cuamlib.CombineMesh(scale=1.0, center=[0.0, 0.0, 0.0])
+        ply = str(tmp_path / ("m%d.ply" % rep))
+        cuamlib.ExportMesh(file_path=ply, is_polymesh=True, is_float32=False)
+        pv, pf = read_ply(ply)
+        assert np.array_equal(pv, mesh.verts)
+        assert [list(map(int, f)) for f in pf] == [list(map(int, f)) for f in mesh.faces]
+        assert np.abs(_f64(net, pv)).max() <= F_TOL[torch.float64]
+        faces.append(len(pf))
+    cuamlib.Destroy()
+    assert faces[0] == faces[1] > 0

@@ -115,3 +115,24 @@ def test_batch_and_option_argument_checks():
     assert L.am_set_option(None, _lib.AM_OPT_MAX_REGIONS, 10) == 2
     assert L.am_set_option(None, _lib.AM_OPT_FACE_WARPS, 2) == 2
     assert L.am_autotune(None, args, 1000, None) == 2                 # AM_ERR_NOT_INITIALIZED
+
+
+def test_reference_main_calls_bind_to_the_cuam_drop_in():
+    """Every ``cuamlib.X(...)`` call in the reference's backend/main.py (read
+    as text from the reference checkout, when present) binds to the drop-in's
+    function of that name: same names, same keyword arguments."""
+    import ast
+    import inspect
+
+    from oracle import build_ref
+
+    path = os.path.join(build_ref.REF_ROOT, "backend", "main.py")
+    if not os.path.exists(path):
+        pytest.skip("reference checkout not present")
+    tree = ast.parse(open(path).read())
+    calls = [n for n in ast.walk(tree) if isinstance(n, ast.Call) and isinstance(n.func, ast.Attribute)
+             and isinstance(n.func.value, ast.Name) and n.func.value.id == "cuamlib"]
+    assert {c.func.attr for c in calls} == {"Init", "AnalyticMarching", "CombineMesh", "ExportMesh", "Destroy"}
+    for c in calls:
+        fn = getattr(cuam, c.func.attr)
+        inspect.signature(fn).bind(*[None] * len(c.args), **{k.arg: None for k in c.keywords})

@@ -166,12 +166,13 @@ def test_polytope_float32_against_the_reference_golden_run():
     assert len(ok) >= 40
     assert on_surface(np.concatenate([reg.verts[i, :reg.nverts[i]] for i in ok]))
     # common faces: the same polygon within 1e-5, or -- where a slab's
-    # planes cut it differently in the two FP32 runs -- both polygons pieces
-    # of the exact surface
+    # planes cut it differently in the two FP32 runs -- ours a piece of the
+    # exact surface; the reference's FP32 walk itself leaves a vertex off the
+    # surface on some of these (counted, a handful at most)
     sa, sb, ra, rb = CM._matched(reg, gold, 3)
     d, count_differs = CM._pair_distances(reg, gold, ra, rb)
     assert len(ra) >= 20
-    same = 0
+    same = ref_off = 0
     for j in range(len(ra)):
         if not count_differs[j] and d[j] <= TOL:
             same += 1
@@ -179,8 +180,9 @@ def test_polytope_float32_against_the_reference_golden_run():
         if reg.status[ra[j]] != 0:
             continue
         assert on_surface(reg.verts[ra[j], :reg.nverts[ra[j]]]), int(ra[j])
-        assert on_surface(gold.verts[rb[j], :gold.nverts[rb[j]]]), int(rb[j])
+        ref_off += not on_surface(gold.verts[rb[j], :gold.nverts[rb[j]]])
     assert same >= len(ra) // 2, (same, len(ra))
+    assert ref_off <= 3, ref_off
     eng.close()
 
 
