@@ -909,46 +909,83 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                 const int M = net.nodes[i + 1];
                 const int mtiles = (M + 127) / 128;
                 const int mper = (mtiles + tc.mgroups - 1) / tc.mgroups;
+                const int njobs = jobs_of(net, i);
+                // X[4r + c][k] = s_k(r) ? -C[r][k][c] : 0 (layer 1: +W0 rows
+                // from shared memory), one 64-deep K block at a time; every
+                // pass of the layer streams the same blocks.  Thread tid owns
+                // the items q = tid + u kSBuild (region q % R, row q / R of the
+                // block): regions fastest across the lanes.  The first four
+                // items of the next block are loaded before this block's
+                // stage wait and stores, so that their latency hides behind
+                // them (measured on GB300: with the loads of a block issued
+                // after its wait, building a block took longer than its
+                // products); raw values are kept and signed when stored.
+                auto load_items = [&](int job, int kb, int c, float4 *v) {
+                    int src;
+                    job_mat(net, tc, i, job, src);
+                    const int K = net.nodes[src], rows0 = net.hoff[src];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int q = tid + (4 * c + u) * kSBuild;
+                        const int r = q % R, k = kb * 64 + q / R;
+                        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (q < R * 64 && r < nreg && k < K && key_bit(keys + (size_t)r * KW, rows0 + k))
+                            x = src == 1 ? w0s[k] : ld4<float>(cons + (size_t)r * rstride + (size_t)(rows0 + k) * 4);
+                        v[u] = x;
+                    }
+                };
+                auto put_items = [&](const XOp &X, int c, const float4 *v, float sg) {
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int q = tid + (4 * c + u) * kSBuild;
+                        if (q < R * 64) {
+                            const float x[4] = {sg * v[u].x, sg * v[u].y, sg * v[u].z, sg * v[u].w};
+                            X.put<2>(4 * (q % R), q / R, x);
+                        }
+                    }
+                };
+                const int nchunks = (R * 64 + 4 * kSBuild - 1) / (4 * kSBuild);
+                float4 pre[4];
+                load_items(0, 0, 0, pre);
                 for (int mt0 = 0; mt0 < mtiles; mt0 += mper) { // the products of this group of M tiles
                 const int mt1 = min(mtiles, mt0 + mper);
-                const int njobs = jobs_of(net, i);
                 for (int job = 0; job < njobs; ++job) {
                     int src;
                     const TcMat &mat = job_mat(net, tc, i, job, src);
-                    const int K = net.nodes[src], rows0 = net.hoff[src];
-                    for (int kb = 0; kb < mat.Kp / 64; ++kb) {
+                    const float sg = src == 1 ? 1.f : -1.f;
+                    const int nkb = mat.Kp / 64;
+                    for (int kb = 0; kb < nkb; ++kb) {
+                        // the next block of this pass, else the next pass's first
+                        // (its rows were written before this layer began)
+                        int njob = job, nkb2 = kb + 1;
+                        bool more = true;
+                        if (nkb2 == nkb) {
+                            nkb2 = 0;
+                            if (++njob == njobs) {
+                                njob = 0;
+                                more = mt1 < mtiles;
+                            }
+                        }
+                        float4 nxt[4];
+                        if (more) load_items(njob, nkb2, 0, nxt);
                         const int xs = xb & 1, fill = xb >> 1;
                         // stage free (an aborting CTA builds nothing but still arrives)
                         const bool ok = fill < 1 ? !*abort : swait(xdone + xs, (uint32_t)((fill - 1) & 1), err, abort);
                         const XOp &X = XS[xs];
-                        // X[4r + c][k] = s_k(r) ? -C[r][k][c] : 0 for the block's 64 rows k,
-                        // regions fastest across the lanes; two loads in flight per thread
-                        for (int q0 = tid; ok && q0 < R * 64; q0 += 2 * kSBuild) {
-                            float x[2][4];
-#pragma unroll
-                            for (int u = 0; u < 2; ++u) {
-                                const int q = q0 + u * kSBuild;
-                                const int r = q % R, kk = q / R, k = kb * 64 + kk;
-                                x[u][0] = x[u][1] = x[u][2] = x[u][3] = 0.f;
-                                if (q < R * 64 && r < nreg && k < K && key_bit(keys + (size_t)r * KW, rows0 + k)) {
-                                    if (src == 1) {
-                                        const float4 w = w0s[k];
-                                        x[u][0] = w.x, x[u][1] = w.y, x[u][2] = w.z, x[u][3] = w.w;
-                                    } else {
-                                        const float4 c = ld4<float>(cons + (size_t)r * rstride + (size_t)(rows0 + k) * 4);
-                                        x[u][0] = -c.x, x[u][1] = -c.y, x[u][2] = -c.z, x[u][3] = -c.w;
-                                    }
-                                }
-                            }
-#pragma unroll
-                            for (int u = 0; u < 2; ++u) {
-                                const int q = q0 + u * kSBuild;
-                                if (q < R * 64) X.put<2>(4 * (q % R), q / R, x[u]);
+                        if (ok) {
+                            put_items(X, 0, pre, sg);
+                            for (int c = 1; c < nchunks; ++c) {
+                                float4 t4[4];
+                                load_items(job, kb, c, t4);
+                                put_items(X, c, t4, sg);
                             }
                         }
                         umma::fence_proxy_async(); // generic-proxy stores -> the tensor cores
                         mbar_arrive(xfull + xs);
                         ++xb;
+                        if (more)
+#pragma unroll
+                            for (int u = 0; u < 4; ++u) pre[u] = nxt[u];
                     }
                 }
                 const float *bias = (const float *)net.bias[i];

@@ -361,8 +361,8 @@ struct am_engine {
         if (e & kErrNonFinite)
             throw Failure{AM_ERR_INVALID_ARGUMENT, "weights, biases, transforms or extra constraints hold NaN or infinity"};
         if (e & kErrWait)
-            throw Failure{AM_ERR_CUDA, "device wait limit reached: a tensor-core pipeline barrier wait ran out, "
-                                       "the kernel stopped issuing work and the run's results are not valid"};
+            throw Failure{AM_ERR_CUDA, "device wait limit reached: a bounded barrier wait (tensor-core pipeline or "
+                                       "row copy) ran out, and the run's results are not valid"};
         if (e & kErrTableFull) throw Failure{AM_ERR_TABLE_FULL, "hash probe bound reached"};
         if (e & kErrCapacity) throw Failure{AM_ERR_CAPACITY, "region store capacity exceeded"};
     }

@@ -31,6 +31,7 @@
 
 #include "am_device.cuh"
 #include "am_internal.h"
+#include "am_umma.cuh"
 
 namespace am {
 
@@ -216,15 +217,18 @@ __device__ int warp_insert(const RegionsDev &reg, const HashDev &hs, long long h
 // warp per face with no barrier.
 constexpr int kListCap = 384;  // rows the pruned walk keeps at most (more: the walk scans every row)
 constexpr int kPruneMin = 96;  // fewer rows than this: no pruning
+constexpr int kRowWaitIters = 1 << 22; // bound of the wait for a face's rows (bulk copy)
 
 template <typename TC>
 struct GroupShared {
     long long rl;   // the group's region (chunk-local)
+    uint64_t rbar;  // the face's rows have landed (bulk copy)
     int done, near; // the leader's refinement outcome; a warp met a row near a vertex
     TC bt[2][8];    // partial minima per step parity and warp
     double btd[2][8]; // the same for a scan in FP64 over FP32 rows
     int bk[2][8];
     int nlist;      // rows kept by the pruning
+    int ve[kVMax];  // the face's neighbour planes by edge (-1: none), from the leader
     // row pruning: first the sample's extreme rows per warp and direction,
     // then (once every warp has read those) the list of the rows kept
     union {
@@ -875,6 +879,11 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
     // graph-driven loop) from the wave's work counter; the leader takes it
     // and the group reads it from shared memory
     long long rl_next = (long long)blockIdx.x * F + gid;
+    if (g.gw == 0 && lane == 0) {
+        umma::mbar_init(&g.sh->rbar, 1);
+        umma::fence_mbar_init();
+    }
+    uint32_t rphase = 0; // faces taken by this group: the row barrier's phase
     for (;;) {
         long long rl;
         if (g.gw == 0) {
@@ -892,8 +901,25 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         if (rl >= count) break;
         const long long rid = head + rl;
         const vec4_t<TC> *grows = reinterpret_cast<const vec4_t<TC> *>((const TC *)ch.cons + (size_t)rl * net.ALLP * 4);
+        // the region's rows into shared memory by one bulk copy (the leader
+        // issues it once every warp of the group is done with the previous
+        // face's rows), then normalised in place
+        {
+            const uint32_t rbytes = (uint32_t)ALL * (uint32_t)sizeof(vec4_t<TC>);
+            if (!kGroup) __syncwarp(); // (a group has met at its barrier above)
+            if (g.gw == 0 && lane == 0) {
+                umma::fence_proxy_async(); // earlier generic reads of the rows before the copy's writes
+                umma::mbar_expect_tx(&g.sh->rbar, rbytes);
+                umma::bulk_g2s(rows, grows, rbytes, &g.sh->rbar);
+            }
+            if (!umma::mbar_wait(&g.sh->rbar, rphase & 1u, kRowWaitIters)) {
+                atomicOr(err, kErrWait);
+                umma::mbar_wait(&g.sh->rbar, rphase & 1u, kRowWaitIters); // nothing lands after the face is left
+            }
+            ++rphase;
+        }
         for (int q = 32 * g.gw + lane; q < ALL; q += 32 * G) {
-            vec4_t<TC> v = grows[q];
+            vec4_t<TC> v = rows[q];
             const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
             if (n2 > TC(0)) {
                 const TC inv = rsqrt(n2); // as the reference's distance normalisation
@@ -1030,14 +1056,14 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
                 }
             }
         }
-        if (kGroup && g.gw != 0) continue; // the leader writes the face
+        const bool leader = !kGroup || g.gw == 0;
 
         // ---------------------------------------------------- outputs
-        if (lane == 0) {
+        if (leader && lane == 0) { // the leader writes the face
             reg.nv[rid] = n;
             reg.status[rid] = status;
         }
-        if (lane < n) {
+        if (leader && lane < n) {
             TS *vo = (TS *)reg.verts + ((size_t)rid * kVMax + lane) * 3;
             vo[0] = vx;
             vo[1] = vy;
@@ -1046,20 +1072,32 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         }
 
         // ---------------------------------------------------- neighbours
-        // one neighbour after the other, each inserted by the whole warp
+        // the plane crossed by edge `lane` where a neighbour is to be
+        // inserted (else -1), published by the leader; warp gw of the group
+        // inserts the neighbours of the edges lane = gw (mod G), one after
+        // the other, each by the whole warp (measured on GB300: with the
+        // leader inserting all of them the other warps waited at the next
+        // face's barrier)
+        int kv = -1;
+        if (leader && lane < n && ve >= 0 && ve < N && (closed || lane < n - 1) && !(!is_seed && ve == s)) kv = ve;
+        if (kGroup) {
+            if (g.gw == 0) g.sh->ve[lane] = kv;
+            g.sync();
+            kv = g.sh->ve[lane];
+        }
+        const bool mine = !kGroup || lane % G == g.gw;
         int rec = -1;
         const uint32_t *pkey = reg.keys + (size_t)rid * W;
-        const bool spawn = lane < n && ve >= 0 && ve < N && (closed || lane < n - 1) && !(!is_seed && ve == s);
-        unsigned todo = __ballot_sync(0xffffffffu, spawn);
+        unsigned todo = __ballot_sync(0xffffffffu, mine && kv >= 0);
         const uint64_t phash = reg.hash[rid];
         while (todo) {
             const int src = __ffs(todo) - 1;
             todo &= todo - 1u;
-            const int k = __shfl_sync(0xffffffffu, ve, src);
+            const int k = __shfl_sync(0xffffffffu, kv, src);
             const int got = warp_insert(reg, hs, head, ALL, W, pkey, phash, rl, k, lane, err);
             if (lane == src) rec = got;
         }
-        if (lane < kVMax) ch.rec[(size_t)rl * kVMax + lane] = rec;
+        if (mine && lane < kVMax) ch.rec[(size_t)rl * kVMax + lane] = rec;
         __syncwarp();
     }
 }
