@@ -955,16 +955,15 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                     const float sg = src == 1 ? 1.f : -1.f;
                     const int nkb = mat.Kp / 64;
                     for (int kb = 0; kb < nkb; ++kb) {
-                        // the next block of this pass, else the next pass's first
-                        // (its rows were written before this layer began)
+                        // the next block of this pass (the next pass's first is
+                        // loaded after this pass's epilogue: measured on GB300,
+                        // loads in flight there slowed the epilogue's stores by
+                        // more than they saved)
                         int njob = job, nkb2 = kb + 1;
                         bool more = true;
                         if (nkb2 == nkb) {
                             nkb2 = 0;
-                            if (++njob == njobs) {
-                                njob = 0;
-                                more = mt1 < mtiles;
-                            }
+                            more = ++njob < njobs;
                         }
                         float4 nxt[4];
                         if (more) load_items(njob, nkb2, 0, nxt);
@@ -1045,6 +1044,7 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                 }
                 umma::fence_before(); // TMEM read out before the next products overwrite it
                 bar_builders();       // rows of hidden layer i + 1 written by every builder
+                if (mt1 < mtiles) load_items(0, 0, 0, pre);
                 }
             }
 

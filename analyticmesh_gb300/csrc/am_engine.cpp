@@ -51,53 +51,82 @@ struct DeferFrees {
     }
 };
 
+// A device allocation.  Inside a batch, allocations that take a stream come
+// from the stream-ordered pool (cudaMallocAsync) and go back to it in stream
+// order (cudaFreeAsync), so that a network's growing stores neither stall
+// the other networks' streams (as cudaFree would) nor wait for the batch's
+// end to be freed.
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
+    cudaStream_t pst = nullptr; // pooled: the stream the allocation is ordered on
+    bool pooled = false;
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { reset(); }
+    static void release(void *q, bool pool, cudaStream_t qst)
+    {
+        if (!q) return;
+        if (pool) cudaFreeAsync(q, qst);
+        else release_device(q);
+    }
     void reset()
     {
-        release_device(p);
+        release(p, pooled, pst);
         p = nullptr;
         bytes = 0;
+        pooled = false;
+        pst = nullptr;
     }
-    cudaError_t alloc(size_t n)
+    static cudaError_t get(void **q, size_t n, cudaStream_t st, bool &pool)
+    {
+        pool = st && t_deferred_frees;
+        return pool ? cudaMallocAsync(q, n, st) : cudaMalloc(q, n);
+    }
+    cudaError_t alloc(size_t n, cudaStream_t st = nullptr)
     {
         reset();
         if (n == 0) n = 16;
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e == cudaSuccess) bytes = n;
-        else p = nullptr;
+        bool pool = false;
+        cudaError_t e = get(&p, n, st, pool);
+        if (e == cudaSuccess) {
+            bytes = n;
+            pooled = pool;
+            pst = pool ? st : nullptr;
+        } else {
+            p = nullptr;
+        }
         return e;
     }
     // at least n bytes, reusing the allocation when it is large enough
     // (contents not kept)
-    cudaError_t reserve(size_t n)
+    cudaError_t reserve(size_t n, cudaStream_t st = nullptr)
     {
         if (p && n <= bytes) return cudaSuccess;
-        return alloc(n);
+        return alloc(n, st);
     }
     // grow keeping the first `keep` bytes
     cudaError_t grow(size_t n, size_t keep, cudaStream_t st)
     {
         if (n <= bytes) return cudaSuccess;
         void *q = nullptr;
-        cudaError_t e = cudaMalloc(&q, n);
+        bool pool = false;
+        cudaError_t e = get(&q, n, st, pool);
         if (e != cudaSuccess) return e;
         if (p && keep) {
             e = cudaMemcpyAsync(q, p, std::min(keep, bytes), cudaMemcpyDeviceToDevice, st);
             if (e != cudaSuccess) {
-                cudaFree(q);
+                release(q, pool, st);
                 return e;
             }
             cudaStreamSynchronize(st);
         }
-        release_device(p);
+        release(p, pooled, pst);
         p = q;
         bytes = n;
+        pooled = pool;
+        pst = pool ? st : nullptr;
         return cudaSuccess;
     }
     template <class T>
@@ -245,6 +274,8 @@ struct am_engine {
 
     ~am_engine()
     {
+        if (own) cudaStreamSynchronize(own);
+        release_run_buffers(); // pooled ones are freed in the order of a stream that still exists
         if (own) cudaStreamDestroy(own);
         if (h_ctl) cudaFreeHost(h_ctl);
         for (cudaEvent_t ev : {ev0, ev1, pa, pb})
@@ -311,7 +342,7 @@ struct am_engine {
             need = std::max<unsigned long long>(need, 1ull << 16);
             if (need <= hcap) return;
         }
-        AM_CUDA(table.reserve(sizeof(unsigned long long) * need));
+        AM_CUDA(table.reserve(sizeof(unsigned long long) * need, st));
         hcap = need;
         AM_CUDA(cudaMemsetAsync(table.p, 0xff, sizeof(unsigned long long) * need, st));
         if (rehash && num_regions > 0) {
@@ -323,10 +354,10 @@ struct am_engine {
     void ensure_chunk(int count)
     {
         if (count <= chunk_cap) return;
-        AM_CUDA(cons.alloc(tc * 4 * (size_t)ALLP * count));
-        AM_CUDA(eq.alloc(tc * 4 * (size_t)count));
-        AM_CUDA(rec.alloc(sizeof(int32_t) * (size_t)kVMax * count));
-        AM_CUDA(blocksum.alloc(sizeof(int) * ((size_t)count * kVMax / 1024 + 6)));
+        AM_CUDA(cons.alloc(tc * 4 * (size_t)ALLP * count, st));
+        AM_CUDA(eq.alloc(tc * 4 * (size_t)count, st));
+        AM_CUDA(rec.alloc(sizeof(int32_t) * (size_t)kVMax * count, st));
+        AM_CUDA(blocksum.alloc(sizeof(int) * ((size_t)count * kVMax / 1024 + 6), st));
         chunk_cap = count;
     }
 
@@ -744,7 +775,9 @@ void run_begin(am_engine *e, const RunArgs &a)
     AM_CUDA(cudaMemsetAsync(e->fp64_counter(), 0, sizeof(unsigned long long), st));
     const int chunk = e->default_chunk();
     e->ensure_chunk(std::min(chunk, std::max(S, 1024)));
-    const long long first_wave = e->lean ? std::min<long long>(chunk, 4ll * S + 1024) : chunk;
+    // the first stores hold the seeds' children of a first wave (a batch
+    // member's, or a small network's, grow on demand from there)
+    const long long first_wave = std::min<long long>(chunk, e->lean ? 4ll * S + 1024 : std::max(4ll * S + 1024, 65536ll));
     e->ensure_regions(std::max<long long>(S, 1) + first_wave * kVMax);
     e->ensure_table((long long)S + first_wave * kVMax, false);
     AM_CUDA(e->blocksum.grow(sizeof(int) * ((size_t)S / 1024 + 6), 0, st));
