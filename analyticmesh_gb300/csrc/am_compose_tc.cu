@@ -680,8 +680,12 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 // copy or product and skips the epilogue work.
 __device__ __forceinline__ bool swait(uint64_t *bar, uint32_t parity, int *err, volatile int *abort)
 {
-    if (*abort) return false;
-    if (umma::mbar_wait(bar, parity, kWaitIters)) return true;
+    // the phase test and the abort flag's load overlap (the issuing
+    // thread's critical path between two blocks of products)
+    const bool ready = umma::mbar_test(bar, parity);
+    const int ab = *abort;
+    if (ab) return false;
+    if (ready || umma::mbar_wait(bar, parity, kWaitIters)) return true;
     atomicOr(err, kErrWait);
     *abort = 1;
     return false;
@@ -700,6 +704,8 @@ __device__ void produce_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws
 {
     const int nst = tc.nstage;
     int h = 0;
+    int ps = 0;        // stage of block h (h % nst) ...
+    uint32_t pph = 0u; // ... and (h / nst) & 1, kept incrementally
     int last[4] = {-1, -1, -1, -1}; // the last block copied into each stage
     for (int t = 0; t < tiles; ++t)
         for (int i = 1; i <= net.n_lin - 2; ++i) {
@@ -712,8 +718,13 @@ __device__ void produce_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws
                 const int mtiles = m.Mp / 128, kblocks = m.Kp / 64;
                 for (int kb = 0; kb < kblocks; ++kb)
                     for (int mt = mt0; mt < min(mtiles, mt0 + mper); ++mt, ++h) {
-                        const int s = h % nst;
-                        if (h >= nst && !swait(wdone + s, (uint32_t)((h - nst) / nst) & 1u, err, abort)) continue;
+                        const int s = ps;
+                        const uint32_t ph = pph; // phase of block h - nst's products
+                        if (++ps == nst) {
+                            ps = 0;
+                            pph ^= 1u;
+                        }
+                        if (h >= nst && !swait(wdone + s, ph ^ 1u, err, abort)) continue;
                         if (*abort) continue;
                         umma::mbar_expect_tx(wfull + s, (uint32_t)kWBlockBytes);
                         umma::bulk_g2s(ws + (size_t)s * kWBlockBytes,
@@ -742,6 +753,11 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
 {
     const int nst = tc.nstage;
     int h = 0, xb = 0, consumed = 0;
+    int ws_ = 0;       // stage of weight block h (h % nst) ...
+    uint32_t wph = 0u; // ... and its phase parity ((h / nst) & 1), kept incrementally
+    // weight stage q's descriptor = wd0 + q * wstep (start address field)
+    const uint64_t wd0 = umma::desc_sw128(umma::smem_addr(ws));
+    const uint64_t wstep = (uint64_t)(kWBlockBytes >> 4);
     // operand descriptors of the two stages; term and K step add constant offsets
     const uint64_t xd0 = XS[0].desc(0, 0, 0), xd1 = XS[1].desc(0, 0, 0);
     const uint64_t xu = XS[0].ustep(), xj = XS[0].jstep();
@@ -761,13 +777,17 @@ __device__ void issue_streamed(const NetDev &net, const TcNet &tc, uint8_t *ws, 
                     const bool xok = swait(xfull + xs, (uint32_t)(xb >> 1) & 1u, err, abort); // operand block built
                     const bool fresh = job == 0 && kb == 0;
                     for (int mt = mt0; mt < min(mtiles, mt0 + mper); ++mt, ++h) {
-                        const int s = h % nst;
-                        if (!xok || !swait(wfull + s, (uint32_t)(h / nst) & 1u, err, abort)) continue;
+                        const int s = ws_;
+                        const uint32_t ph = wph;
+                        if (++ws_ == nst) {
+                            ws_ = 0;
+                            wph ^= 1u;
+                        }
+                        if (!xok || !swait(wfull + s, ph, err, abort)) continue;
                         umma::fence_after();
-                        const uint32_t a0 = umma::smem_addr(ws + (size_t)s * kWBlockBytes);
                         const uint32_t d_main = tmem + (uint32_t)((mt - mt0) * ncols);
                         const uint32_t d_corr = tmem + (uint32_t)((mper + mt - mt0) * ncols);
-                        const uint64_t ad = umma::desc_sw128(a0); // term t at +16 KB, K step j at +32 B
+                        const uint64_t ad = wd0 + wstep * (uint64_t)s; // term t at +16 KB, K step j at +32 B
 #pragma unroll
                         for (int j = 0; j < 4; ++j) {
                             umma::mma_bf16(d_main, ad + 2u * j, xd + xj * j, idesc, (fresh && j == 0) ? 0u : 1u);

@@ -229,6 +229,9 @@ struct GroupShared {
     int bk[2][8];
     int nlist;      // rows kept by the pruning
     int ve[kVMax];  // the face's neighbour planes by edge (-1: none), from the leader
+    unsigned long long sk[2][8]; // seed start search: partial choices of a selection pass
+    double sv[3];   // and the start vertex found, with its plane
+    int sri;
     // row pruning: first the sample's extreme rows per warp and direction,
     // then (once every warp has read those) the list of the rows kept
     union {
@@ -951,8 +954,14 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         // ---------------------------------------------------- seed start search
         if (is_seed) {
             // pairs x <= 812 reach sorted positions up to 56: keep the 64 nearest,
-            // position q in lane q % 32, register q / 32
+            // position q in lane q % 32, register q / 32.  In a group, every
+            // selection pass splits the rows over the warps (the partial
+            // choices meet in shared memory), and the warps test G pairs at a
+            // time, the smallest feasible x winning (measured on GB300: with
+            // every warp repeating the whole search, the seeds of a 4,096-row
+            // network took a whole wave's time)
             const int ksel = ALL < kTopK ? ALL : kTopK;
+            const int k0 = kGroup ? 32 * g.gw + lane : lane, ks = kGroup ? 32 * G : 32;
             int top0 = -1, top1 = -1;
             unsigned long long pk = ~0ull;
             int pi = -1;
@@ -960,7 +969,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             for (int sel = 0; sel < ksel; ++sel) {
                 unsigned long long bk = 0ull;
                 int bi = 0x7fffffff;
-                for (int k = lane; k < ALL; k += 32) {
+                for (int k = k0; k < ALL; k += ks) {
                     const vec4_t<TC> v = rows[k];
                     const TC d = v.x * pc[0] + v.y * pc[1] + v.z * pc[2] + v.w;
                     const unsigned long long key = order_key<TC>(d);
@@ -979,6 +988,21 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
                         bi = oi;
                     }
                 }
+                if (kGroup) {
+                    const int par = sel & 1;
+                    if (lane == 0) {
+                        g.sh->sk[par][g.gw] = bk;
+                        g.sh->bk[par][g.gw] = bi;
+                    }
+                    g.sync();
+                    bk = g.sh->sk[par][0];
+                    bi = g.sh->bk[par][0];
+                    for (int w = 1; w < G; ++w)
+                        if (ahead(g.sh->sk[par][w], g.sh->bk[par][w], bk, bi)) {
+                            bk = g.sh->sk[par][w];
+                            bi = g.sh->bk[par][w];
+                        }
+                }
                 if (lane == (sel & 31)) {
                     if (sel < 32) top0 = bi;
                     else top1 = bi;
@@ -990,23 +1014,50 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             if (x_max > 812) x_max = 812;
             if (x_max < 0) x_max = 0;
             s = -1;
-            for (int x = 0; x <= x_max; ++x) {
-                int i, j;
-                get_i_j(x, ALL, i, j);
-                const int ri0 = __shfl_sync(0xffffffffu, top0, i & 31), ri1 = __shfl_sync(0xffffffffu, top1, i & 31);
-                const int rj0 = __shfl_sync(0xffffffffu, top0, j & 31), rj1 = __shfl_sync(0xffffffffu, top1, j & 31);
-                const int ri = i < 32 ? ri0 : ri1;
-                const int rj = j < 32 ? rj0 : rj1;
+            for (int xb = 0, round = 0; xb <= x_max; xb += G, ++round) {
+                const int x = xb + (kGroup ? g.gw : 0);
+                bool good = false;
                 TS v[3];
-                TC vc[3];
-                warp_solve<TC, TS>(rows, ri, rj, eqv, v, vc, lane);
-                bool bad = false;
-                for (int k = lane; k < ALL; k += 32) {
-                    if (k == ri || k == rj) continue;
-                    const vec4_t<TC> r = rows[k];
-                    if (r.x * vc[0] + r.y * vc[1] + r.z * vc[2] + r.w > eps) bad = true;
+                int ri = -1;
+                if (x <= x_max) {
+                    int i, j;
+                    get_i_j(x, ALL, i, j);
+                    const int ri0 = __shfl_sync(0xffffffffu, top0, i & 31), ri1 = __shfl_sync(0xffffffffu, top1, i & 31);
+                    const int rj0 = __shfl_sync(0xffffffffu, top0, j & 31), rj1 = __shfl_sync(0xffffffffu, top1, j & 31);
+                    ri = i < 32 ? ri0 : ri1;
+                    const int rj = j < 32 ? rj0 : rj1;
+                    TC vc[3];
+                    warp_solve<TC, TS>(rows, ri, rj, eqv, v, vc, lane);
+                    bool bad = false;
+                    for (int k = lane; k < ALL; k += 32) {
+                        if (k == ri || k == rj) continue;
+                        const vec4_t<TC> r = rows[k];
+                        if (r.x * vc[0] + r.y * vc[1] + r.z * vc[2] + r.w > eps) bad = true;
+                    }
+                    good = !__any_sync(0xffffffffu, bad);
                 }
-                if (!__any_sync(0xffffffffu, bad)) {
+                if (kGroup) { // the smallest feasible pair of the round, from its warp
+                    const int par = (round + ksel) & 1; // not the last selection pass's slots
+                    // (a warp still reading those may lag one barrier behind)
+                    if (lane == 0) g.sh->bk[par][g.gw] = good ? x : 0x7fffffff;
+                    g.sync();
+                    int xw = 0x7fffffff;
+                    for (int w = 0; w < G; ++w) xw = min(xw, g.sh->bk[par][w]);
+                    if (xw == 0x7fffffff) continue;
+                    if (good && x == xw && lane == 0) {
+                        g.sh->sri = ri;
+                        g.sh->sv[0] = (double)v[0];
+                        g.sh->sv[1] = (double)v[1];
+                        g.sh->sv[2] = (double)v[2];
+                    }
+                    g.sync();
+                    s = g.sh->sri;
+                    p[0] = (TS)g.sh->sv[0];
+                    p[1] = (TS)g.sh->sv[1];
+                    p[2] = (TS)g.sh->sv[2];
+                    break;
+                }
+                if (good) {
                     s = ri;
                     p[0] = v[0];
                     p[1] = v[1];

@@ -389,27 +389,44 @@ def bench_batched(args, ws, rank, local):
         sum(t.numel() * t.element_size() for t in hsts + hpts)
     d2h = sum(m.verts.nbytes + m.face_sizes.nbytes + m.face_indices.nbytes for m in meshes)
 
-    # plain form: FP32, one network at a time
-    plain_engines = [engine.Engine("float32", n.nodes, n.arc_table, n.num_extra) for n in nets]
-    for e, n, s_, p_ in zip(plain_engines, dnets, sts, pts):
-        e.run(n.W, n.b, s_, p_, n.tms)
-    torch.cuda.synchronize()
-    pt = []
-    for _ in range(max(1, args.steps // 2)):
-        flush.zero_()
-        torch.cuda.synchronize()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record()
-        f = 0
-        for e, n, s_, p_ in zip(plain_engines, dnets, sts, pts):
-            f += e.run(n.W, n.b, s_, p_, n.tms)["num_faces"]
-        ev1.record()
-        ev1.synchronize()
-        pt.append(f / (ev0.elapsed_time(ev1) / 1e3))
-    plain = ws * statistics.mean(pt)
-    for e in chosen + plain_engines:
+    # the chosen results go back before the plain form runs (tens of GB)
+    for e in chosen:
         e.close()
+    del chosen
+    torch.cuda.empty_cache()
+
+    # plain form: FP32, one network at a time (each engine closed before the
+    # next; a run that passes twice the chosen form's regions for its network
+    # is stopped there and counted as not converging)
+    from analyticmesh_gb300 import _lib
+
+    plain_ms, plain_faces, diverged = 0.0, 0, []
+    for i, (n, s_, p_) in enumerate(zip(dnets, sts, pts)):
+        e = engine.Engine("float32", n.nodes, n.arc_table, n.num_extra)
+        e.set_option(_lib.AM_OPT_MAX_REGIONS, 2 * int(regions[i]))
+        try:
+            e.run(n.W, n.b, s_, p_, n.tms)
+            ms = []
+            for _ in range(max(1, args.steps // 2)):
+                flush.zero_()
+                ev0 = torch.cuda.Event(enable_timing=True)
+                ev1 = torch.cuda.Event(enable_timing=True)
+                ev0.record()
+                f = e.run(n.W, n.b, s_, p_, n.tms)["num_faces"]
+                ev1.record()
+                ev1.synchronize()
+                ms.append(ev0.elapsed_time(ev1))
+            plain_ms += statistics.mean(ms)
+            plain_faces += f
+        except _lib.AmError as exc:
+            if exc.status != _lib.AM_ERR_CAPACITY:
+                raise
+            diverged.append(i)
+        e.close()
+        torch.cuda.empty_cache()
+    plain = ws * plain_faces / (plain_ms / 1e3) if plain_ms > 0 and not diverged else None
+    plain_note = ("plain FP32 does not converge on networks %s (stopped at twice the chosen form's regions)"
+                  % diverged) if diverged else "float32, networks one after the other"
     if rank != 0:
         return
     line = {
@@ -425,8 +442,8 @@ def bench_batched(args, ws, rank, local):
                                 "tile_and_face_warps": ["%d/%d" % t for t in tuned]},
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "e2e": {"value": e2e, "unit": "faces/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-        "plain_fp32_value": plain, "plain_form": "float32, networks one after the other",
-        "chosen_vs_plain": value / plain, "clocks": clocks,
+        "plain_fp32_value": plain, "plain_note": plain_note,
+        "chosen_vs_plain": (value / plain) if plain else None, "clocks": clocks,
     }
     print(json.dumps(line), flush=True)
 
