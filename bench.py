@@ -401,8 +401,8 @@ def bench_batched(args, ws, rank, local):
     from analyticmesh_gb300 import _lib
 
     plain_ms, plain_faces, diverged = 0.0, 0, []
-    for i, (n, s_, p_) in enumerate(zip(dnets, sts, pts)):
-        e = engine.Engine("float32", n.nodes, n.arc_table, n.num_extra)
+    for i, (na, n, s_, p_) in enumerate(zip(nets, dnets, sts, pts)):
+        e = engine.Engine("float32", na.nodes, na.arc_table, na.num_extra)
         e.set_option(_lib.AM_OPT_MAX_REGIONS, 2 * int(regions[i]))
         try:
             e.run(n.W, n.b, s_, p_, n.tms)
