@@ -268,6 +268,7 @@ struct am_engine {
     double iso = 0.0;
     // mesh
     DevBuf w_table, w_rep, w_flag, w_vidx, w_bsum, w_fflag, w_fsize, w_fid, w_foff, w_verts, w_fs, w_fi, w_counts;
+    DevBuf w_voff, w_vsid; // compacted polygon vertex slots
     std::vector<double> mesh_verts;
     std::vector<int32_t> mesh_fs, mesh_fi;
     bool mesh_host = false; // the welded mesh has been copied into the vectors above
@@ -1462,40 +1463,54 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
     return guarded(e, [&] {
         cudaStream_t st = e->st;
         const long long R = e->num_regions;
-        const long long ns = std::max<long long>(R * kVMax, 1);
+        const long long nr = std::max<long long>(R, 1);
+        // the vertex slots in use, compacted (a face has ~4 of its 32)
+        AM_CUDA(e->w_voff.reserve(sizeof(int) * (nr + 1)));
+        AM_CUDA(e->w_fflag.reserve(sizeof(int) * (nr + 1)));
+        AM_CUDA(e->w_bsum.reserve(sizeof(int) * (nr / 1024 + 2)));
+        AM_CUDA(e->w_counts.reserve(sizeof(long long) * 3));
+        WeldBuffers wb{};
+        wb.voff = e->w_voff.as<int>();
+        wb.fflag = e->w_fflag.as<int>();
+        wb.bsum = e->w_bsum.as<int>();
+        wb.counts = e->w_counts.as<long long>();
+        launch_weld_slots(e->regions(), R, wb, st);
+        AM_CUDA(cudaGetLastError());
+        long long V = 0;
+        AM_CUDA(cudaMemcpyAsync(&V, wb.counts, sizeof(long long), cudaMemcpyDeviceToHost, st));
+        AM_CUDA(cudaStreamSynchronize(st));
+        AM_CHECK(V < 0x7fffffffll, "too many polygon vertices for one mesh (2^31)");
+        const long long ns = std::max<long long>(V, 1);
         unsigned long long tcap = 1;
         while (tcap < (unsigned long long)ns * 2ull) tcap <<= 1;
+        AM_CUDA(e->w_vsid.reserve(sizeof(long long) * ns));
         AM_CUDA(e->w_table.reserve(sizeof(unsigned long long) * tcap));
-        AM_CUDA(e->w_rep.reserve(sizeof(long long) * ns));
+        AM_CUDA(e->w_rep.reserve(sizeof(int) * ns));
         AM_CUDA(e->w_flag.reserve(sizeof(int) * ns));
         AM_CUDA(e->w_vidx.reserve(sizeof(int) * ns));
-        AM_CUDA(e->w_bsum.reserve(sizeof(int) * (ns / 1024 + 2)));
-        AM_CUDA(e->w_fflag.reserve(sizeof(int) * (R + 1)));
-        AM_CUDA(e->w_fsize.reserve(sizeof(int) * (R + 1)));
-        AM_CUDA(e->w_fid.reserve(sizeof(int) * (R + 1)));
-        AM_CUDA(e->w_foff.reserve(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_bsum.reserve(sizeof(int) * (std::max(ns, nr) / 1024 + 2)));
+        AM_CUDA(e->w_fsize.reserve(sizeof(int) * (nr + 1)));
+        AM_CUDA(e->w_fid.reserve(sizeof(int) * (nr + 1)));
+        AM_CUDA(e->w_foff.reserve(sizeof(int) * (nr + 1)));
         AM_CUDA(e->w_verts.reserve(e->ts * 3 * ns));
-        AM_CUDA(e->w_fs.reserve(sizeof(int) * (R + 1)));
+        AM_CUDA(e->w_fs.reserve(sizeof(int) * (nr + 1)));
         AM_CUDA(e->w_fi.reserve(sizeof(int) * ns));
-        AM_CUDA(e->w_counts.reserve(sizeof(long long) * 3));
-        WeldBuffers wb;
+        wb.vsid = e->w_vsid.as<long long>();
         wb.table = e->w_table.as<unsigned long long>();
         wb.mask = tcap - 1;
-        wb.rep = e->w_rep.as<long long>();
+        wb.rep = e->w_rep.as<int>();
         wb.flag = e->w_flag.as<int>();
         wb.vidx = e->w_vidx.as<int>();
         wb.bsum = e->w_bsum.as<int>();
-        wb.fflag = e->w_fflag.as<int>();
         wb.fsize = e->w_fsize.as<int>();
         wb.fid = e->w_fid.as<int>();
         wb.foff = e->w_foff.as<int>();
         wb.out_verts = e->w_verts.p;
         wb.face_sizes = e->w_fs.as<int>();
         wb.face_idx = e->w_fi.as<int>();
-        wb.counts = e->w_counts.as<long long>();
         const double c0[3] = {0, 0, 0};
         AM_CUDA(cudaMemsetAsync(e->d_err.p, 0, sizeof(int), st));
-        launch_weld(e->prec, e->weld_mode, e->N, e->W, e->regions(), R, wb, scale, center3 ? center3 : c0, e->flip,
+        launch_weld(e->prec, e->weld_mode, e->N, e->W, e->regions(), R, V, wb, scale, center3 ? center3 : c0, e->flip,
                     e->d_err.as<int>(), st);
         AM_CUDA(cudaGetLastError());
         long long cnt[3] = {0, 0, 0};
@@ -1510,10 +1525,10 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
         // large weld buffers go back (many engines of a batch weld one after
         // the other): their mesh moves to the host first
         DevBuf *weld[] = {&e->w_table, &e->w_rep, &e->w_flag, &e->w_vidx, &e->w_bsum, &e->w_fflag, &e->w_fsize,
-                          &e->w_fid, &e->w_foff, &e->w_verts, &e->w_fs, &e->w_fi};
+                          &e->w_fid, &e->w_foff, &e->w_verts, &e->w_fs, &e->w_fi, &e->w_voff, &e->w_vsid};
         size_t held = 0;
         for (DevBuf *b : weld) held += b->bytes;
-        if (held > ((size_t)1 << 30)) {
+        if (held > ((size_t)8 << 30)) {
             fetch_mesh(e);
             for (DevBuf *b : weld) b->reset();
         }

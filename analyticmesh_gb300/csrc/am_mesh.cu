@@ -105,22 +105,43 @@ __device__ bool same_vertex(const RegionsDev &reg, int mode, int N, int W, const
     return true;
 }
 
-template <typename TS>
-__global__ void weld_insert_kernel(RegionsDev reg, long long R, int mode, int N, int W, unsigned long long *table,
-                                   unsigned long long mask, double mul, int *err)
+__global__ void vertex_counts_kernel(const int32_t *nv, long long R, int *cnt)
 {
-    const long long sid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (sid >= R * kVMax) return;
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r < R) cnt[r] = min(max(nv[r], 0), kVMax);
+}
+
+// the polygon vertex slots (sid = region x kVMax + corner) in region order,
+// compacted: slot j of region r is voff[r] + corner
+__global__ void expand_slots_kernel(const int32_t *nv, long long R, const int *voff, long long *vsid)
+{
+    const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (r >= R) return;
+    const int n = min(max(nv[r], 0), kVMax);
+    long long *o = vsid + voff[r];
+    for (int i = 0; i < n; ++i) o[i] = r * kVMax + i;
+}
+
+// the table holds compacted slot indices; the smallest index of a vertex's
+// copies (the first in region order) represents it
+template <typename TS>
+__global__ void weld_insert_kernel(RegionsDev reg, const long long *vsid, long long V, int mode, int N, int W,
+                                   unsigned long long *table, unsigned long long mask, double mul, int *err)
+{
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= V) return;
+    const long long sid = vsid[j];
     VKey k;
     if (!make_key<TS>(reg, mode, N, W, mul, sid, k)) return;
     unsigned long long slot = k.h & mask;
     for (int probe = 0; probe < kMaxProbes; ++probe) {
-        const unsigned long long cur = atomicCAS(table + slot, kEmpty, (unsigned long long)sid);
+        const unsigned long long cur = atomicCAS(table + slot, kEmpty, (unsigned long long)j);
         if (cur == kEmpty) return;
+        const long long osid = vsid[cur];
         VKey o;
-        make_key<TS>(reg, mode, N, W, mul, (long long)cur, o);
-        if (o.h == k.h && same_vertex(reg, mode, N, W, k, sid, o, (long long)cur)) {
-            atomicMin(table + slot, (unsigned long long)sid);
+        make_key<TS>(reg, mode, N, W, mul, osid, o);
+        if (o.h == k.h && same_vertex(reg, mode, N, W, k, sid, o, osid)) {
+            atomicMin(table + slot, (unsigned long long)j);
             return;
         }
         slot = (slot + (unsigned long long)probe + 1ull) & mask;
@@ -129,43 +150,41 @@ __global__ void weld_insert_kernel(RegionsDev reg, long long R, int mode, int N,
 }
 
 template <typename TS>
-__global__ void weld_rep_kernel(RegionsDev reg, long long R, int mode, int N, int W, const unsigned long long *table,
-                                unsigned long long mask, double mul, long long *rep, int *flag)
+__global__ void weld_rep_kernel(RegionsDev reg, const long long *vsid, long long V, int mode, int N, int W,
+                                const unsigned long long *table, unsigned long long mask, double mul, int *rep, int *flag)
 {
-    const long long sid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (sid >= R * kVMax) return;
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= V) return;
+    const long long sid = vsid[j];
     VKey k;
-    if (!make_key<TS>(reg, mode, N, W, mul, sid, k)) {
-        flag[sid] = 0;
-        rep[sid] = -1;
-        return;
-    }
+    make_key<TS>(reg, mode, N, W, mul, sid, k);
     unsigned long long slot = k.h & mask;
     long long found = -1;
     for (int probe = 0; probe < kMaxProbes; ++probe) {
         const unsigned long long cur = table[slot];
         if (cur == kEmpty) break;
+        const long long osid = vsid[cur];
         VKey o;
-        make_key<TS>(reg, mode, N, W, mul, (long long)cur, o);
-        if (o.h == k.h && same_vertex(reg, mode, N, W, k, sid, o, (long long)cur)) {
+        make_key<TS>(reg, mode, N, W, mul, osid, o);
+        if (o.h == k.h && same_vertex(reg, mode, N, W, k, sid, o, osid)) {
             found = (long long)cur;
             break;
         }
         slot = (slot + (unsigned long long)probe + 1ull) & mask;
     }
-    rep[sid] = found;
-    flag[sid] = (found == sid) ? 1 : 0;
+    rep[j] = (int)found;
+    flag[j] = (found == j) ? 1 : 0;
 }
 
 template <typename TS>
-__global__ void weld_verts_kernel(RegionsDev reg, long long R, const long long *rep, const int *vidx, TS scale, TS cx,
-                                  TS cy, TS cz, TS *out)
+__global__ void weld_verts_kernel(RegionsDev reg, const long long *vsid, long long V, const int *rep, const int *vidx,
+                                  TS scale, TS cx, TS cy, TS cz, TS *out)
 {
-    const long long sid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (sid >= R * kVMax) return;
-    if (rep[sid] != sid) return;
-    const TS *v = (const TS *)reg.verts + (size_t)sid * 3;
-    TS *o = out + (size_t)vidx[sid] * 3;
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= V) return;
+    if (rep[j] != j) return;
+    const TS *v = (const TS *)reg.verts + (size_t)vsid[j] * 3;
+    TS *o = out + (size_t)vidx[j] * 3;
     o[0] = v[0] * scale + cx;
     o[1] = v[1] * scale + cy;
     o[2] = v[2] * scale + cz;
@@ -180,8 +199,8 @@ __global__ void face_counts_kernel(RegionsDev reg, long long R, int *fflag, int 
     fsize[r] = n >= 3 ? n : 0;
 }
 
-__global__ void faces_kernel(RegionsDev reg, long long R, const long long *rep, const int *vidx, const int *fid,
-                             const int *foff, int flip, int *face_sizes, int *face_idx)
+__global__ void faces_kernel(RegionsDev reg, long long R, const int *voff, const int *rep, const int *vidx,
+                             const int *fid, const int *foff, int flip, int *face_sizes, int *face_idx)
 {
     const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (r >= R) return;
@@ -189,10 +208,10 @@ __global__ void faces_kernel(RegionsDev reg, long long R, const long long *rep, 
     if (n < 3) return;
     face_sizes[fid[r]] = n;
     int *o = face_idx + foff[r];
+    const int *rp = rep + voff[r];
     for (int j = 0; j < n; ++j) {
         const int i = flip ? (n - 1 - j) : j;
-        const long long rp = rep[r * kVMax + i];
-        o[j] = rp >= 0 ? vidx[rp] : -1;
+        o[j] = rp[i] >= 0 ? vidx[rp[i]] : -1;
     }
 }
 
@@ -282,37 +301,51 @@ void scan_exclusive(const int *in, long long n, int *out, int *bsum, long long *
     scan_apply_kernel<<<(unsigned)nb, kScanBlock, 0, st>>>(in, n, bsum, out);
 }
 
-void launch_weld(int prec, int mode, int N, int W, const RegionsDev &reg, long long R, const WeldBuffers &wb,
-                 double scale, const double *center, int flip, int *d_err, cudaStream_t st)
+void launch_weld_slots(const RegionsDev &reg, long long R, const WeldBuffers &wb, cudaStream_t st)
 {
-    const long long nslots = R * kVMax;
-    const unsigned g1 = (unsigned)((nslots + 255) / 256);
+    if (R <= 0) {
+        cudaMemsetAsync(wb.counts, 0, sizeof(long long), st);
+        return;
+    }
+    // vertex counts (into fflag, which the face counts overwrite later)
+    vertex_counts_kernel<<<(unsigned)((R + 255) / 256), 256, 0, st>>>(reg.nv, R, wb.fflag);
+    scan_exclusive(wb.fflag, R, wb.voff, wb.bsum, wb.counts + 0, st);
+}
+
+void launch_weld(int prec, int mode, int N, int W, const RegionsDev &reg, long long R, long long V,
+                 const WeldBuffers &wb, double scale, const double *center, int flip, int *d_err, cudaStream_t st)
+{
+    const unsigned g1 = (unsigned)((V + 255) / 256);
     const unsigned g2 = (unsigned)((R + 255) / 256);
     cudaMemsetAsync(wb.table, 0xff, sizeof(unsigned long long) * (size_t)(wb.mask + 1), st);
     const bool f64 = (prec != kFloat32);
     const double mul = (prec == kFloat64) ? 1e9 : 1e6;
-    if (R <= 0) {
+    if (R <= 0 || V <= 0) {
         cudaMemsetAsync(wb.counts, 0, sizeof(long long) * 3, st);
         return;
     }
+    expand_slots_kernel<<<g2, 256, 0, st>>>(reg.nv, R, wb.voff, wb.vsid);
     if (f64) {
-        weld_insert_kernel<double><<<g1, 256, 0, st>>>(reg, R, mode, N, W, wb.table, wb.mask, mul, d_err);
-        weld_rep_kernel<double><<<g1, 256, 0, st>>>(reg, R, mode, N, W, wb.table, wb.mask, mul, wb.rep, wb.flag);
+        weld_insert_kernel<double><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, d_err);
+        weld_rep_kernel<double><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, wb.rep,
+                                                    wb.flag);
     } else {
-        weld_insert_kernel<float><<<g1, 256, 0, st>>>(reg, R, mode, N, W, wb.table, wb.mask, mul, d_err);
-        weld_rep_kernel<float><<<g1, 256, 0, st>>>(reg, R, mode, N, W, wb.table, wb.mask, mul, wb.rep, wb.flag);
+        weld_insert_kernel<float><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, d_err);
+        weld_rep_kernel<float><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, wb.rep,
+                                                   wb.flag);
     }
-    scan_exclusive(wb.flag, nslots, wb.vidx, wb.bsum, wb.counts + 0, st);
+    scan_exclusive(wb.flag, V, wb.vidx, wb.bsum, wb.counts + 0, st);
     if (f64)
-        weld_verts_kernel<double><<<g1, 256, 0, st>>>(reg, R, wb.rep, wb.vidx, scale, center[0], center[1], center[2],
-                                                      (double *)wb.out_verts);
+        weld_verts_kernel<double><<<g1, 256, 0, st>>>(reg, wb.vsid, V, wb.rep, wb.vidx, scale, center[0], center[1],
+                                                      center[2], (double *)wb.out_verts);
     else
-        weld_verts_kernel<float><<<g1, 256, 0, st>>>(reg, R, wb.rep, wb.vidx, (float)scale, (float)center[0],
+        weld_verts_kernel<float><<<g1, 256, 0, st>>>(reg, wb.vsid, V, wb.rep, wb.vidx, (float)scale, (float)center[0],
                                                      (float)center[1], (float)center[2], (float *)wb.out_verts);
     face_counts_kernel<<<g2, 256, 0, st>>>(reg, R, wb.fflag, wb.fsize);
     scan_exclusive(wb.fflag, R, wb.fid, wb.bsum, wb.counts + 1, st);
     scan_exclusive(wb.fsize, R, wb.foff, wb.bsum, wb.counts + 2, st);
-    faces_kernel<<<g2, 256, 0, st>>>(reg, R, wb.rep, wb.vidx, wb.fid, wb.foff, flip, wb.face_sizes, wb.face_idx);
+    faces_kernel<<<g2, 256, 0, st>>>(reg, R, wb.voff, wb.rep, wb.vidx, wb.fid, wb.foff, flip, wb.face_sizes,
+                                     wb.face_idx);
 }
 
 } // namespace am

@@ -228,18 +228,22 @@ struct GroupShared {
     double btd[2][8]; // the same for a scan in FP64 over FP32 rows
     int bk[2][8];
     int nlist;      // rows kept by the pruning
-    int ve[kVMax];  // the face's neighbour planes by edge (-1: none), from the leader
-    unsigned long long sk[2][8]; // seed start search: partial choices of a selection pass
-    double sv[3];   // and the start vertex found, with its plane
-    int sri;
-    // row pruning: first the sample's extreme rows per warp and direction,
-    // then (once every warp has read those) the list of the rows kept
+    // phases of a face, one at a time (a barrier between any two): the seed
+    // start search; row pruning, first the sample's extreme rows per warp
+    // and direction, then (once every warp has read those) the list of the
+    // rows kept, read by the walk; the neighbour planes by edge after it
     union {
+        struct {
+            unsigned long long sk[2][8]; // partial choices of a selection pass
+            double sv[3];                // the start vertex found ...
+            int sri;                     // ... and its plane
+        } seed;
         struct {
             TC v[8][8];
             int16_t i[8][8];
         } ext;
         uint16_t list[kListCap];
+        int ve[kVMax]; // -1: no neighbour across the edge (from the leader)
     };
 };
 
@@ -991,15 +995,15 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
                 if (kGroup) {
                     const int par = sel & 1;
                     if (lane == 0) {
-                        g.sh->sk[par][g.gw] = bk;
+                        g.sh->seed.sk[par][g.gw] = bk;
                         g.sh->bk[par][g.gw] = bi;
                     }
                     g.sync();
-                    bk = g.sh->sk[par][0];
+                    bk = g.sh->seed.sk[par][0];
                     bi = g.sh->bk[par][0];
                     for (int w = 1; w < G; ++w)
-                        if (ahead(g.sh->sk[par][w], g.sh->bk[par][w], bk, bi)) {
-                            bk = g.sh->sk[par][w];
+                        if (ahead(g.sh->seed.sk[par][w], g.sh->bk[par][w], bk, bi)) {
+                            bk = g.sh->seed.sk[par][w];
                             bi = g.sh->bk[par][w];
                         }
                 }
@@ -1045,16 +1049,17 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
                     for (int w = 0; w < G; ++w) xw = min(xw, g.sh->bk[par][w]);
                     if (xw == 0x7fffffff) continue;
                     if (good && x == xw && lane == 0) {
-                        g.sh->sri = ri;
-                        g.sh->sv[0] = (double)v[0];
-                        g.sh->sv[1] = (double)v[1];
-                        g.sh->sv[2] = (double)v[2];
+                        g.sh->seed.sri = ri;
+                        g.sh->seed.sv[0] = (double)v[0];
+                        g.sh->seed.sv[1] = (double)v[1];
+                        g.sh->seed.sv[2] = (double)v[2];
                     }
                     g.sync();
-                    s = g.sh->sri;
-                    p[0] = (TS)g.sh->sv[0];
-                    p[1] = (TS)g.sh->sv[1];
-                    p[2] = (TS)g.sh->sv[2];
+                    s = g.sh->seed.sri;
+                    p[0] = (TS)g.sh->seed.sv[0];
+                    p[1] = (TS)g.sh->seed.sv[1];
+                    p[2] = (TS)g.sh->seed.sv[2];
+                    g.sync(); // read by every warp before the pruning may overwrite it
                     break;
                 }
                 if (good) {
@@ -1132,6 +1137,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         int kv = -1;
         if (leader && lane < n && ve >= 0 && ve < N && (closed || lane < n - 1) && !(!is_seed && ve == s)) kv = ve;
         if (kGroup) {
+            if (list) g.sync(); // every warp's walk has done with the pruning list
             if (g.gw == 0) g.sh->ve[lane] = kv;
             g.sync();
             kv = g.sh->ve[lane];
