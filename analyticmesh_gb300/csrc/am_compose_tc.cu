@@ -925,68 +925,137 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
             }
             bar_builders(); // layer-1 rows written by every builder
 
+            // X[4r + c][k] = s_k(r) ? -C[r][k][c] : 0 (layer 1: +W0 rows from
+            // shared memory), one 64-deep K block at a time; every pass of a
+            // layer streams the same blocks.  Thread tid owns the items q = tid
+            // + u kSBuild (region q % R, row q / R of the block): regions
+            // fastest across the lanes.  The first four items of the next
+            // block are loaded one step ahead, so that their latency hides
+            // behind the stage wait; raw values are kept and signed when
+            // stored.
+            auto load_items = [&](int li, int job, int kb, int c, float4 *v) {
+                int src;
+                job_mat(net, tc, li, job, src);
+                const int K = net.nodes[src], rows0 = net.hoff[src];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int q = tid + (4 * c + u) * kSBuild;
+                    const int r = q % R, k = kb * 64 + q / R;
+                    float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+                    if (q < R * 64 && r < nreg && k < K && key_bit(keys + (size_t)r * KW, rows0 + k))
+                        x = src == 1 ? w0s[k] : ld4<float>(cons + (size_t)r * rstride + (size_t)(rows0 + k) * 4);
+                    v[u] = x;
+                }
+            };
+            auto put_items = [&](const XOp &X, int c, const float4 *v, float sg) {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int q = tid + (4 * c + u) * kSBuild;
+                    if (q < R * 64) {
+                        const float x[4] = {sg * v[u].x, sg * v[u].y, sg * v[u].z, sg * v[u].w};
+                        X.put<2>(4 * (q % R), q / R, x);
+                    }
+                }
+            };
+            const int nchunks = (R * 64 + 4 * kSBuild - 1) / (4 * kSBuild);
+            // The epilogue of a pass reads its accumulators into registers
+            // (warp w: TMEM lanes 32 (w % 4).., column blocks cgrp, cgrp +
+            // ngrp, ... of each M tile; at most four blocks of 16 columns),
+            // which frees TMEM for the next pass at once, and its rows are
+            // stored during the next pass's first steps, one column block a
+            // step, while the tensor core works (measured on GB300: a pass's
+            // 128 KB of rows take ~4 K cycles of the SM's store bandwidth
+            // alone, and the stores before the next products left the
+            // tensor core idle for a third of the time).  A barrier follows
+            // the last deferred store, so that later loads see the rows.
+            const int ncb = ncols / 16;
+            const int ncbw = cgrp < ncb ? (ncb - cgrp + ngrp - 1) / ngrp : 0; // this warp's column blocks
+            const int ncbu = (ncb + ngrp - 1) / ngrp;                          // the most any warp has
+            const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
+            // o[0..kKeep-1][16]: the (at most kKeep) deferred column blocks in
+            // store order -- the first blocks of a pass are stored at once,
+            // before the TMEM is given up; a stored block leaves o[0] and the
+            // others move up (constant indices only, so that the blocks stay
+            // in registers; more than one block spilled at 96 registers)
+            constexpr int kKeep = 1;
+            float o[kKeep][16];
+            int nd = 0, def_i = 1, def_mt0 = 0; // deferred column blocks (uniform count), their pass
+            int def_first = 0, def_nit = 0;     // this warp's first deferred block, its blocks in that pass
+            bool def_ok = false;
+            auto shift_o = [&]() {
+#pragma unroll
+                for (int b = 0; b + 1 < kKeep; ++b)
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) o[b][k] = o[b + 1][k];
+            };
+            auto store_block = [&](int it) { // block it of the pass def_i / def_mt0, from o[0]
+                if (!def_ok || it >= def_nit) return; // (this warp's share)
+                const int li = def_i;
+                const int mt = def_mt0 + it / ncbw, cb = cgrp + (it % ncbw) * ngrp;
+                const int m = mt * 128 + q4 * 32 + lane;
+                if (m >= net.nodes[li + 1]) return;
+                const int row = net.hoff[li + 1] + m;
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq) {
+                    const int r = cb * 4 + qq;
+                    if (r >= nreg) continue;
+                    const uint32_t *key = keys + (size_t)r * KW;
+                    float *cr = cons + (size_t)r * rstride;
+                    float v4[4] = {o[0][4 * qq], o[0][4 * qq + 1], o[0][4 * qq + 2], o[0][4 * qq + 3]};
+                    for (int s = 0; s < net.nskip[li]; ++s) {
+                        const SkipDev &sk = net.skip[li][s];
+                        if (sk.kind == 0) {
+                            if (sk.from == 0) {
+                                if (m < 3) v4[m] += 1.f;
+                            } else {
+                                const int srow = net.hoff[sk.from] + m;
+                                if (key_bit(key, srow)) {
+                                    const float4 c = ld4<float>(cr + (size_t)srow * 4);
+                                    v4[0] -= c.x;
+                                    v4[1] -= c.y;
+                                    v4[2] -= c.z;
+                                    v4[3] -= c.w;
+                                }
+                            }
+                        } else if (sk.from == 0) {
+                            const float *tt = (const float *)sk.tmt;
+                            v4[0] += tt[m];
+                            v4[1] += tt[(size_t)sk.Mp + m];
+                            v4[2] += tt[2 * (size_t)sk.Mp + m];
+                        }
+                    }
+                    const float sg = key_bit(key, row) ? -1.f : 1.f;
+                    st4<float>(cr + (size_t)row * 4, make_float4(sg * v4[0], sg * v4[1], sg * v4[2], sg * v4[3]));
+                }
+            };
+            float4 pre[4];
             for (int i = 1; i <= net.n_lin - 2; ++i) {
                 const int M = net.nodes[i + 1];
                 const int mtiles = (M + 127) / 128;
                 const int mper = (mtiles + tc.mgroups - 1) / tc.mgroups;
                 const int njobs = jobs_of(net, i);
-                // X[4r + c][k] = s_k(r) ? -C[r][k][c] : 0 (layer 1: +W0 rows
-                // from shared memory), one 64-deep K block at a time; every
-                // pass of the layer streams the same blocks.  Thread tid owns
-                // the items q = tid + u kSBuild (region q % R, row q / R of the
-                // block): regions fastest across the lanes.  The first four
-                // items of the next block are loaded before this block's
-                // stage wait and stores, so that their latency hides behind
-                // them (measured on GB300: with the loads of a block issued
-                // after its wait, building a block took longer than its
-                // products); raw values are kept and signed when stored.
-                auto load_items = [&](int job, int kb, int c, float4 *v) {
-                    int src;
-                    job_mat(net, tc, i, job, src);
-                    const int K = net.nodes[src], rows0 = net.hoff[src];
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int q = tid + (4 * c + u) * kSBuild;
-                        const int r = q % R, k = kb * 64 + q / R;
-                        float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (q < R * 64 && r < nreg && k < K && key_bit(keys + (size_t)r * KW, rows0 + k))
-                            x = src == 1 ? w0s[k] : ld4<float>(cons + (size_t)r * rstride + (size_t)(rows0 + k) * 4);
-                        v[u] = x;
-                    }
-                };
-                auto put_items = [&](const XOp &X, int c, const float4 *v, float sg) {
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int q = tid + (4 * c + u) * kSBuild;
-                        if (q < R * 64) {
-                            const float x[4] = {sg * v[u].x, sg * v[u].y, sg * v[u].z, sg * v[u].w};
-                            X.put<2>(4 * (q % R), q / R, x);
-                        }
-                    }
-                };
-                const int nchunks = (R * 64 + 4 * kSBuild - 1) / (4 * kSBuild);
-                float4 pre[4];
-                load_items(0, 0, 0, pre);
+                load_items(i, 0, 0, 0, pre);
                 for (int mt0 = 0; mt0 < mtiles; mt0 += mper) { // the products of this group of M tiles
                 const int mt1 = min(mtiles, mt0 + mper);
+                int t = 0; // step of the pass
                 for (int job = 0; job < njobs; ++job) {
                     int src;
                     const TcMat &mat = job_mat(net, tc, i, job, src);
                     const float sg = src == 1 ? 1.f : -1.f;
                     const int nkb = mat.Kp / 64;
-                    for (int kb = 0; kb < nkb; ++kb) {
-                        // the next block of this pass (the next pass's first is
-                        // loaded after this pass's epilogue: measured on GB300,
-                        // loads in flight there slowed the epilogue's stores by
-                        // more than they saved)
+                    for (int kb = 0; kb < nkb; ++kb, ++t) {
+                        // the next block: of this pass, else the next pass's
+                        // first (the next layer's first is loaded when the
+                        // layer begins: registers)
                         int njob = job, nkb2 = kb + 1;
                         bool more = true;
                         if (nkb2 == nkb) {
                             nkb2 = 0;
-                            more = ++njob < njobs;
+                            if (++njob == njobs) {
+                                njob = 0;
+                                more = mt1 < mtiles;
+                            }
                         }
-                        float4 nxt[4];
-                        if (more) load_items(njob, nkb2, 0, nxt);
                         const int xs = xb & 1, fill = xb >> 1;
                         // stage free (an aborting CTA builds nothing but still arrives)
                         const bool ok = fill < 1 ? !*abort : swait(xdone + xs, (uint32_t)((fill - 1) & 1), err, abort);
@@ -995,76 +1064,95 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                             put_items(X, 0, pre, sg);
                             for (int c = 1; c < nchunks; ++c) {
                                 float4 t4[4];
-                                load_items(job, kb, c, t4);
+                                load_items(i, job, kb, c, t4);
                                 put_items(X, c, t4, sg);
                             }
                         }
                         umma::fence_proxy_async(); // generic-proxy stores -> the tensor cores
                         mbar_arrive(xfull + xs);
                         ++xb;
-                        if (more)
-#pragma unroll
-                            for (int u = 0; u < 4; ++u) pre[u] = nxt[u];
+                        if (t < nd) {
+                            store_block(def_first + t);
+                            shift_o();
+                            if (t == nd - 1) bar_builders();
+                        }
+                        if (more) load_items(i, njob, nkb2, 0, pre);
                     }
                 }
+                if (t < nd) { // a pass shorter than the deferred blocks
+                    for (; t < nd; ++t) {
+                        store_block(def_first + t);
+                        shift_o();
+                    }
+                    bar_builders();
+                }
+                nd = 0;
                 const float *bias = (const float *)net.bias[i];
-                float bnext = mt0 * 128 + q4 * 32 + lane < M ? bias[mt0 * 128 + q4 * 32 + lane] : 0.f; // loaded while the products run
+                const int mA = mt0 * 128 + q4 * 32 + lane, mB = mA + 128;
+                const float bA = mA < M ? bias[mA] : 0.f;                   // loaded while the products run
+                const float bB = mt0 + 1 < mt1 && mB < M ? bias[mB] : 0.f;
                 // the layer's products are in TMEM; the TMEM loads below are
                 // warp-collective, so the warp decides as one
                 bool acc_ok = swait(accdone, (uint32_t)(accph & 1), err, abort);
                 acc_ok = __all_sync(0xffffffffu, acc_ok) && !__any_sync(0xffffffffu, *abort != 0);
                 ++accph;
                 umma::fence_after();
-                // epilogue: accumulators -> constraint rows of hidden layer i + 1
-                for (int mt = mt0; acc_ok && mt < mt1; ++mt) {
-                    const int m = mt * 128 + q4 * 32 + lane;
-                    const uint32_t lane_base = tmem + ((uint32_t)(q4 * 32) << 16);
-                    const float bm = bnext;
-                    if (mt + 1 < mt1) bnext = m + 128 < M ? bias[m + 128] : 0.f;
-                    const int row = net.hoff[i + 1] + m;
-                    for (int cb = cgrp; cb < ncols / 16; cb += ngrp) {
-                        float v[16], vc[16];
-                        umma::tmem_ld16x2(lane_base + (uint32_t)((mt - mt0) * ncols + cb * 16),
-                                          lane_base + (uint32_t)((mper + mt - mt0) * ncols + cb * 16), v, vc);
-                        if (m >= M) continue;
+                // accumulators -> registers: main + correction (+ bias); the
+                // first blocks are stored at once, the last two (at most)
+                // kept in o for the next pass's first steps
+                const int nit = (mt1 - mt0) * ncbw;
+                const int nkeep = min(kKeep, nit);
+                def_i = i;
+                def_mt0 = mt0;
+                def_ok = acc_ok;
+                def_nit = nit;
+                def_first = nit - nkeep;
 #pragma unroll
-                        for (int qq = 0; qq < 4; ++qq) {
-                            const int r = cb * 4 + qq;
-                            if (r >= nreg) continue;
-                            const uint32_t *key = keys + (size_t)r * KW;
-                            float *cr = cons + (size_t)r * rstride;
-                            float o[4] = {v[4 * qq] + vc[4 * qq], v[4 * qq + 1] + vc[4 * qq + 1],
-                                          v[4 * qq + 2] + vc[4 * qq + 2], v[4 * qq + 3] + vc[4 * qq + 3] + bm};
-                            for (int s = 0; s < net.nskip[i]; ++s) {
-                                const SkipDev &sk = net.skip[i][s];
-                                if (sk.kind == 0) {
-                                    if (sk.from == 0) {
-                                        if (m < 3) o[m] += 1.f;
-                                    } else {
-                                        const int srow = net.hoff[sk.from] + m;
-                                        if (key_bit(key, srow)) {
-                                            const float4 c = ld4<float>(cr + (size_t)srow * 4);
-                                            o[0] -= c.x;
-                                            o[1] -= c.y;
-                                            o[2] -= c.z;
-                                            o[3] -= c.w;
-                                        }
-                                    }
-                                } else if (sk.from == 0) {
-                                    const float *tt = (const float *)sk.tmt;
-                                    o[0] += tt[m];
-                                    o[1] += tt[(size_t)sk.Mp + m];
-                                    o[2] += tt[2 * (size_t)sk.Mp + m];
-                                }
-                            }
-                            const float sg = key_bit(key, row) ? -1.f : 1.f;
-                            st4<float>(cr + (size_t)row * 4, make_float4(sg * o[0], sg * o[1], sg * o[2], sg * o[3]));
+                for (int it = 0; it < 4; ++it) {
+                    if (!acc_ok || it >= nit) break;
+                    const int mt = mt0 + it / ncbw, cb = cgrp + (it % ncbw) * ngrp;
+                    const float bm = it / ncbw == 0 ? bA : bB;
+                    // (eight columns at a time: fewer live registers; the
+                    // destination block by constant index: registers)
+                    const uint32_t ta = lane_base + (uint32_t)((mt - mt0) * ncols + cb * 16);
+                    const uint32_t tb = lane_base + (uint32_t)((mper + mt - mt0) * ncols + cb * 16);
+                    if (it < def_first) { // stored now
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            float v[8], vc[8];
+                            umma::tmem_ld8x2(ta + 8 * h, tb + 8 * h, v, vc);
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) o[0][8 * h + k] = (k & 3) == 3 ? v[k] + vc[k] + bm : v[k] + vc[k];
+                        }
+                        store_block(it);
+                    } else { // kept: into o[kKeep - 1] after the earlier kept ones moved up
+                        if (kKeep > 1) shift_o();
+#pragma unroll
+                        for (int h = 0; h < 2; ++h) {
+                            float v[8], vc[8];
+                            umma::tmem_ld8x2(ta + 8 * h, tb + 8 * h, v, vc);
+#pragma unroll
+                            for (int k = 0; k < 8; ++k)
+                                o[kKeep - 1][8 * h + k] = (k & 3) == 3 ? v[k] + vc[k] + bm : v[k] + vc[k];
                         }
                     }
                 }
+                for (int b = nkeep; b < kKeep; ++b) shift_o(); // the kept blocks from o[0] on
                 umma::fence_before(); // TMEM read out before the next products overwrite it
-                bar_builders();       // rows of hidden layer i + 1 written by every builder
-                if (mt1 < mtiles) load_items(0, 0, 0, pre);
+                nd = min(kKeep, (mt1 - mt0) * ncbu);
+                // the kept rows: stored during the next pass of this layer,
+                // or the next layer's first (whose early blocks read only rows
+                // of this layer's earlier passes and of this pass's first
+                // blocks ...), else now
+                const bool defer = mt1 < mtiles || (i < net.n_lin - 2 && nd <= 2 * mt0);
+                if (!defer) {
+                    for (int t2 = 0; t2 < nd; ++t2) {
+                        store_block(def_first + t2);
+                        shift_o();
+                    }
+                    nd = 0;
+                    bar_builders(); // rows of hidden layer i + 1 written by every builder
+                }
                 }
             }
 

@@ -206,5 +206,24 @@ __device__ __forceinline__ void tmem_ld16x2(uint32_t a, uint32_t b, float *v, fl
     }
 }
 
+// 32 lanes x 32 bit, 8 consecutive columns per thread from two addresses
+__device__ __forceinline__ void tmem_ld8x2(uint32_t a, uint32_t b, float *v, float *w)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%16];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%8,%9,%10,%11,%12,%13,%14,%15}, [%17];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(a), "r"(b)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        v[i] = __uint_as_float(r[i]);
+        w[i] = __uint_as_float(r[8 + i]);
+    }
+}
+
 } // namespace umma
 } // namespace am
