@@ -1111,7 +1111,8 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                 for (int it = 0; it < 4; ++it) {
                     if (!acc_ok || it >= nit) break;
                     const int mt = mt0 + it / ncbw, cb = cgrp + (it % ncbw) * ngrp;
-                    const float bm = it / ncbw == 0 ? bA : bB;
+                    const int mm = mt * 128 + q4 * 32 + lane;
+                    const float bm = mt == mt0 ? bA : (mt == mt0 + 1 ? bB : (mm < M ? bias[mm] : 0.f));
                     // (eight columns at a time: fewer live registers; the
                     // destination block by constant index: registers)
                     const uint32_t ta = lane_base + (uint32_t)((mt - mt0) * ncols + cb * 16);
