@@ -60,8 +60,8 @@ NCU_TRAFFIC_PER_REGION = {("sphere", "mixed"): {"compose": (1.214e6 + 45.631e6) 
                                                 "polygon": (109.571e6 + 4.067e6) / 12672},
                           # a wave of ~12,030 regions of a bounded march (the full march is too
                           # large to capture): per region, scaled to the step's regions
-                          ("large_skip", "mixed"): {"compose": (55.605e6 + 746.199e6) / 12030,
-                                                    "polygon": (805.019e6 + 15.494e6) / 12030},
+                          ("large_skip", "mixed"): {"compose": (52.502e6 + 747.137e6) / 12030,
+                                                    "polygon": (806.011e6 + 16.420e6) / 12030},
                           ("deep", "mixed"): {"compose": (27.491e6 + 957.757e6) / 40150,
                                               "polygon": (1018.464e6 + 20.326e6) / 40150}}
 

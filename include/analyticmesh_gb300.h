@@ -57,7 +57,10 @@ int am_analytic_marching(am_engine *engine, const void *const *weights, const vo
                          double iso, int flip_insideout, void *stream);
 
 /* CombineMesh -- backend/src/cuam_kernel.cu:185-200: weld vertices, index
- * faces; output vertex = vertex * scale + center. */
+ * faces; output vertex = vertex * scale + center.  The weld runs on the
+ * device over the polygon corners in use; the welded mesh stays in device
+ * memory (moved to the host only when it passes 8 GB) until am_get_mesh
+ * copies it into the caller's arrays or the next run replaces it. */
 int am_combine_mesh(am_engine *engine, double scale, const double *center3);
 
 /* ExportMesh -- backend/src/cuam_kernel.cu:205-246 (binary little-endian PLY,

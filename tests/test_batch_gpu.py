@@ -54,3 +54,31 @@ def test_batch_rejects_an_engine_twice():
     with pytest.raises(_lib.AmError):
         engine.run_batch([eng, eng], [net, net], [st, st], [pt, pt])
     eng.close()
+
+
+def test_batched_configuration_networks_against_float64():
+    """Networks of the batched configuration (64 networks, seeds 100..163;
+    here the small ones, so that their FP64 marches stay short) marched as
+    one mixed-precision batch: each against its own FP64 march, every
+    difference explained as in the single-network parity tests."""
+    from test_parity_gpu import assert_explained
+
+    pick = [2, 3, 12, 13, 55, 57]
+    models = wl.batched(64, 100)
+    nets, sts, pts = [], [], []
+    for i in pick:
+        m = models[i]
+        nets.append(wl.net_arrays(m))
+        st, pt = wl.seeds_for(m, init_num=1024, seed=100 + i)
+        sts.append(st)
+        pts.append(pt)
+    engines = [engine.Engine("mixed", n.nodes, n.arc_table, n.num_extra) for n in nets]
+    engine.run_batch(engines, nets, sts, pts)
+    for k, (eng, net) in enumerate(zip(engines, nets)):
+        f64 = engine.march(net, sts[k], pts[k], "float64")
+        assert eng.stats()["num_faces"] > 0
+        assert_explained(eng.regions(), f64.regions(), True, True)
+        rep = eng.error_report(0)
+        assert rep["max_abs_f"] <= 1e-5, (pick[k], rep)
+        f64.close()
+        eng.close()
