@@ -268,7 +268,7 @@ struct am_engine {
     double iso = 0.0;
     // mesh
     DevBuf w_table, w_rep, w_flag, w_vidx, w_bsum, w_fflag, w_fsize, w_fid, w_foff, w_verts, w_fs, w_fi, w_counts;
-    DevBuf w_voff, w_vsid; // compacted polygon vertex slots
+    DevBuf w_voff, w_vsid, w_wslot; // compacted polygon vertex slots, their keys' table slots
     std::vector<double> mesh_verts;
     std::vector<int32_t> mesh_fs, mesh_fi;
     bool mesh_host = false; // the welded mesh has been copied into the vectors above
@@ -1479,13 +1479,14 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
         long long V = 0;
         AM_CUDA(cudaMemcpyAsync(&V, wb.counts, sizeof(long long), cudaMemcpyDeviceToHost, st));
         AM_CUDA(cudaStreamSynchronize(st));
-        AM_CHECK(V < 0x7fffffffll, "too many polygon vertices for one mesh (2^31)");
+        AM_CHECK(V < (1ll << 30), "too many polygon vertices for one mesh (2^30)");
         const long long ns = std::max<long long>(V, 1);
         unsigned long long tcap = 1;
         while (tcap < (unsigned long long)ns * 2ull) tcap <<= 1;
         AM_CUDA(e->w_vsid.reserve(sizeof(long long) * ns));
         AM_CUDA(e->w_table.reserve(sizeof(unsigned long long) * tcap));
         AM_CUDA(e->w_rep.reserve(sizeof(int) * ns));
+        AM_CUDA(e->w_wslot.reserve(sizeof(unsigned) * ns));
         AM_CUDA(e->w_flag.reserve(sizeof(int) * ns));
         AM_CUDA(e->w_vidx.reserve(sizeof(int) * ns));
         AM_CUDA(e->w_bsum.reserve(sizeof(int) * (std::max(ns, nr) / 1024 + 2)));
@@ -1499,6 +1500,7 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
         wb.table = e->w_table.as<unsigned long long>();
         wb.mask = tcap - 1;
         wb.rep = e->w_rep.as<int>();
+        wb.wslot = e->w_wslot.as<unsigned>();
         wb.flag = e->w_flag.as<int>();
         wb.vidx = e->w_vidx.as<int>();
         wb.bsum = e->w_bsum.as<int>();
@@ -1525,7 +1527,8 @@ int am_combine_mesh(am_engine *e, double scale, const double *center3)
         // large weld buffers go back (many engines of a batch weld one after
         // the other): their mesh moves to the host first
         DevBuf *weld[] = {&e->w_table, &e->w_rep, &e->w_flag, &e->w_vidx, &e->w_bsum, &e->w_fflag, &e->w_fsize,
-                          &e->w_fid, &e->w_foff, &e->w_verts, &e->w_fs, &e->w_fi, &e->w_voff, &e->w_vsid};
+                          &e->w_fid, &e->w_foff, &e->w_verts, &e->w_fs, &e->w_fi, &e->w_voff, &e->w_vsid,
+                          &e->w_wslot};
         size_t held = 0;
         for (DevBuf *b : weld) held += b->bytes;
         if (held > ((size_t)8 << 30)) {

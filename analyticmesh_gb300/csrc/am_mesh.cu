@@ -126,22 +126,28 @@ __global__ void expand_slots_kernel(const int32_t *nv, long long R, const int *v
 // copies (the first in region order) represents it
 template <typename TS>
 __global__ void weld_insert_kernel(RegionsDev reg, const long long *vsid, long long V, int mode, int N, int W,
-                                   unsigned long long *table, unsigned long long mask, double mul, int *err)
+                                   unsigned long long *table, unsigned long long mask, double mul, unsigned *wslot,
+                                   int *err)
 {
     const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (j >= V) return;
+    wslot[j] = ~0u;
     const long long sid = vsid[j];
     VKey k;
     if (!make_key<TS>(reg, mode, N, W, mul, sid, k)) return;
     unsigned long long slot = k.h & mask;
     for (int probe = 0; probe < kMaxProbes; ++probe) {
         const unsigned long long cur = atomicCAS(table + slot, kEmpty, (unsigned long long)j);
-        if (cur == kEmpty) return;
+        if (cur == kEmpty) {
+            wslot[j] = (unsigned)slot;
+            return;
+        }
         const long long osid = vsid[cur];
         VKey o;
         make_key<TS>(reg, mode, N, W, mul, osid, o);
         if (o.h == k.h && same_vertex(reg, mode, N, W, k, sid, o, osid)) {
             atomicMin(table + slot, (unsigned long long)j);
+            wslot[j] = (unsigned)slot;
             return;
         }
         slot = (slot + (unsigned long long)probe + 1ull) & mask;
@@ -149,29 +155,14 @@ __global__ void weld_insert_kernel(RegionsDev reg, const long long *vsid, long l
     atomicOr(err, kErrTableFull);
 }
 
-template <typename TS>
-__global__ void weld_rep_kernel(RegionsDev reg, const long long *vsid, long long V, int mode, int N, int W,
-                                const unsigned long long *table, unsigned long long mask, double mul, int *rep, int *flag)
+// the representative: the table's value (the smallest index of the
+// vertex's copies) at the slot where the insert found or placed the key
+__global__ void weld_rep_kernel(long long V, const unsigned long long *table, const unsigned *wslot, int *rep, int *flag)
 {
     const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (j >= V) return;
-    const long long sid = vsid[j];
-    VKey k;
-    make_key<TS>(reg, mode, N, W, mul, sid, k);
-    unsigned long long slot = k.h & mask;
-    long long found = -1;
-    for (int probe = 0; probe < kMaxProbes; ++probe) {
-        const unsigned long long cur = table[slot];
-        if (cur == kEmpty) break;
-        const long long osid = vsid[cur];
-        VKey o;
-        make_key<TS>(reg, mode, N, W, mul, osid, o);
-        if (o.h == k.h && same_vertex(reg, mode, N, W, k, sid, o, osid)) {
-            found = (long long)cur;
-            break;
-        }
-        slot = (slot + (unsigned long long)probe + 1ull) & mask;
-    }
+    const unsigned sl = wslot[j];
+    const long long found = sl != ~0u ? (long long)table[sl] : -1;
     rep[j] = (int)found;
     flag[j] = (found == j) ? 1 : 0;
 }
@@ -325,15 +316,13 @@ void launch_weld(int prec, int mode, int N, int W, const RegionsDev &reg, long l
         return;
     }
     expand_slots_kernel<<<g2, 256, 0, st>>>(reg.nv, R, wb.voff, wb.vsid);
-    if (f64) {
-        weld_insert_kernel<double><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, d_err);
-        weld_rep_kernel<double><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, wb.rep,
-                                                    wb.flag);
-    } else {
-        weld_insert_kernel<float><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, d_err);
-        weld_rep_kernel<float><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, wb.rep,
-                                                   wb.flag);
-    }
+    if (f64)
+        weld_insert_kernel<double><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, wb.wslot,
+                                                       d_err);
+    else
+        weld_insert_kernel<float><<<g1, 256, 0, st>>>(reg, wb.vsid, V, mode, N, W, wb.table, wb.mask, mul, wb.wslot,
+                                                      d_err);
+    weld_rep_kernel<<<g1, 256, 0, st>>>(V, wb.table, wb.wslot, wb.rep, wb.flag);
     scan_exclusive(wb.flag, V, wb.vidx, wb.bsum, wb.counts + 0, st);
     if (f64)
         weld_verts_kernel<double><<<g1, 256, 0, st>>>(reg, wb.vsid, V, wb.rep, wb.vidx, scale, center[0], center[1],

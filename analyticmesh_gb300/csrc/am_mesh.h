@@ -12,6 +12,7 @@ struct WeldBuffers {
     long long *vsid;            // [V] vertex slot (region x kVMax + corner) of each compacted slot
     unsigned long long *table;  // weld hash table (compacted slot indices)
     unsigned long long mask;
+    unsigned *wslot;            // [V] table slot holding each compacted slot's key
     int *rep;                   // [V] representative compacted slot
     int *flag;                  // [V]
     int *vidx;                  // [V] output vertex index of each representative
