@@ -289,7 +289,10 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const 
     TA bnum = TA(1), bden = TA(0), bnum1 = TA(1), bden1 = TA(0);
     int bk = 0x7fffffff, bk1 = 0x7fffffff;
     bool nr = false;
-    auto consider = [&](int k, TA &bn, TA &bd, int &bi) {
+    // rows of one chain come in increasing k, so that a later row never
+    // wins a tie against the chain's earlier choice: the index test is only
+    // needed for the pruning list, whose rows come in any order
+    auto consider = [&](int k, TA &bn, TA &bd, int &bi, bool any_order) {
         const vec4_t<TR> r = rows[k];
         const TA rx = (TA)r.x, ry = (TA)r.y, rz = (TA)r.z, rw = (TA)r.w;
         const TA a = rx * d0 + ry * d1 + rz * d2;
@@ -304,7 +307,7 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const 
         }
         num = num > TA(0) ? num : TA(0);
         const TA lhs = num * bd, rhs = bn * a;
-        if (lhs < rhs || (lhs == rhs && k < bi)) {
+        if (lhs < rhs || (any_order && lhs == rhs && k < bi)) {
             bn = num;
             bd = a;
             bi = k;
@@ -313,17 +316,17 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const 
     if (list) { // the rows that survived pruning
         int j = k0;
         for (; j + kstep < nlist; j += 2 * kstep) {
-            consider(list[j], bnum, bden, bk);
-            consider(list[j + kstep], bnum1, bden1, bk1);
+            consider(list[j], bnum, bden, bk, true);
+            consider(list[j + kstep], bnum1, bden1, bk1, true);
         }
-        if (j < nlist) consider(list[j], bnum, bden, bk);
+        if (j < nlist) consider(list[j], bnum, bden, bk, true);
     } else {
         int k = k0;
         for (; k + kstep < ALL; k += 2 * kstep) {
-            consider(k, bnum, bden, bk);
-            consider(k + kstep, bnum1, bden1, bk1);
+            consider(k, bnum, bden, bk, false);
+            consider(k + kstep, bnum1, bden1, bk1, false);
         }
-        if (k < ALL) consider(k, bnum, bden, bk);
+        if (k < ALL) consider(k, bnum, bden, bk, false);
     }
     {
         const TA lhs = bnum1 * bden, rhs = bnum * bden1;
