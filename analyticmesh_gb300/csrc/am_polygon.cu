@@ -322,6 +322,7 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const 
         if (j < nlist) consider(list[j], bnum, bden, bk, true);
     } else {
         int k = k0;
+#pragma unroll 2
         for (; k + kstep < ALL; k += 2 * kstep) {
             consider(k, bnum, bden, bk, false);
             consider(k + kstep, bnum1, bden1, bk1, false);
