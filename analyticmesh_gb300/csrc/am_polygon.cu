@@ -219,6 +219,44 @@ constexpr int kListCap = 384;  // rows the pruned walk keeps at most (more: the 
 constexpr int kPruneMin = 96;  // fewer rows than this: no pruning
 constexpr int kRowWaitIters = 1 << 22; // bound of the wait for a face's rows (bulk copy)
 
+// Nearest rows first (FP32 scans of faces with at least kNearMin rows).  Each
+// row's value at the walk's start point v0, lowered by its FP32 evaluation
+// bound, is kept as an 8-bit lower bound (its float's exponent and top three
+// mantissa bits: exact truncation); the kNearK rows with the smallest codes
+// form the face's list, and lam is a lower bound of every other row's value
+// at v0.  A step scans the list; its best hit distance t |d| then decides: a
+// row outside the list has value >= lam - |c - v0|_1 at the current point c
+// (unit normals), so when that exceeds the hit distance and the near-zero
+// threshold, with margins well above FP32 rounding, no other row can be hit
+// first, tie, or lie near the point, and the full scan is skipped -- the
+// same hit, the same faces.
+constexpr int kNearMin = 1024;
+constexpr int kNearK = 128;
+
+__device__ __forceinline__ uint8_t near_code(float lb)
+{
+    if (!(lb >= 1.52587890625e-05f)) return 0; // below 2^-16 (or NaN): always listed
+    const int c = (int)(__float_as_uint(lb) >> 20) - (111 << 3) + 1;
+    return (uint8_t)min(c, 255);
+}
+__device__ __forceinline__ float near_decode(int c) // <= every lb coded c (c >= 1)
+{
+    return __uint_as_float((uint32_t)(c - 1 + (111 << 3)) << 20);
+}
+
+struct NearList {
+    const uint16_t *idx;
+    int n;
+    float lam; // lower bound of the unlisted rows' values at v0
+    float v0[3];
+};
+
+// per-face bytes of the codes and their histogram (FP32 scans of wide faces)
+__host__ __device__ constexpr size_t near_bytes(int ALL, int ALLP, int tc_bytes)
+{
+    return (tc_bytes == 4 && ALL >= kNearMin) ? ((size_t)ALLP + 15) / 16 * 16 + 256 * sizeof(uint32_t) : 0;
+}
+
 template <typename TC>
 struct GroupShared {
     long long rl;   // the group's region (chunk-local)
@@ -228,6 +266,8 @@ struct GroupShared {
     double btd[2][8]; // the same for a scan in FP64 over FP32 rows
     int bk[2][8];
     int nlist;      // rows kept by the pruning
+    int nl_n, nl_c; // the nearest-row list's length and its largest code (-1: no list)
+    float nl_lam;
     // phases of a face, one at a time (a barrier between any two): the seed
     // start search; row pruning, first the sample's extreme rows per warp
     // and direction, then (once every warp has read those) the list of the
@@ -427,9 +467,31 @@ template <typename TC, typename TS, bool kGroup, typename TA = TC, bool kNear = 
 __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
                      const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy, TS &vz,
                      int &ve, int &n, bool &closed, int8_t &status, int &sbk, int &sdec, int &nsteps, const Grp<TC> &g,
-                     bool *near = nullptr)
+                     bool *near = nullptr, const NearList *nl = nullptr)
 {
     constexpr bool kWide = sizeof(TA) > sizeof(TC); // FP64 scan over FP32 rows
+    int red = 0; // group reductions so far: their shared slots alternate
+    // the group's first hit: the warps' partial minima meet in shared memory
+    auto group_min = [&](TA &bt, int &bk) {
+        if (!kGroup) return;
+        const int par = red++ & 1;
+        TA *sbt = kWide ? (TA *)&g.sh->btd[par][0] : (TA *)&g.sh->bt[par][0];
+        if (lane == 0) {
+            sbt[g.gw] = bt;
+            g.sh->bk[par][g.gw] = bk;
+        }
+        g.sync();
+        bt = sbt[0];
+        bk = g.sh->bk[par][0];
+        for (int w = 1; w < g.G; ++w) {
+            const TA ot = sbt[w];
+            const int ok = g.sh->bk[par][w];
+            if (ot < bt || (ot == bt && ok < bk)) {
+                bt = ot;
+                bk = ok;
+            }
+        }
+    };
     TC cx = 0, cy = 0, cz = 0; // the vertex rounded to the scan precision
     vx = vy = vz = TS(0);
     ve = -1;
@@ -453,6 +515,7 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
         // first hit along the edge line, the scan split over the group
         TA bt;
         int bk;
+        bool reduced = false;
         if constexpr (kWide) {
             const TA q0 = (TA)eqv[0], q1 = (TA)eqv[1], q2 = (TA)eqv[2];
             const TA rx = (TA)ref_.x, ry = (TA)ref_.y, rz = (TA)ref_.z;
@@ -461,30 +524,32 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
             hit_scan_wide(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1, d2,
                           thr, curc[0], curc[1], curc[2], D0, D1, D2, thr64, cur[0], cur[1], cur[2], e, prev, bt, bk);
         } else {
-            bool nr = false;
-            hit_scan<TC, TC, kNear>(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0,
-                                    d1, d2, thr, curc[0], curc[1], curc[2], e, prev, bt, bk, nr);
+            const int k0 = kGroup ? 32 * g.gw + lane : lane, ks = kGroup ? 32 * g.G : 32;
+            bool nr = false, full = true;
+            if (nl && !list) { // the face's nearest rows first
+                hit_scan<TC, TC, kNear>(rows, ALL, nl->idx, nl->n, k0, ks, d0, d1, d2, thr, curc[0], curc[1], curc[2],
+                                        e, prev, bt, bk, nr);
+                group_min(bt, bk);
+                // every other row's value here is at least lam - |c - v0|_1:
+                // enough when that beats both the hit distance and the
+                // near-zero threshold by margins far above FP32 rounding
+                const float D = fabsf((float)curc[0] - nl->v0[0]) + fabsf((float)curc[1] - nl->v0[1]) +
+                                fabsf((float)curc[2] - nl->v0[2]);
+                const float cm = fabsf((float)curc[0]) + fabsf((float)curc[1]) + fabsf((float)curc[2]);
+                const float dn = sqrtf((float)(d0 * d0 + d1 * d1 + d2 * d2));
+                const float reach = bk == 0x7fffffff ? INFINITY : (float)bt * dn;
+                full = !(nl->lam - 1.000001f * D - 1e-5f * (1.f + cm) > fmaxf(reach * 1.0001f + 1e-6f, 3e-6f));
+            }
+            if (full) {
+                bool nf = false;
+                hit_scan<TC, TC, kNear>(rows, ALL, list, nlist, k0, ks, d0, d1, d2, thr, curc[0], curc[1], curc[2], e,
+                                        prev, bt, bk, nf);
+                nr = nr || nf;
+            }
             any_near = any_near || nr;
+            reduced = !full; // the list's minimum is the group's
         }
-        if (kGroup) {
-            const int par = step & 1;
-            TA *sbt = kWide ? (TA *)&g.sh->btd[par][0] : (TA *)&g.sh->bt[par][0];
-            if (lane == 0) {
-                sbt[g.gw] = bt;
-                g.sh->bk[par][g.gw] = bk;
-            }
-            g.sync();
-            bt = sbt[0];
-            bk = g.sh->bk[par][0];
-            for (int w = 1; w < g.G; ++w) {
-                const TA ot = sbt[w];
-                const int ok = g.sh->bk[par][w];
-                if (ot < bt || (ot == bt && ok < bk)) {
-                    bt = ot;
-                    bk = ok;
-                }
-            }
-        }
+        if (!reduced) group_min(bt, bk);
         if (bk == 0x7fffffff) { // the edge line never leaves the region
             status = kOpen;
             break;
@@ -583,7 +648,8 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
 template <typename TC, typename TS, bool kGroup>
 __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
                              const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy,
-                             TS &vz, int &ve, int &n, bool &closed, int8_t &status, const Grp<TC> &g)
+                             TS &vz, int &ve, int &n, bool &closed, int8_t &status, const Grp<TC> &g,
+                             const NearList *nl = nullptr)
 {
     const unsigned full = 0xffffffffu;
     const TC eqf[4] = {eqc.x, eqc.y, eqc.z, eqc.w};
@@ -594,7 +660,7 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *li
     int8_t fst = kOk;
     bool near = false;
     walk<TC, TC, kGroup, TC, true>(rows, ALL, list, nlist, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz,
-                                   fve, fn, fclosed, fst, sbk, sdec, nsteps, g, &near);
+                                   fve, fn, fclosed, fst, sbk, sdec, nsteps, g, &near, nl);
     if (kGroup) { // a row near a vertex in any warp's share of the scan
         if (near && lane == 0) atomicOr(&g.sh->near, 1);
         g.sync();
@@ -880,6 +946,20 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
     g.sh = reinterpret_cast<GroupShared<TC> *>(smem_raw + (size_t)F * net.ALLP * sizeof(vec4_t<TC>) +
                                                (size_t)gid * group_shared_bytes<TC>());
     // (the group's shared block also holds the pruning list: one per face)
+    // the face's nearest-row codes and their histogram, after the shared blocks
+    uint8_t *nlc = nullptr;
+    unsigned *nlh = nullptr;
+    {
+        const size_t nlb = near_bytes(ALL, net.ALLP, (int)sizeof(TC));
+        if (nlb) {
+            uint8_t *base = smem_raw + (size_t)F * net.ALLP * sizeof(vec4_t<TC>) + (size_t)F * group_shared_bytes<TC>() +
+                            (size_t)gid * nlb;
+            nlc = base;
+            nlh = reinterpret_cast<unsigned *>(base + nlb - 256 * sizeof(unsigned));
+            for (int i = 32 * g.gw + lane; i < 256; i += 32 * G) nlh[i] = 0u;
+            __syncwarp();
+        }
+    }
     const TC eps = (TC)tol.eps, par_eps = (TC)tol.par_eps;
     const TS same_eps = (TS)tol.same_eps;
 
@@ -929,6 +1009,15 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             }
             ++rphase;
         }
+        const TS *midp = (const TS *)reg.mid + (size_t)rid * 4;
+        TS p[3] = {midp[0], midp[1], midp[2]};
+        int s = reg.start[rid];
+        const bool is_seed = (s < 0);
+        // the nearest-row list (FP32 scans of wide faces; a seed's start
+        // point is found later, its face scans every row)
+        const bool nl_on = nlc != nullptr && !is_seed && !prune && (ALL + 32 * G - 1) / (32 * G) * G <= 256;
+        const float v0[3] = {(float)p[0], (float)p[1], (float)p[2]};
+        const float v0m = fabsf(v0[0]) + fabsf(v0[1]) + fabsf(v0[2]);
         for (int q = 32 * g.gw + lane; q < ALL; q += 32 * G) {
             vec4_t<TC> v = rows[q];
             const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
@@ -942,21 +1031,129 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
                 v.w = v.w > TC(0) ? TC(INFINITY) : (v.w < TC(0) ? TC(-INFINITY) : TC(NAN));
             }
             rows[q] = v;
+            if (nl_on) {
+                // value at v0 (the scan's formula), less its FP32 rounding
+                // bound; a row with a zero normal is never hit nor near
+                uint8_t c = 255;
+                if (n2 > TC(0)) {
+                    const float num0 = -((float)v.x * v0[0] + (float)v.y * v0[1] + (float)v.z * v0[2] + (float)v.w);
+                    c = near_code(num0 - 1e-6f * (v0m + fabsf((float)v.w)));
+                }
+                nlc[q] = c;
+                atomicAdd(nlh + c, 1u);
+            }
         }
         if (kGroup)
             g.sync();
         else
             __syncwarp();
+        NearList nlist_face{nullptr, 0, 0.f, {v0[0], v0[1], v0[2]}};
+        if (nl_on) {
+            // the largest code c* whose rows number at most kNearK (lanes
+            // take eight bins each; the histogram is cleared for the next face)
+            if (g.gw == 0) {
+                unsigned cnt[8], tot = 0u;
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    cnt[b] = nlh[8 * lane + b];
+                    nlh[8 * lane + b] = 0u;
+                    tot += cnt[b];
+                }
+                unsigned incl = tot;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += y;
+                }
+                unsigned cum = incl - tot;
+                int best = -1;
+#pragma unroll
+                for (int b = 0; b < 8; ++b) {
+                    cum += cnt[b];
+                    if (cum <= (unsigned)kNearK) best = 8 * lane + b;
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+                if (lane == 0) {
+                    g.sh->nl_c = best;
+                    g.sh->nl_n = 0;
+                    g.sh->nl_lam = best < 0 ? 0.f : (best >= 255 ? INFINITY : near_decode(best + 1));
+                }
+            }
+            if (kGroup)
+                g.sync();
+            else
+                __syncwarp();
+            const int cstar = g.sh->nl_c;
+            if (cstar >= 0) {
+                // the listed rows in index order (the scan's choice must not
+                // depend on where a row sits): per 32-row chunk of each
+                // warp, counts, their exclusive prefix, then ballot ranks;
+                // the cleared histogram holds the counts
+                const int per = 32 * G, nit = (ALL + per - 1) / per;
+                unsigned *cnt = nlh;
+                for (int i = 0; i < nit; ++i) {
+                    const int q = i * per + 32 * g.gw + lane;
+                    const unsigned m = __ballot_sync(0xffffffffu, q < ALL && nlc[q] <= cstar);
+                    if (lane == 0) cnt[i * G + g.gw] = __popc(m);
+                }
+                if (kGroup)
+                    g.sync();
+                else
+                    __syncwarp();
+                if (g.gw == 0) { // exclusive prefix of the nit * G <= 256 counts
+                    unsigned c8[8], tot = 0u;
+#pragma unroll
+                    for (int b = 0; b < 8; ++b) {
+                        const int j = 8 * lane + b;
+                        c8[b] = j < nit * G ? cnt[j] : 0u;
+                        tot += c8[b];
+                    }
+                    unsigned incl = tot;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += y;
+                    }
+                    unsigned run = incl - tot;
+#pragma unroll
+                    for (int b = 0; b < 8; ++b) {
+                        const int j = 8 * lane + b;
+                        if (j < nit * G) cnt[j] = run;
+                        run += c8[b];
+                    }
+                    if (lane == 31) g.sh->nl_n = (int)incl;
+                }
+                if (kGroup)
+                    g.sync();
+                else
+                    __syncwarp();
+                for (int i = 0; i < nit; ++i) {
+                    const int q = i * per + 32 * g.gw + lane;
+                    const bool in = q < ALL && nlc[q] <= cstar;
+                    const unsigned m = __ballot_sync(0xffffffffu, in);
+                    if (in) g.sh->list[cnt[i * G + g.gw] + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+                }
+            }
+            if (kGroup)
+                g.sync();
+            else
+                __syncwarp();
+            if (cstar >= 0) {
+                nlist_face.idx = g.sh->list;
+                nlist_face.n = g.sh->nl_n;
+                nlist_face.lam = g.sh->nl_lam;
+                // the histogram cleared again for the next face (it held the counts)
+                for (int i = 32 * g.gw + lane; i < 256; i += 32 * G) nlh[i] = 0u;
+            }
+        }
+        const bool nl_used = nlist_face.idx != nullptr;
         TS eqv[4];
         const vec4_t<TC> eqc = ld4<TC>((const TC *)ch.eq + (size_t)rl * 4); // scan precision copy
         eqv[0] = (TS)eqc.x;
         eqv[1] = (TS)eqc.y;
         eqv[2] = (TS)eqc.z;
         eqv[3] = (TS)eqc.w;
-        const TS *midp = (const TS *)reg.mid + (size_t)rid * 4;
-        TS p[3] = {midp[0], midp[1], midp[2]};
-        int s = reg.start[rid];
-        const bool is_seed = (s < 0);
         int8_t status = kOk;
 
         // ---------------------------------------------------- seed start search
@@ -1097,7 +1294,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             if (sizeof(TS) > sizeof(TC)) // scan-precision walk, vertices refined in the solve precision
             {
                 done = walk_refined<TC, TS, kGroup>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx,
-                                                    vy, vz, ve, n, closed, status, g);
+                                                    vy, vz, ve, n, closed, status, g, nl_used ? &nlist_face : nullptr);
                 if (kGroup) { // the leader's outcome for the group
                     if (g.gw == 0 && lane == 0) g.sh->done = done ? 1 : 0;
                     g.sync();
@@ -1112,7 +1309,8 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
                                                     vy, vz, ve, n, closed, status, sbk, sdec, nsteps, g);
                 } else {
                     walk<TC, TS, kGroup>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve,
-                                         n, closed, status, sbk, sdec, nsteps, g);
+                                         n, closed, status, sbk, sdec, nsteps, g, nullptr,
+                                         nl_used ? &nlist_face : nullptr);
                 }
             }
         }
@@ -1141,7 +1339,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         int kv = -1;
         if (leader && lane < n && ve >= 0 && ve < N && (closed || lane < n - 1) && !(!is_seed && ve == s)) kv = ve;
         if (kGroup) {
-            if (list) g.sync(); // every warp's walk has done with the pruning list
+            if (list || nl_used) g.sync(); // every warp's walk has done with the row list
             if (g.gw == 0) g.sh->ve[lane] = kv;
             g.sync();
             kv = g.sh->ve[lane];
@@ -1177,10 +1375,11 @@ int polygon_faces_per_block(size_t face_bytes, int G)
 
 // Automatic warps per face: eight warps per block, split between faces
 // and the warps of a face as the rows allow.
-int polygon_face_warps(int prec, int ALLP)
+int polygon_face_warps(int prec, int ALL, int ALLP)
 {
     const size_t face_bytes = prec == kFloat64 ? sizeof(double4) * (size_t)ALLP + group_shared_bytes<double>()
-                                               : sizeof(float4) * (size_t)ALLP + group_shared_bytes<float>();
+                                               : sizeof(float4) * (size_t)ALLP + group_shared_bytes<float>() +
+                                                     near_bytes(ALL, ALLP, 4);
     const int F = polygon_faces_per_block(face_bytes, 1);
     return 8 / F;
 }
@@ -1190,8 +1389,9 @@ void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, co
                 int *d_err, int G, int prune, unsigned long long *nfp64, cudaStream_t st)
 {
     const size_t row_bytes = sizeof(vec4_t<TC>) * (size_t)net.ALLP;
-    const int F = polygon_faces_per_block(row_bytes + group_shared_bytes<TC>(), G);
-    const size_t smem = (row_bytes + group_shared_bytes<TC>()) * F;
+    const size_t face_bytes = row_bytes + group_shared_bytes<TC>() + near_bytes(net.ALL, net.ALLP, (int)sizeof(TC));
+    const int F = polygon_faces_per_block(face_bytes, G);
+    const size_t smem = face_bytes * F;
     auto k = G > 1 ? polygon_kernel<TC, TS, true> : polygon_kernel<TC, TS, false>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int sms = device_sms();
@@ -1213,7 +1413,7 @@ void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const Ch
                     cudaStream_t st)
 {
     if (!ch.ctl && ch.count <= 0) return;
-    const int G = face_warps > 0 ? face_warps : polygon_face_warps(prec, net.ALLP);
+    const int G = face_warps > 0 ? face_warps : polygon_face_warps(prec, net.ALL, net.ALLP);
     if (prec == kFloat64)
         launch_one<double, double>(net, reg, ch, hs, tol, d_err, G, prune, nfp64, st);
     else if (prec == kMixed)
