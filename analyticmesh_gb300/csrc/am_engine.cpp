@@ -1224,7 +1224,7 @@ int am_autotune(am_engine *e, const am_run_args *x, int64_t sample_regions, int3
     };
     std::vector<int> cts = {0};
     if (e->prec == kMixed) cts = {1, 2, 3};
-    const int fws[] = {1, 2, 4, 8};
+    const int fws[] = {0, 1, 2, 4, 8}; // 0: the automatic choice (one warp per face from global rows when wide)
     double c = 0, p = 0;
     for (int ct : cts) sample(ct, 0, c, p); // untimed pass
     for (int fw : fws) sample(0, fw, c, p);

@@ -29,6 +29,8 @@
 #include <cuda/atomic>
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "am_device.cuh"
 #include "am_internal.h"
 #include "am_umma.cuh"
@@ -78,14 +80,50 @@ __device__ __forceinline__ bool finite_bits(double v)
 // same cost however few lanes are active.  Every lane returns the vertex in
 // the solve precision (V) and rounded to the scan precision (Vc); false if a
 // coordinate is not finite.
-template <typename TC, typename TS>
-__device__ __forceinline__ bool warp_solve(const vec4_t<TC> *rows, int a, int b, const TS *eqv, TS *V, TC *Vc,
-                                           int lane)
+// A face's rows, normalised (unit normal; a zero normal keeps an infinite
+// or NaN offset).  SmemRows: staged in shared memory and normalised there
+// once; GlobalRows: read from the constraint rows in global memory and
+// normalised on every read, by the same arithmetic.
+template <typename TC>
+__device__ __forceinline__ vec4_t<TC> normalize_row(vec4_t<TC> v)
 {
-    const TC *ra = reinterpret_cast<const TC *>(rows + a);
-    const TC *rb = reinterpret_cast<const TC *>(rows + b);
+    const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    if (n2 > TC(0)) {
+        const TC inv = rsqrt(n2); // as the reference's distance normalisation
+        v.x *= inv;
+        v.y *= inv;
+        v.z *= inv;
+        v.w *= inv;
+    } else {
+        v.w = v.w > TC(0) ? TC(INFINITY) : (v.w < TC(0) ? TC(-INFINITY) : TC(NAN));
+    }
+    return v;
+}
+template <typename TC>
+struct SmemRows {
+    const vec4_t<TC> *p;
+    __device__ __forceinline__ vec4_t<TC> operator[](int k) const { return p[k]; }
+};
+template <typename TC>
+struct GlobalRows {
+    const vec4_t<TC> *p;
+    __device__ __forceinline__ vec4_t<TC> operator[](int k) const
+    {
+        return normalize_row<TC>(ld4<TC>(reinterpret_cast<const TC *>(p + k)));
+    }
+};
+template <typename TC>
+__device__ __forceinline__ TC comp4(const vec4_t<TC> &v, int i)
+{
+    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+template <typename TC, typename TS, typename R>
+__device__ __forceinline__ bool warp_solve(const R &rows, int a, int b, const TS *eqv, TS *V, TC *Vc, int lane)
+{
+    const vec4_t<TC> ra = rows[a], rb = rows[b];
     const int c = lane & 7;
-    const TS cs = (TS)(c < 4 ? ra[c] : rb[c - 4]);
+    const TS cs = (TS)(c < 4 ? comp4<TC>(ra, c) : comp4<TC>(rb, c - 4));
     TS m[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) m[j] = __shfl_sync(0xffffffffu, cs, j);
@@ -219,7 +257,8 @@ constexpr int kListCap = 384;  // rows the pruned walk keeps at most (more: the 
 constexpr int kPruneMin = 96;  // fewer rows than this: no pruning
 constexpr int kRowWaitIters = 1 << 22; // bound of the wait for a face's rows (bulk copy)
 
-// Nearest rows first (FP32 scans of faces with at least kNearMin rows).  Each
+// Nearest rows first (the one-warp faces of wide networks read from global
+// memory, kGlob below, with at least kNearMin rows).  Each
 // row's value at the walk's start point v0, lowered by its FP32 evaluation
 // bound, is kept as an 8-bit lower bound (its float's exponent and top three
 // mantissa bits: exact truncation); the kNearK rows with the smallest codes
@@ -232,6 +271,7 @@ constexpr int kRowWaitIters = 1 << 22; // bound of the wait for a face's rows (b
 // same hit, the same faces.
 constexpr int kNearMin = 1024;
 constexpr int kNearK = 128;
+constexpr int kGlobMin = 2048; // rows from which a face is walked from global memory
 
 __device__ __forceinline__ uint8_t near_code(float lb)
 {
@@ -321,8 +361,8 @@ __host__ __device__ constexpr size_t group_shared_bytes()
 // current point lies on has |g| < 1e-6 there (the rows are normalised, so g
 // is a distance): a predicate near zero, which the mixed form takes again in
 // FP64.
-template <typename TR, typename TA, bool kNear>
-__device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const uint16_t *list, int nlist, int k0,
+template <typename TR, typename TA, bool kNear, typename R>
+__device__ __forceinline__ void hit_scan(const R &rows, int ALL, const uint16_t *list, int nlist, int k0,
                                          int kstep, TA d0, TA d1, TA d2, TA thr, TA c0, TA c1, TA c2, int e, int prev,
                                          TA &bt_out, int &bk_out, bool &near)
 {
@@ -398,7 +438,8 @@ __device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const 
 // a sign or feasibility decision near zero, taken in FP64.  The first hit is
 // the smaller of the FP32 candidates' best and the FP64 candidates' best,
 // compared in FP64, ties to the lower row.
-__device__ __forceinline__ void hit_scan_wide(const float4 *rows, int ALL, const uint16_t *list, int nlist, int k0,
+template <typename R>
+__device__ __forceinline__ void hit_scan_wide(const R &rows, int ALL, const uint16_t *list, int nlist, int k0,
                                               int kstep, float d0, float d1, float d2, float thr, float c0, float c1,
                                               float c2, double D0, double D1, double D2, double thr64, double C0,
                                               double C1, double C2, int e, int prev, double &bt_out, int &bk_out)
@@ -463,8 +504,8 @@ __device__ __forceinline__ void hit_scan_wide(const float4 *rows, int ALL, const
 // decision (sdec, 0 append, 1 merge with the previous vertex, 2 merge with
 // the first), nsteps the steps taken.  kNear: `near` (this warp) is set when
 // some step's scan met a row within 1e-6 of the current point.
-template <typename TC, typename TS, bool kGroup, typename TA = TC, bool kNear = false>
-__device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
+template <typename TC, typename TS, bool kGroup, typename TA = TC, bool kNear = false, typename R = SmemRows<TC>>
+__device__ void walk(const R &rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
                      const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy, TS &vz,
                      int &ve, int &n, bool &closed, int8_t &status, int &sbk, int &sdec, int &nsteps, const Grp<TC> &g,
                      bool *near = nullptr, const NearList *nl = nullptr)
@@ -645,8 +686,8 @@ __device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int 
 // near zero), when the TC walk did not close normally, took more than 32
 // steps or met a vertex that is not finite in TS, or when a decision comes
 // out differently in TS.
-template <typename TC, typename TS, bool kGroup>
-__device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
+template <typename TC, typename TS, bool kGroup, typename R>
+__device__ bool walk_refined(const R &rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
                              const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy,
                              TS &vz, int &ve, int &n, bool &closed, int8_t &status, const Grp<TC> &g,
                              const NearList *nl = nullptr)
@@ -681,11 +722,10 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *li
         const int pa = j == 0 ? s : pj;                    // and the edge plane it walked on
         const bool in = (unsigned)pa < (unsigned)ALL && (unsigned)pb < (unsigned)ALL;
         planes_ok = planes_ok && in;
-        const TC *ra = reinterpret_cast<const TC *>(rows + (in ? pa : 0));
-        const TC *rb = reinterpret_cast<const TC *>(rows + (in ? pb : 0));
+        const vec4_t<TC> ra = rows[in ? pa : 0], rb = rows[in ? pb : 0];
         // lane t of the group converts components 2t, 2t + 1 of [row a | row b]
-        const TS c0 = (TS)(L < 2 ? ra[2 * L] : rb[2 * L - 4]);
-        const TS c1 = (TS)(L < 2 ? ra[2 * L + 1] : rb[2 * L - 3]);
+        const TS c0 = (TS)(L < 2 ? comp4<TC>(ra, 2 * L) : comp4<TC>(rb, 2 * L - 4));
+        const TS c1 = (TS)(L < 2 ? comp4<TC>(ra, 2 * L + 1) : comp4<TC>(rb, 2 * L - 3));
         TS m[8];
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
@@ -770,8 +810,8 @@ __device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *li
 // rounding bound, so that its dual points are accurate.  Returns the number
 // of kept rows (their indices in sh->list), or -1 -- the walk scans every
 // row -- when the sample gives no circle or more than kListCap rows are kept.
-template <typename TC, bool kGroup>
-__device__ int prune_rows(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TC *pc, int lane,
+template <typename TC, bool kGroup, typename R>
+__device__ int prune_rows(const R &rows, int ALL, const vec4_t<TC> &eqc, const TC *pc, int lane,
                           const Grp<TC> &g)
 {
     const unsigned full = 0xffffffffu;
@@ -925,10 +965,16 @@ __device__ int prune_rows(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc
 // signed geometric distances are then plain dot products, the same quantity
 // the reference's feasibility test computes as (w.x + b) * rsqrt(|w|^2)
 // (kernel.h:729-795).  TC is the scan precision, TS the solve precision.
-template <typename TC, typename TS, bool kGroup>
+//
+// kGlob (FP32 scans of wide networks, one warp per face): the rows are not
+// staged; every read takes a row from global memory and normalises it, and a
+// face's walk scans its nearest rows (the list below) from L1, so that a
+// block holds eight faces and an SM twenty-four instead of three.
+template <typename TC, typename TS, bool kGroup, bool kGlob>
 __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
                                                       int G_, int prune, unsigned long long *nfp64, int *err)
 {
+    static_assert(!(kGlob && kGroup), "global rows: one warp per face");
     const int G = kGroup ? G_ : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -938,22 +984,21 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
     const int ALL = net.ALL;
     const int N = net.N;
     const int W = net.W;
-    vec4_t<TC> *rows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)gid * net.ALLP;
+    const size_t rows_region = kGlob ? 0 : (size_t)F * net.ALLP * sizeof(vec4_t<TC>);
+    vec4_t<TC> *srows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)gid * net.ALLP;
     Grp<TC> g;
     g.G = G;
     g.gw = wib % G;
     g.bar = 1 + gid;
-    g.sh = reinterpret_cast<GroupShared<TC> *>(smem_raw + (size_t)F * net.ALLP * sizeof(vec4_t<TC>) +
-                                               (size_t)gid * group_shared_bytes<TC>());
+    g.sh = reinterpret_cast<GroupShared<TC> *>(smem_raw + rows_region + (size_t)gid * group_shared_bytes<TC>());
     // (the group's shared block also holds the pruning list: one per face)
     // the face's nearest-row codes and their histogram, after the shared blocks
     uint8_t *nlc = nullptr;
     unsigned *nlh = nullptr;
     {
-        const size_t nlb = near_bytes(ALL, net.ALLP, (int)sizeof(TC));
+        const size_t nlb = kGlob ? near_bytes(ALL, net.ALLP, (int)sizeof(TC)) : 0;
         if (nlb) {
-            uint8_t *base = smem_raw + (size_t)F * net.ALLP * sizeof(vec4_t<TC>) + (size_t)F * group_shared_bytes<TC>() +
-                            (size_t)gid * nlb;
+            uint8_t *base = smem_raw + rows_region + (size_t)F * group_shared_bytes<TC>() + (size_t)gid * nlb;
             nlc = base;
             nlh = reinterpret_cast<unsigned *>(base + nlb - 256 * sizeof(unsigned));
             for (int i = 32 * g.gw + lane; i < 256; i += 32 * G) nlh[i] = 0u;
@@ -995,13 +1040,13 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         // the region's rows into shared memory by one bulk copy (the leader
         // issues it once every warp of the group is done with the previous
         // face's rows), then normalised in place
-        {
+        if (!kGlob) {
             const uint32_t rbytes = (uint32_t)ALL * (uint32_t)sizeof(vec4_t<TC>);
             if (!kGroup) __syncwarp(); // (a group has met at its barrier above)
             if (g.gw == 0 && lane == 0) {
                 umma::fence_proxy_async(); // earlier generic reads of the rows before the copy's writes
                 umma::mbar_expect_tx(&g.sh->rbar, rbytes);
-                umma::bulk_g2s(rows, grows, rbytes, &g.sh->rbar);
+                umma::bulk_g2s(srows, grows, rbytes, &g.sh->rbar);
             }
             if (!umma::mbar_wait(&g.sh->rbar, rphase & 1u, kRowWaitIters)) {
                 atomicOr(err, kErrWait);
@@ -1015,27 +1060,24 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         const bool is_seed = (s < 0);
         // the nearest-row list (FP32 scans of wide faces; a seed's start
         // point is found later, its face scans every row)
-        const bool nl_on = nlc != nullptr && !is_seed && !prune && (ALL + 32 * G - 1) / (32 * G) * G <= 256;
+        const bool nl_on = kGlob && nlc != nullptr && !is_seed && !prune && (ALL + 32 * G - 1) / (32 * G) * G <= 256;
         const float v0[3] = {(float)p[0], (float)p[1], (float)p[2]};
         const float v0m = fabsf(v0[0]) + fabsf(v0[1]) + fabsf(v0[2]);
-        for (int q = 32 * g.gw + lane; q < ALL; q += 32 * G) {
-            vec4_t<TC> v = rows[q];
-            const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
-            if (n2 > TC(0)) {
-                const TC inv = rsqrt(n2); // as the reference's distance normalisation
-                v.x *= inv;
-                v.y *= inv;
-                v.z *= inv;
-                v.w *= inv;
+        using Rows = std::conditional_t<kGlob, GlobalRows<TC>, SmemRows<TC>>;
+        const Rows rows{kGlob ? grows : srows};
+        for (int q = 32 * g.gw + lane; q < ALL && (!kGlob || nl_on); q += 32 * G) {
+            vec4_t<TC> v;
+            if constexpr (kGlob) {
+                v = rows[q];
             } else {
-                v.w = v.w > TC(0) ? TC(INFINITY) : (v.w < TC(0) ? TC(-INFINITY) : TC(NAN));
+                v = normalize_row<TC>(srows[q]);
+                srows[q] = v;
             }
-            rows[q] = v;
             if (nl_on) {
                 // value at v0 (the scan's formula), less its FP32 rounding
                 // bound; a row with a zero normal is never hit nor near
                 uint8_t c = 255;
-                if (n2 > TC(0)) {
+                if (v.x * v.x + v.y * v.y + v.z * v.z > TC(0)) {
                     const float num0 = -((float)v.x * v0[0] + (float)v.y * v0[1] + (float)v.z * v0[2] + (float)v.w);
                     c = near_code(num0 - 1e-6f * (v0m + fabsf((float)v.w)));
                 }
@@ -1377,9 +1419,9 @@ int polygon_faces_per_block(size_t face_bytes, int G)
 // and the warps of a face as the rows allow.
 int polygon_face_warps(int prec, int ALL, int ALLP)
 {
+    (void)ALL;
     const size_t face_bytes = prec == kFloat64 ? sizeof(double4) * (size_t)ALLP + group_shared_bytes<double>()
-                                               : sizeof(float4) * (size_t)ALLP + group_shared_bytes<float>() +
-                                                     near_bytes(ALL, ALLP, 4);
+                                               : sizeof(float4) * (size_t)ALLP + group_shared_bytes<float>();
     const int F = polygon_faces_per_block(face_bytes, 1);
     return 8 / F;
 }
@@ -1388,11 +1430,18 @@ template <typename TC, typename TS>
 void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs, const Tolerances &tol,
                 int *d_err, int G, int prune, unsigned long long *nfp64, cudaStream_t st)
 {
-    const size_t row_bytes = sizeof(vec4_t<TC>) * (size_t)net.ALLP;
-    const size_t face_bytes = row_bytes + group_shared_bytes<TC>() + near_bytes(net.ALL, net.ALLP, (int)sizeof(TC));
-    const int F = polygon_faces_per_block(face_bytes, G);
+    // global rows, one warp per face: FP32 scans of networks whose rows fill
+    // shared memory three faces to an SM (the automatic warps per face)
+    const bool glob = sizeof(TC) == 4 && net.ALL >= kGlobMin && G == 0 && !prune;
+    if (G == 0) G = polygon_face_warps(sizeof(TC) == 8 ? kFloat64 : kFloat32, net.ALL, net.ALLP);
+    if (glob) G = 1;
+    const size_t row_bytes = glob ? 0 : sizeof(vec4_t<TC>) * (size_t)net.ALLP;
+    const size_t face_bytes =
+        row_bytes + group_shared_bytes<TC>() + (glob ? near_bytes(net.ALL, net.ALLP, (int)sizeof(TC)) : 0);
+    const int F = glob ? 8 : polygon_faces_per_block(face_bytes, G);
     const size_t smem = face_bytes * F;
-    auto k = G > 1 ? polygon_kernel<TC, TS, true> : polygon_kernel<TC, TS, false>;
+    auto k = glob ? polygon_kernel<TC, TS, false, true>
+                  : (G > 1 ? polygon_kernel<TC, TS, true, false> : polygon_kernel<TC, TS, false, false>);
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int sms = device_sms();
     const int threads = 32 * F * G;
@@ -1413,7 +1462,7 @@ void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const Ch
                     cudaStream_t st)
 {
     if (!ch.ctl && ch.count <= 0) return;
-    const int G = face_warps > 0 ? face_warps : polygon_face_warps(prec, net.ALL, net.ALLP);
+    const int G = face_warps > 0 ? face_warps : 0; // 0: automatic (launch_one)
     if (prec == kFloat64)
         launch_one<double, double>(net, reg, ch, hs, tol, d_err, G, prune, nfp64, st);
     else if (prec == kMixed)
