@@ -1105,7 +1105,8 @@ int am_set_option(am_engine *e, int option, int64_t value)
         return AM_OK;
     }
     if (option == AM_OPT_FACE_WARPS) {
-        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8) return AM_ERR_INVALID_ARGUMENT;
+        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8 && value != 32)
+            return AM_ERR_INVALID_ARGUMENT;
         e->face_warps = (int)value;
         return AM_OK;
     }

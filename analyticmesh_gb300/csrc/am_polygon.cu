@@ -372,8 +372,7 @@ __device__ __forceinline__ void hit_scan(const R &rows, int ALL, const uint16_t 
     // rows of one chain come in increasing k, so that a later row never
     // wins a tie against the chain's earlier choice: the index test is only
     // needed for the pruning list, whose rows come in any order
-    auto consider = [&](int k, TA &bn, TA &bd, int &bi, bool any_order) {
-        const vec4_t<TR> r = rows[k];
+    auto consider = [&](int k, const vec4_t<TR> &r, TA &bn, TA &bd, int &bi, bool any_order) {
         const TA rx = (TA)r.x, ry = (TA)r.y, rz = (TA)r.z, rw = (TA)r.w;
         const TA a = rx * d0 + ry * d1 + rz * d2;
         TA num;
@@ -393,21 +392,35 @@ __device__ __forceinline__ void hit_scan(const R &rows, int ALL, const uint16_t 
             bi = k;
         }
     };
-    if (list) { // the rows that survived pruning
+    // (rows loaded four at a time ahead of their use: latency hidden also
+    // when they come from global memory)
+    if (list) { // a list of rows (pruning, or a face's nearest rows)
         int j = k0;
         for (; j + kstep < nlist; j += 2 * kstep) {
-            consider(list[j], bnum, bden, bk, true);
-            consider(list[j + kstep], bnum1, bden1, bk1, true);
+            const int ka = list[j], kb = list[j + kstep];
+            const vec4_t<TR> ra = rows[ka], rb = rows[kb];
+            consider(ka, ra, bnum, bden, bk, true);
+            consider(kb, rb, bnum1, bden1, bk1, true);
         }
-        if (j < nlist) consider(list[j], bnum, bden, bk, true);
+        if (j < nlist) consider(list[j], rows[list[j]], bnum, bden, bk, true);
     } else {
         int k = k0;
+        if constexpr (std::is_same_v<R, GlobalRows<TR>>)
+            for (; k + 3 * kstep < ALL; k += 4 * kstep) {
+                const vec4_t<TR> r0 = rows[k], r1 = rows[k + kstep], r2 = rows[k + 2 * kstep],
+                                 r3 = rows[k + 3 * kstep];
+                consider(k, r0, bnum, bden, bk, false);
+                consider(k + kstep, r1, bnum1, bden1, bk1, false);
+                consider(k + 2 * kstep, r2, bnum, bden, bk, false);
+                consider(k + 3 * kstep, r3, bnum1, bden1, bk1, false);
+            }
 #pragma unroll 2
         for (; k + kstep < ALL; k += 2 * kstep) {
-            consider(k, bnum, bden, bk, false);
-            consider(k + kstep, bnum1, bden1, bk1, false);
+            const vec4_t<TR> r0 = rows[k], r1 = rows[k + kstep];
+            consider(k, r0, bnum, bden, bk, false);
+            consider(k + kstep, r1, bnum1, bden1, bk1, false);
         }
-        if (k < ALL) consider(k, bnum, bden, bk, false);
+        if (k < ALL) consider(k, rows[k], bnum, bden, bk, false);
     }
     {
         const TA lhs = bnum1 * bden, rhs = bnum * bden1;
@@ -448,9 +461,8 @@ __device__ __forceinline__ void hit_scan_wide(const R &rows, int ALL, const uint
     int bk = 0x7fffffff;
     double tn = INFINITY;
     int tk = 0x7fffffff;
-    auto consider = [&](int k) {
+    auto consider = [&](int k, const float4 &r) {
         if (k == e || k == prev) return;
-        const float4 r = rows[k];
         const float g = r.x * c0 + r.y * c1 + r.z * c2 + r.w;
         if (fabsf(g) < 2e-6f) {
             const double a = (double)r.x * D0 + (double)r.y * D1 + (double)r.z * D2;
@@ -475,9 +487,18 @@ __device__ __forceinline__ void hit_scan_wide(const R &rows, int ALL, const uint
         }
     };
     if (list) {
-        for (int j = k0; j < nlist; j += kstep) consider(list[j]);
+        for (int j = k0; j < nlist; j += kstep) consider(list[j], rows[list[j]]);
     } else {
-        for (int k = k0; k < ALL; k += kstep) consider(k);
+        int k = k0;
+        if constexpr (std::is_same_v<R, GlobalRows<float>>)
+            for (; k + 3 * kstep < ALL; k += 4 * kstep) { // (four loads ahead of their use)
+                const float4 r0 = rows[k], r1 = rows[k + kstep], r2 = rows[k + 2 * kstep], r3 = rows[k + 3 * kstep];
+                consider(k, r0);
+                consider(k + kstep, r1);
+                consider(k + 2 * kstep, r2);
+                consider(k + 3 * kstep, r3);
+            }
+        for (; k < ALL; k += kstep) consider(k, rows[k]);
     }
     double bt = bk == 0x7fffffff ? INFINITY : (double)bnum / (double)bden;
     if (tk != 0x7fffffff && (tn < bt || (tn == bt && tk < bk))) {
@@ -1065,14 +1086,20 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         const float v0m = fabsf(v0[0]) + fabsf(v0[1]) + fabsf(v0[2]);
         using Rows = std::conditional_t<kGlob, GlobalRows<TC>, SmemRows<TC>>;
         const Rows rows{kGlob ? grows : srows};
-        for (int q = 32 * g.gw + lane; q < ALL && (!kGlob || nl_on); q += 32 * G) {
-            vec4_t<TC> v;
-            if constexpr (kGlob) {
-                v = rows[q];
-            } else {
-                v = normalize_row<TC>(srows[q]);
-                srows[q] = v;
-            }
+        constexpr int kB = kGlob ? 8 : 1; // rows per batch (global reads: eight in flight)
+        for (int q0 = 32 * g.gw + lane; q0 < ALL && (!kGlob || nl_on); q0 += kB * 32 * G) {
+          vec4_t<TC> vb[kB];
+#pragma unroll
+          for (int u = 0; u < kB; ++u) {
+              const int q = q0 + u * 32 * G;
+              if (q < ALL) vb[u] = kGlob ? ld4<TC>(reinterpret_cast<const TC *>(grows + q)) : srows[q];
+          }
+#pragma unroll
+          for (int u = 0; u < kB; ++u) {
+            const int q = q0 + u * 32 * G;
+            if (q >= ALL) break;
+            const vec4_t<TC> v = normalize_row<TC>(vb[u]);
+            if (!kGlob) srows[q] = v;
             if (nl_on) {
                 // value at v0 (the scan's formula), less its FP32 rounding
                 // bound; a row with a zero normal is never hit nor near
@@ -1084,6 +1111,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
                 nlc[q] = c;
                 atomicAdd(nlh + c, 1u);
             }
+          }
         }
         if (kGroup)
             g.sync();
@@ -1432,8 +1460,8 @@ void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, co
 {
     // global rows, one warp per face: FP32 scans of networks whose rows fill
     // shared memory three faces to an SM (the automatic warps per face)
-    const bool glob = sizeof(TC) == 4 && net.ALL >= kGlobMin && G == 0 && !prune;
-    if (G == 0) G = polygon_face_warps(sizeof(TC) == 8 ? kFloat64 : kFloat32, net.ALL, net.ALLP);
+    const bool glob = sizeof(TC) == 4 && !prune && (G == 32 || (G == 0 && net.ALL >= kGlobMin));
+    if (G == 0 || G == 32) G = polygon_face_warps(sizeof(TC) == 8 ? kFloat64 : kFloat32, net.ALL, net.ALLP);
     if (glob) G = 1;
     const size_t row_bytes = glob ? 0 : sizeof(vec4_t<TC>) * (size_t)net.ALLP;
     const size_t face_bytes =
