@@ -1105,8 +1105,7 @@ int am_set_option(am_engine *e, int option, int64_t value)
         return AM_OK;
     }
     if (option == AM_OPT_FACE_WARPS) {
-        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8 && value != 32)
-            return AM_ERR_INVALID_ARGUMENT;
+        if (value != 0 && value != 1 && value != 2 && value != 4 && value != 8) return AM_ERR_INVALID_ARGUMENT;
         e->face_warps = (int)value;
         return AM_OK;
     }
@@ -1225,7 +1224,7 @@ int am_autotune(am_engine *e, const am_run_args *x, int64_t sample_regions, int3
     };
     std::vector<int> cts = {0};
     if (e->prec == kMixed) cts = {1, 2, 3};
-    const int fws[] = {0, 1, 2, 4, 8}; // 0: the automatic choice (one warp per face from global rows when wide)
+    const int fws[] = {1, 2, 4, 8};
     double c = 0, p = 0;
     for (int ct : cts) sample(ct, 0, c, p); // untimed pass
     for (int fw : fws) sample(0, fw, c, p);

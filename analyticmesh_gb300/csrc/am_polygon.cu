@@ -29,8 +29,6 @@
 #include <cuda/atomic>
 #include <cuda_runtime.h>
 
-#include <type_traits>
-
 #include "am_device.cuh"
 #include "am_internal.h"
 #include "am_umma.cuh"
@@ -80,50 +78,14 @@ __device__ __forceinline__ bool finite_bits(double v)
 // same cost however few lanes are active.  Every lane returns the vertex in
 // the solve precision (V) and rounded to the scan precision (Vc); false if a
 // coordinate is not finite.
-// A face's rows, normalised (unit normal; a zero normal keeps an infinite
-// or NaN offset).  SmemRows: staged in shared memory and normalised there
-// once; GlobalRows: read from the constraint rows in global memory and
-// normalised on every read, by the same arithmetic.
-template <typename TC>
-__device__ __forceinline__ vec4_t<TC> normalize_row(vec4_t<TC> v)
+template <typename TC, typename TS>
+__device__ __forceinline__ bool warp_solve(const vec4_t<TC> *rows, int a, int b, const TS *eqv, TS *V, TC *Vc,
+                                           int lane)
 {
-    const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
-    if (n2 > TC(0)) {
-        const TC inv = rsqrt(n2); // as the reference's distance normalisation
-        v.x *= inv;
-        v.y *= inv;
-        v.z *= inv;
-        v.w *= inv;
-    } else {
-        v.w = v.w > TC(0) ? TC(INFINITY) : (v.w < TC(0) ? TC(-INFINITY) : TC(NAN));
-    }
-    return v;
-}
-template <typename TC>
-struct SmemRows {
-    const vec4_t<TC> *p;
-    __device__ __forceinline__ vec4_t<TC> operator[](int k) const { return p[k]; }
-};
-template <typename TC>
-struct GlobalRows {
-    const vec4_t<TC> *p;
-    __device__ __forceinline__ vec4_t<TC> operator[](int k) const
-    {
-        return normalize_row<TC>(ld4<TC>(reinterpret_cast<const TC *>(p + k)));
-    }
-};
-template <typename TC>
-__device__ __forceinline__ TC comp4(const vec4_t<TC> &v, int i)
-{
-    return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
-}
-
-template <typename TC, typename TS, typename R>
-__device__ __forceinline__ bool warp_solve(const R &rows, int a, int b, const TS *eqv, TS *V, TC *Vc, int lane)
-{
-    const vec4_t<TC> ra = rows[a], rb = rows[b];
+    const TC *ra = reinterpret_cast<const TC *>(rows + a);
+    const TC *rb = reinterpret_cast<const TC *>(rows + b);
     const int c = lane & 7;
-    const TS cs = (TS)(c < 4 ? comp4<TC>(ra, c) : comp4<TC>(rb, c - 4));
+    const TS cs = (TS)(c < 4 ? ra[c] : rb[c - 4]);
     TS m[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) m[j] = __shfl_sync(0xffffffffu, cs, j);
@@ -257,46 +219,6 @@ constexpr int kListCap = 384;  // rows the pruned walk keeps at most (more: the 
 constexpr int kPruneMin = 96;  // fewer rows than this: no pruning
 constexpr int kRowWaitIters = 1 << 22; // bound of the wait for a face's rows (bulk copy)
 
-// Nearest rows first (the one-warp faces of wide networks read from global
-// memory, kGlob below, with at least kNearMin rows).  Each
-// row's value at the walk's start point v0, lowered by its FP32 evaluation
-// bound, is kept as an 8-bit lower bound (its float's exponent and top three
-// mantissa bits: exact truncation); the kNearK rows with the smallest codes
-// form the face's list, and lam is a lower bound of every other row's value
-// at v0.  A step scans the list; its best hit distance t |d| then decides: a
-// row outside the list has value >= lam - |c - v0|_1 at the current point c
-// (unit normals), so when that exceeds the hit distance and the near-zero
-// threshold, with margins well above FP32 rounding, no other row can be hit
-// first, tie, or lie near the point, and the full scan is skipped -- the
-// same hit, the same faces.
-constexpr int kNearMin = 1024;
-constexpr int kNearK = 128;
-constexpr int kGlobMin = 2048; // rows from which a face is walked from global memory
-
-__device__ __forceinline__ uint8_t near_code(float lb)
-{
-    if (!(lb >= 1.52587890625e-05f)) return 0; // below 2^-16 (or NaN): always listed
-    const int c = (int)(__float_as_uint(lb) >> 20) - (111 << 3) + 1;
-    return (uint8_t)min(c, 255);
-}
-__device__ __forceinline__ float near_decode(int c) // <= every lb coded c (c >= 1)
-{
-    return __uint_as_float((uint32_t)(c - 1 + (111 << 3)) << 20);
-}
-
-struct NearList {
-    const uint16_t *idx;
-    int n;
-    float lam; // lower bound of the unlisted rows' values at v0
-    float v0[3];
-};
-
-// per-face bytes of the codes and their histogram (FP32 scans of wide faces)
-__host__ __device__ constexpr size_t near_bytes(int ALL, int ALLP, int tc_bytes)
-{
-    return (tc_bytes == 4 && ALL >= kNearMin) ? ((size_t)ALLP + 15) / 16 * 16 + 256 * sizeof(uint32_t) : 0;
-}
-
 template <typename TC>
 struct GroupShared {
     long long rl;   // the group's region (chunk-local)
@@ -306,8 +228,6 @@ struct GroupShared {
     double btd[2][8]; // the same for a scan in FP64 over FP32 rows
     int bk[2][8];
     int nlist;      // rows kept by the pruning
-    int nl_n, nl_c; // the nearest-row list's length and its largest code (-1: no list)
-    float nl_lam;
     // phases of a face, one at a time (a barrier between any two): the seed
     // start search; row pruning, first the sample's extreme rows per warp
     // and direction, then (once every warp has read those) the list of the
@@ -361,8 +281,8 @@ __host__ __device__ constexpr size_t group_shared_bytes()
 // current point lies on has |g| < 1e-6 there (the rows are normalised, so g
 // is a distance): a predicate near zero, which the mixed form takes again in
 // FP64.
-template <typename TR, typename TA, bool kNear, typename R>
-__device__ __forceinline__ void hit_scan(const R &rows, int ALL, const uint16_t *list, int nlist, int k0,
+template <typename TR, typename TA, bool kNear>
+__device__ __forceinline__ void hit_scan(const vec4_t<TR> *rows, int ALL, const uint16_t *list, int nlist, int k0,
                                          int kstep, TA d0, TA d1, TA d2, TA thr, TA c0, TA c1, TA c2, int e, int prev,
                                          TA &bt_out, int &bk_out, bool &near)
 {
@@ -372,7 +292,8 @@ __device__ __forceinline__ void hit_scan(const R &rows, int ALL, const uint16_t 
     // rows of one chain come in increasing k, so that a later row never
     // wins a tie against the chain's earlier choice: the index test is only
     // needed for the pruning list, whose rows come in any order
-    auto consider = [&](int k, const vec4_t<TR> &r, TA &bn, TA &bd, int &bi, bool any_order) {
+    auto consider = [&](int k, TA &bn, TA &bd, int &bi, bool any_order) {
+        const vec4_t<TR> r = rows[k];
         const TA rx = (TA)r.x, ry = (TA)r.y, rz = (TA)r.z, rw = (TA)r.w;
         const TA a = rx * d0 + ry * d1 + rz * d2;
         TA num;
@@ -392,35 +313,21 @@ __device__ __forceinline__ void hit_scan(const R &rows, int ALL, const uint16_t 
             bi = k;
         }
     };
-    // (rows loaded four at a time ahead of their use: latency hidden also
-    // when they come from global memory)
-    if (list) { // a list of rows (pruning, or a face's nearest rows)
+    if (list) { // the rows that survived pruning
         int j = k0;
         for (; j + kstep < nlist; j += 2 * kstep) {
-            const int ka = list[j], kb = list[j + kstep];
-            const vec4_t<TR> ra = rows[ka], rb = rows[kb];
-            consider(ka, ra, bnum, bden, bk, true);
-            consider(kb, rb, bnum1, bden1, bk1, true);
+            consider(list[j], bnum, bden, bk, true);
+            consider(list[j + kstep], bnum1, bden1, bk1, true);
         }
-        if (j < nlist) consider(list[j], rows[list[j]], bnum, bden, bk, true);
+        if (j < nlist) consider(list[j], bnum, bden, bk, true);
     } else {
         int k = k0;
-        if constexpr (std::is_same_v<R, GlobalRows<TR>>)
-            for (; k + 3 * kstep < ALL; k += 4 * kstep) {
-                const vec4_t<TR> r0 = rows[k], r1 = rows[k + kstep], r2 = rows[k + 2 * kstep],
-                                 r3 = rows[k + 3 * kstep];
-                consider(k, r0, bnum, bden, bk, false);
-                consider(k + kstep, r1, bnum1, bden1, bk1, false);
-                consider(k + 2 * kstep, r2, bnum, bden, bk, false);
-                consider(k + 3 * kstep, r3, bnum1, bden1, bk1, false);
-            }
 #pragma unroll 2
         for (; k + kstep < ALL; k += 2 * kstep) {
-            const vec4_t<TR> r0 = rows[k], r1 = rows[k + kstep];
-            consider(k, r0, bnum, bden, bk, false);
-            consider(k + kstep, r1, bnum1, bden1, bk1, false);
+            consider(k, bnum, bden, bk, false);
+            consider(k + kstep, bnum1, bden1, bk1, false);
         }
-        if (k < ALL) consider(k, rows[k], bnum, bden, bk, false);
+        if (k < ALL) consider(k, bnum, bden, bk, false);
     }
     {
         const TA lhs = bnum1 * bden, rhs = bnum * bden1;
@@ -451,8 +358,7 @@ __device__ __forceinline__ void hit_scan(const R &rows, int ALL, const uint16_t 
 // a sign or feasibility decision near zero, taken in FP64.  The first hit is
 // the smaller of the FP32 candidates' best and the FP64 candidates' best,
 // compared in FP64, ties to the lower row.
-template <typename R>
-__device__ __forceinline__ void hit_scan_wide(const R &rows, int ALL, const uint16_t *list, int nlist, int k0,
+__device__ __forceinline__ void hit_scan_wide(const float4 *rows, int ALL, const uint16_t *list, int nlist, int k0,
                                               int kstep, float d0, float d1, float d2, float thr, float c0, float c1,
                                               float c2, double D0, double D1, double D2, double thr64, double C0,
                                               double C1, double C2, int e, int prev, double &bt_out, int &bk_out)
@@ -461,8 +367,9 @@ __device__ __forceinline__ void hit_scan_wide(const R &rows, int ALL, const uint
     int bk = 0x7fffffff;
     double tn = INFINITY;
     int tk = 0x7fffffff;
-    auto consider = [&](int k, const float4 &r) {
+    auto consider = [&](int k) {
         if (k == e || k == prev) return;
+        const float4 r = rows[k];
         const float g = r.x * c0 + r.y * c1 + r.z * c2 + r.w;
         if (fabsf(g) < 2e-6f) {
             const double a = (double)r.x * D0 + (double)r.y * D1 + (double)r.z * D2;
@@ -487,18 +394,9 @@ __device__ __forceinline__ void hit_scan_wide(const R &rows, int ALL, const uint
         }
     };
     if (list) {
-        for (int j = k0; j < nlist; j += kstep) consider(list[j], rows[list[j]]);
+        for (int j = k0; j < nlist; j += kstep) consider(list[j]);
     } else {
-        int k = k0;
-        if constexpr (std::is_same_v<R, GlobalRows<float>>)
-            for (; k + 3 * kstep < ALL; k += 4 * kstep) { // (four loads ahead of their use)
-                const float4 r0 = rows[k], r1 = rows[k + kstep], r2 = rows[k + 2 * kstep], r3 = rows[k + 3 * kstep];
-                consider(k, r0);
-                consider(k + kstep, r1);
-                consider(k + 2 * kstep, r2);
-                consider(k + 3 * kstep, r3);
-            }
-        for (; k < ALL; k += kstep) consider(k, rows[k]);
+        for (int k = k0; k < ALL; k += kstep) consider(k);
     }
     double bt = bk == 0x7fffffff ? INFINITY : (double)bnum / (double)bden;
     if (tk != 0x7fffffff && (tn < bt || (tn == bt && tk < bk))) {
@@ -525,35 +423,13 @@ __device__ __forceinline__ void hit_scan_wide(const R &rows, int ALL, const uint
 // decision (sdec, 0 append, 1 merge with the previous vertex, 2 merge with
 // the first), nsteps the steps taken.  kNear: `near` (this warp) is set when
 // some step's scan met a row within 1e-6 of the current point.
-template <typename TC, typename TS, bool kGroup, typename TA = TC, bool kNear = false, typename R = SmemRows<TC>>
-__device__ void walk(const R &rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
+template <typename TC, typename TS, bool kGroup, typename TA = TC, bool kNear = false>
+__device__ void walk(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
                      const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy, TS &vz,
                      int &ve, int &n, bool &closed, int8_t &status, int &sbk, int &sdec, int &nsteps, const Grp<TC> &g,
-                     bool *near = nullptr, const NearList *nl = nullptr)
+                     bool *near = nullptr)
 {
     constexpr bool kWide = sizeof(TA) > sizeof(TC); // FP64 scan over FP32 rows
-    int red = 0; // group reductions so far: their shared slots alternate
-    // the group's first hit: the warps' partial minima meet in shared memory
-    auto group_min = [&](TA &bt, int &bk) {
-        if (!kGroup) return;
-        const int par = red++ & 1;
-        TA *sbt = kWide ? (TA *)&g.sh->btd[par][0] : (TA *)&g.sh->bt[par][0];
-        if (lane == 0) {
-            sbt[g.gw] = bt;
-            g.sh->bk[par][g.gw] = bk;
-        }
-        g.sync();
-        bt = sbt[0];
-        bk = g.sh->bk[par][0];
-        for (int w = 1; w < g.G; ++w) {
-            const TA ot = sbt[w];
-            const int ok = g.sh->bk[par][w];
-            if (ot < bt || (ot == bt && ok < bk)) {
-                bt = ot;
-                bk = ok;
-            }
-        }
-    };
     TC cx = 0, cy = 0, cz = 0; // the vertex rounded to the scan precision
     vx = vy = vz = TS(0);
     ve = -1;
@@ -577,7 +453,6 @@ __device__ void walk(const R &rows, int ALL, const uint16_t *list, int nlist, co
         // first hit along the edge line, the scan split over the group
         TA bt;
         int bk;
-        bool reduced = false;
         if constexpr (kWide) {
             const TA q0 = (TA)eqv[0], q1 = (TA)eqv[1], q2 = (TA)eqv[2];
             const TA rx = (TA)ref_.x, ry = (TA)ref_.y, rz = (TA)ref_.z;
@@ -586,32 +461,30 @@ __device__ void walk(const R &rows, int ALL, const uint16_t *list, int nlist, co
             hit_scan_wide(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0, d1, d2,
                           thr, curc[0], curc[1], curc[2], D0, D1, D2, thr64, cur[0], cur[1], cur[2], e, prev, bt, bk);
         } else {
-            const int k0 = kGroup ? 32 * g.gw + lane : lane, ks = kGroup ? 32 * g.G : 32;
-            bool nr = false, full = true;
-            if (nl && !list) { // the face's nearest rows first
-                hit_scan<TC, TC, kNear>(rows, ALL, nl->idx, nl->n, k0, ks, d0, d1, d2, thr, curc[0], curc[1], curc[2],
-                                        e, prev, bt, bk, nr);
-                group_min(bt, bk);
-                // every other row's value here is at least lam - |c - v0|_1:
-                // enough when that beats both the hit distance and the
-                // near-zero threshold by margins far above FP32 rounding
-                const float D = fabsf((float)curc[0] - nl->v0[0]) + fabsf((float)curc[1] - nl->v0[1]) +
-                                fabsf((float)curc[2] - nl->v0[2]);
-                const float cm = fabsf((float)curc[0]) + fabsf((float)curc[1]) + fabsf((float)curc[2]);
-                const float dn = sqrtf((float)(d0 * d0 + d1 * d1 + d2 * d2));
-                const float reach = bk == 0x7fffffff ? INFINITY : (float)bt * dn;
-                full = !(nl->lam - 1.000001f * D - 1e-5f * (1.f + cm) > fmaxf(reach * 1.0001f + 1e-6f, 3e-6f));
-            }
-            if (full) {
-                bool nf = false;
-                hit_scan<TC, TC, kNear>(rows, ALL, list, nlist, k0, ks, d0, d1, d2, thr, curc[0], curc[1], curc[2], e,
-                                        prev, bt, bk, nf);
-                nr = nr || nf;
-            }
+            bool nr = false;
+            hit_scan<TC, TC, kNear>(rows, ALL, list, nlist, kGroup ? 32 * g.gw + lane : lane, kGroup ? 32 * g.G : 32, d0,
+                                    d1, d2, thr, curc[0], curc[1], curc[2], e, prev, bt, bk, nr);
             any_near = any_near || nr;
-            reduced = !full; // the list's minimum is the group's
         }
-        if (!reduced) group_min(bt, bk);
+        if (kGroup) {
+            const int par = step & 1;
+            TA *sbt = kWide ? (TA *)&g.sh->btd[par][0] : (TA *)&g.sh->bt[par][0];
+            if (lane == 0) {
+                sbt[g.gw] = bt;
+                g.sh->bk[par][g.gw] = bk;
+            }
+            g.sync();
+            bt = sbt[0];
+            bk = g.sh->bk[par][0];
+            for (int w = 1; w < g.G; ++w) {
+                const TA ot = sbt[w];
+                const int ok = g.sh->bk[par][w];
+                if (ot < bt || (ot == bt && ok < bk)) {
+                    bt = ot;
+                    bk = ok;
+                }
+            }
+        }
         if (bk == 0x7fffffff) { // the edge line never leaves the region
             status = kOpen;
             break;
@@ -707,11 +580,10 @@ __device__ void walk(const R &rows, int ALL, const uint16_t *list, int nlist, co
 // near zero), when the TC walk did not close normally, took more than 32
 // steps or met a vertex that is not finite in TS, or when a decision comes
 // out differently in TS.
-template <typename TC, typename TS, bool kGroup, typename R>
-__device__ bool walk_refined(const R &rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
+template <typename TC, typename TS, bool kGroup>
+__device__ bool walk_refined(const vec4_t<TC> *rows, int ALL, const uint16_t *list, int nlist, const vec4_t<TC> &eqc,
                              const TS *eqv, const TS *p, int s, TC par_eps, TS same_eps, int lane, TS &vx, TS &vy,
-                             TS &vz, int &ve, int &n, bool &closed, int8_t &status, const Grp<TC> &g,
-                             const NearList *nl = nullptr)
+                             TS &vz, int &ve, int &n, bool &closed, int8_t &status, const Grp<TC> &g)
 {
     const unsigned full = 0xffffffffu;
     const TC eqf[4] = {eqc.x, eqc.y, eqc.z, eqc.w};
@@ -722,7 +594,7 @@ __device__ bool walk_refined(const R &rows, int ALL, const uint16_t *list, int n
     int8_t fst = kOk;
     bool near = false;
     walk<TC, TC, kGroup, TC, true>(rows, ALL, list, nlist, eqc, eqf, pf, s, par_eps, (TC)same_eps, lane, fx, fy, fz,
-                                   fve, fn, fclosed, fst, sbk, sdec, nsteps, g, &near, nl);
+                                   fve, fn, fclosed, fst, sbk, sdec, nsteps, g, &near);
     if (kGroup) { // a row near a vertex in any warp's share of the scan
         if (near && lane == 0) atomicOr(&g.sh->near, 1);
         g.sync();
@@ -743,10 +615,11 @@ __device__ bool walk_refined(const R &rows, int ALL, const uint16_t *list, int n
         const int pa = j == 0 ? s : pj;                    // and the edge plane it walked on
         const bool in = (unsigned)pa < (unsigned)ALL && (unsigned)pb < (unsigned)ALL;
         planes_ok = planes_ok && in;
-        const vec4_t<TC> ra = rows[in ? pa : 0], rb = rows[in ? pb : 0];
+        const TC *ra = reinterpret_cast<const TC *>(rows + (in ? pa : 0));
+        const TC *rb = reinterpret_cast<const TC *>(rows + (in ? pb : 0));
         // lane t of the group converts components 2t, 2t + 1 of [row a | row b]
-        const TS c0 = (TS)(L < 2 ? comp4<TC>(ra, 2 * L) : comp4<TC>(rb, 2 * L - 4));
-        const TS c1 = (TS)(L < 2 ? comp4<TC>(ra, 2 * L + 1) : comp4<TC>(rb, 2 * L - 3));
+        const TS c0 = (TS)(L < 2 ? ra[2 * L] : rb[2 * L - 4]);
+        const TS c1 = (TS)(L < 2 ? ra[2 * L + 1] : rb[2 * L - 3]);
         TS m[8];
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
@@ -831,8 +704,8 @@ __device__ bool walk_refined(const R &rows, int ALL, const uint16_t *list, int n
 // rounding bound, so that its dual points are accurate.  Returns the number
 // of kept rows (their indices in sh->list), or -1 -- the walk scans every
 // row -- when the sample gives no circle or more than kListCap rows are kept.
-template <typename TC, bool kGroup, typename R>
-__device__ int prune_rows(const R &rows, int ALL, const vec4_t<TC> &eqc, const TC *pc, int lane,
+template <typename TC, bool kGroup>
+__device__ int prune_rows(const vec4_t<TC> *rows, int ALL, const vec4_t<TC> &eqc, const TC *pc, int lane,
                           const Grp<TC> &g)
 {
     const unsigned full = 0xffffffffu;
@@ -986,16 +859,10 @@ __device__ int prune_rows(const R &rows, int ALL, const vec4_t<TC> &eqc, const T
 // signed geometric distances are then plain dot products, the same quantity
 // the reference's feasibility test computes as (w.x + b) * rsqrt(|w|^2)
 // (kernel.h:729-795).  TC is the scan precision, TS the solve precision.
-//
-// kGlob (FP32 scans of wide networks, one warp per face): the rows are not
-// staged; every read takes a row from global memory and normalises it, and a
-// face's walk scans its nearest rows (the list below) from L1, so that a
-// block holds eight faces and an SM twenty-four instead of three.
-template <typename TC, typename TS, bool kGroup, bool kGlob>
+template <typename TC, typename TS, bool kGroup>
 __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev reg, ChunkDev ch, HashDev hs, Tolerances tol,
                                                       int G_, int prune, unsigned long long *nfp64, int *err)
 {
-    static_assert(!(kGlob && kGroup), "global rows: one warp per face");
     const int G = kGroup ? G_ : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -1005,27 +872,14 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
     const int ALL = net.ALL;
     const int N = net.N;
     const int W = net.W;
-    const size_t rows_region = kGlob ? 0 : (size_t)F * net.ALLP * sizeof(vec4_t<TC>);
-    vec4_t<TC> *srows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)gid * net.ALLP;
+    vec4_t<TC> *rows = reinterpret_cast<vec4_t<TC> *>(smem_raw) + (size_t)gid * net.ALLP;
     Grp<TC> g;
     g.G = G;
     g.gw = wib % G;
     g.bar = 1 + gid;
-    g.sh = reinterpret_cast<GroupShared<TC> *>(smem_raw + rows_region + (size_t)gid * group_shared_bytes<TC>());
+    g.sh = reinterpret_cast<GroupShared<TC> *>(smem_raw + (size_t)F * net.ALLP * sizeof(vec4_t<TC>) +
+                                               (size_t)gid * group_shared_bytes<TC>());
     // (the group's shared block also holds the pruning list: one per face)
-    // the face's nearest-row codes and their histogram, after the shared blocks
-    uint8_t *nlc = nullptr;
-    unsigned *nlh = nullptr;
-    {
-        const size_t nlb = kGlob ? near_bytes(ALL, net.ALLP, (int)sizeof(TC)) : 0;
-        if (nlb) {
-            uint8_t *base = smem_raw + rows_region + (size_t)F * group_shared_bytes<TC>() + (size_t)gid * nlb;
-            nlc = base;
-            nlh = reinterpret_cast<unsigned *>(base + nlb - 256 * sizeof(unsigned));
-            for (int i = 32 * g.gw + lane; i < 256; i += 32 * G) nlh[i] = 0u;
-            __syncwarp();
-        }
-    }
     const TC eps = (TC)tol.eps, par_eps = (TC)tol.par_eps;
     const TS same_eps = (TS)tol.same_eps;
 
@@ -1061,13 +915,13 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         // the region's rows into shared memory by one bulk copy (the leader
         // issues it once every warp of the group is done with the previous
         // face's rows), then normalised in place
-        if (!kGlob) {
+        {
             const uint32_t rbytes = (uint32_t)ALL * (uint32_t)sizeof(vec4_t<TC>);
             if (!kGroup) __syncwarp(); // (a group has met at its barrier above)
             if (g.gw == 0 && lane == 0) {
                 umma::fence_proxy_async(); // earlier generic reads of the rows before the copy's writes
                 umma::mbar_expect_tx(&g.sh->rbar, rbytes);
-                umma::bulk_g2s(srows, grows, rbytes, &g.sh->rbar);
+                umma::bulk_g2s(rows, grows, rbytes, &g.sh->rbar);
             }
             if (!umma::mbar_wait(&g.sh->rbar, rphase & 1u, kRowWaitIters)) {
                 atomicOr(err, kErrWait);
@@ -1075,155 +929,34 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             }
             ++rphase;
         }
-        const TS *midp = (const TS *)reg.mid + (size_t)rid * 4;
-        TS p[3] = {midp[0], midp[1], midp[2]};
-        int s = reg.start[rid];
-        const bool is_seed = (s < 0);
-        // the nearest-row list (FP32 scans of wide faces; a seed's start
-        // point is found later, its face scans every row)
-        const bool nl_on = kGlob && nlc != nullptr && !is_seed && !prune && (ALL + 32 * G - 1) / (32 * G) * G <= 256;
-        const float v0[3] = {(float)p[0], (float)p[1], (float)p[2]};
-        const float v0m = fabsf(v0[0]) + fabsf(v0[1]) + fabsf(v0[2]);
-        using Rows = std::conditional_t<kGlob, GlobalRows<TC>, SmemRows<TC>>;
-        const Rows rows{kGlob ? grows : srows};
-        constexpr int kB = kGlob ? 8 : 1; // rows per batch (global reads: eight in flight)
-        for (int q0 = 32 * g.gw + lane; q0 < ALL && (!kGlob || nl_on); q0 += kB * 32 * G) {
-          vec4_t<TC> vb[kB];
-#pragma unroll
-          for (int u = 0; u < kB; ++u) {
-              const int q = q0 + u * 32 * G;
-              if (q < ALL) vb[u] = kGlob ? ld4<TC>(reinterpret_cast<const TC *>(grows + q)) : srows[q];
-          }
-#pragma unroll
-          for (int u = 0; u < kB; ++u) {
-            const int q = q0 + u * 32 * G;
-            if (q >= ALL) break;
-            const vec4_t<TC> v = normalize_row<TC>(vb[u]);
-            if (!kGlob) srows[q] = v;
-            if (nl_on) {
-                // value at v0 (the scan's formula), less its FP32 rounding
-                // bound; a row with a zero normal is never hit nor near
-                uint8_t c = 255;
-                if (v.x * v.x + v.y * v.y + v.z * v.z > TC(0)) {
-                    const float num0 = -((float)v.x * v0[0] + (float)v.y * v0[1] + (float)v.z * v0[2] + (float)v.w);
-                    c = near_code(num0 - 1e-6f * (v0m + fabsf((float)v.w)));
-                }
-                nlc[q] = c;
-                atomicAdd(nlh + c, 1u);
+        for (int q = 32 * g.gw + lane; q < ALL; q += 32 * G) {
+            vec4_t<TC> v = rows[q];
+            const TC n2 = v.x * v.x + v.y * v.y + v.z * v.z;
+            if (n2 > TC(0)) {
+                const TC inv = rsqrt(n2); // as the reference's distance normalisation
+                v.x *= inv;
+                v.y *= inv;
+                v.z *= inv;
+                v.w *= inv;
+            } else {
+                v.w = v.w > TC(0) ? TC(INFINITY) : (v.w < TC(0) ? TC(-INFINITY) : TC(NAN));
             }
-          }
+            rows[q] = v;
         }
         if (kGroup)
             g.sync();
         else
             __syncwarp();
-        NearList nlist_face{nullptr, 0, 0.f, {v0[0], v0[1], v0[2]}};
-        if (nl_on) {
-            // the largest code c* whose rows number at most kNearK (lanes
-            // take eight bins each; the histogram is cleared for the next face)
-            if (g.gw == 0) {
-                unsigned cnt[8], tot = 0u;
-#pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    cnt[b] = nlh[8 * lane + b];
-                    nlh[8 * lane + b] = 0u;
-                    tot += cnt[b];
-                }
-                unsigned incl = tot;
-#pragma unroll
-                for (int o = 1; o < 32; o <<= 1) {
-                    const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-                    if (lane >= o) incl += y;
-                }
-                unsigned cum = incl - tot;
-                int best = -1;
-#pragma unroll
-                for (int b = 0; b < 8; ++b) {
-                    cum += cnt[b];
-                    if (cum <= (unsigned)kNearK) best = 8 * lane + b;
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
-                if (lane == 0) {
-                    g.sh->nl_c = best;
-                    g.sh->nl_n = 0;
-                    g.sh->nl_lam = best < 0 ? 0.f : (best >= 255 ? INFINITY : near_decode(best + 1));
-                }
-            }
-            if (kGroup)
-                g.sync();
-            else
-                __syncwarp();
-            const int cstar = g.sh->nl_c;
-            if (cstar >= 0) {
-                // the listed rows in index order (the scan's choice must not
-                // depend on where a row sits): per 32-row chunk of each
-                // warp, counts, their exclusive prefix, then ballot ranks;
-                // the cleared histogram holds the counts
-                const int per = 32 * G, nit = (ALL + per - 1) / per;
-                unsigned *cnt = nlh;
-                for (int i = 0; i < nit; ++i) {
-                    const int q = i * per + 32 * g.gw + lane;
-                    const unsigned m = __ballot_sync(0xffffffffu, q < ALL && nlc[q] <= cstar);
-                    if (lane == 0) cnt[i * G + g.gw] = __popc(m);
-                }
-                if (kGroup)
-                    g.sync();
-                else
-                    __syncwarp();
-                if (g.gw == 0) { // exclusive prefix of the nit * G <= 256 counts
-                    unsigned c8[8], tot = 0u;
-#pragma unroll
-                    for (int b = 0; b < 8; ++b) {
-                        const int j = 8 * lane + b;
-                        c8[b] = j < nit * G ? cnt[j] : 0u;
-                        tot += c8[b];
-                    }
-                    unsigned incl = tot;
-#pragma unroll
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const unsigned y = __shfl_up_sync(0xffffffffu, incl, o);
-                        if (lane >= o) incl += y;
-                    }
-                    unsigned run = incl - tot;
-#pragma unroll
-                    for (int b = 0; b < 8; ++b) {
-                        const int j = 8 * lane + b;
-                        if (j < nit * G) cnt[j] = run;
-                        run += c8[b];
-                    }
-                    if (lane == 31) g.sh->nl_n = (int)incl;
-                }
-                if (kGroup)
-                    g.sync();
-                else
-                    __syncwarp();
-                for (int i = 0; i < nit; ++i) {
-                    const int q = i * per + 32 * g.gw + lane;
-                    const bool in = q < ALL && nlc[q] <= cstar;
-                    const unsigned m = __ballot_sync(0xffffffffu, in);
-                    if (in) g.sh->list[cnt[i * G + g.gw] + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
-                }
-            }
-            if (kGroup)
-                g.sync();
-            else
-                __syncwarp();
-            if (cstar >= 0) {
-                nlist_face.idx = g.sh->list;
-                nlist_face.n = g.sh->nl_n;
-                nlist_face.lam = g.sh->nl_lam;
-                // the histogram cleared again for the next face (it held the counts)
-                for (int i = 32 * g.gw + lane; i < 256; i += 32 * G) nlh[i] = 0u;
-            }
-        }
-        const bool nl_used = nlist_face.idx != nullptr;
         TS eqv[4];
         const vec4_t<TC> eqc = ld4<TC>((const TC *)ch.eq + (size_t)rl * 4); // scan precision copy
         eqv[0] = (TS)eqc.x;
         eqv[1] = (TS)eqc.y;
         eqv[2] = (TS)eqc.z;
         eqv[3] = (TS)eqc.w;
+        const TS *midp = (const TS *)reg.mid + (size_t)rid * 4;
+        TS p[3] = {midp[0], midp[1], midp[2]};
+        int s = reg.start[rid];
+        const bool is_seed = (s < 0);
         int8_t status = kOk;
 
         // ---------------------------------------------------- seed start search
@@ -1364,7 +1097,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
             if (sizeof(TS) > sizeof(TC)) // scan-precision walk, vertices refined in the solve precision
             {
                 done = walk_refined<TC, TS, kGroup>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx,
-                                                    vy, vz, ve, n, closed, status, g, nl_used ? &nlist_face : nullptr);
+                                                    vy, vz, ve, n, closed, status, g);
                 if (kGroup) { // the leader's outcome for the group
                     if (g.gw == 0 && lane == 0) g.sh->done = done ? 1 : 0;
                     g.sync();
@@ -1379,8 +1112,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
                                                     vy, vz, ve, n, closed, status, sbk, sdec, nsteps, g);
                 } else {
                     walk<TC, TS, kGroup>(rows, ALL, list, nlist, eqc, eqv, p, s, par_eps, same_eps, lane, vx, vy, vz, ve,
-                                         n, closed, status, sbk, sdec, nsteps, g, nullptr,
-                                         nl_used ? &nlist_face : nullptr);
+                                         n, closed, status, sbk, sdec, nsteps, g);
                 }
             }
         }
@@ -1409,7 +1141,7 @@ __global__ void __launch_bounds__(256, 3) polygon_kernel(NetDev net, RegionsDev 
         int kv = -1;
         if (leader && lane < n && ve >= 0 && ve < N && (closed || lane < n - 1) && !(!is_seed && ve == s)) kv = ve;
         if (kGroup) {
-            if (list || nl_used) g.sync(); // every warp's walk has done with the row list
+            if (list) g.sync(); // every warp's walk has done with the pruning list
             if (g.gw == 0) g.sh->ve[lane] = kv;
             g.sync();
             kv = g.sh->ve[lane];
@@ -1445,9 +1177,8 @@ int polygon_faces_per_block(size_t face_bytes, int G)
 
 // Automatic warps per face: eight warps per block, split between faces
 // and the warps of a face as the rows allow.
-int polygon_face_warps(int prec, int ALL, int ALLP)
+int polygon_face_warps(int prec, int ALLP)
 {
-    (void)ALL;
     const size_t face_bytes = prec == kFloat64 ? sizeof(double4) * (size_t)ALLP + group_shared_bytes<double>()
                                                : sizeof(float4) * (size_t)ALLP + group_shared_bytes<float>();
     const int F = polygon_faces_per_block(face_bytes, 1);
@@ -1458,18 +1189,10 @@ template <typename TC, typename TS>
 void launch_one(const NetDev &net, const RegionsDev &reg, const ChunkDev &ch, const HashDev &hs, const Tolerances &tol,
                 int *d_err, int G, int prune, unsigned long long *nfp64, cudaStream_t st)
 {
-    // global rows, one warp per face: FP32 scans of networks whose rows fill
-    // shared memory three faces to an SM (the automatic warps per face)
-    const bool glob = sizeof(TC) == 4 && !prune && (G == 32 || (G == 0 && net.ALL >= kGlobMin));
-    if (G == 0 || G == 32) G = polygon_face_warps(sizeof(TC) == 8 ? kFloat64 : kFloat32, net.ALL, net.ALLP);
-    if (glob) G = 1;
-    const size_t row_bytes = glob ? 0 : sizeof(vec4_t<TC>) * (size_t)net.ALLP;
-    const size_t face_bytes =
-        row_bytes + group_shared_bytes<TC>() + (glob ? near_bytes(net.ALL, net.ALLP, (int)sizeof(TC)) : 0);
-    const int F = glob ? 8 : polygon_faces_per_block(face_bytes, G);
-    const size_t smem = face_bytes * F;
-    auto k = glob ? polygon_kernel<TC, TS, false, true>
-                  : (G > 1 ? polygon_kernel<TC, TS, true, false> : polygon_kernel<TC, TS, false, false>);
+    const size_t row_bytes = sizeof(vec4_t<TC>) * (size_t)net.ALLP;
+    const int F = polygon_faces_per_block(row_bytes + group_shared_bytes<TC>(), G);
+    const size_t smem = (row_bytes + group_shared_bytes<TC>()) * F;
+    auto k = G > 1 ? polygon_kernel<TC, TS, true> : polygon_kernel<TC, TS, false>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     const int sms = device_sms();
     const int threads = 32 * F * G;
@@ -1490,7 +1213,7 @@ void launch_polygon(int prec, const NetDev &net, const RegionsDev &reg, const Ch
                     cudaStream_t st)
 {
     if (!ch.ctl && ch.count <= 0) return;
-    const int G = face_warps > 0 ? face_warps : 0; // 0: automatic (launch_one)
+    const int G = face_warps > 0 ? face_warps : polygon_face_warps(prec, net.ALLP);
     if (prec == kFloat64)
         launch_one<double, double>(net, reg, ch, hs, tol, d_err, G, prune, nfp64, st);
     else if (prec == kMixed)

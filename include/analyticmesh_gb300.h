@@ -193,12 +193,8 @@ typedef enum {
                                  passes, so that TMEM holds accumulators for twice as many regions (layers
                                  of 512 units).  All give the same bits. */
     AM_OPT_FACE_WARPS = 7,    /* warps per face polygon: 0 (default) automatic (one for narrow networks,
-                                 up to eight for wide ones, whose rows leave room for few faces per SM;
-                                 FP32 scans of 2,048 rows or more: one warp per face reading its rows
-                                 from global memory, nearest rows first), or 1, 2, 4, 8 (rows staged in
-                                 shared memory; the warps of a face split the walk's scan over them), or
-                                 32 (one warp per face from global memory, for any width).  The same
-                                 faces up to FP32 ties, which the mixed form's FP64 re-walks settle. */
+                                 up to eight for wide ones, whose rows leave room for few faces per SM),
+                                 or 1, 2, 4, 8.  The warps of a face split the walk's scan over the rows. */
     AM_OPT_TABLE_SLOTS = 8,   /* region hash table: 0 (default) sized by the engine (load factor <= 1/2,
                                  grown as regions are found); n > 0: fixed at n slots rounded up to a
                                  power of two, never grown.  A run that outgrows a fixed table returns
