@@ -958,16 +958,15 @@ __global__ void __launch_bounds__(kSThreads, 1) compose_tcs_kernel(NetDev net, T
                 }
             };
             const int nchunks = (R * 64 + 4 * kSBuild - 1) / (4 * kSBuild);
-            // The epilogue of a pass reads its accumulators into registers
-            // (warp w: TMEM lanes 32 (w % 4).., column blocks cgrp, cgrp +
-            // ngrp, ... of each M tile; at most four blocks of 16 columns),
-            // which frees TMEM for the next pass at once, and its rows are
-            // stored during the next pass's first steps, one column block a
-            // step, while the tensor core works (measured on GB300: a pass's
-            // 128 KB of rows take ~4 K cycles of the SM's store bandwidth
-            // alone, and the stores before the next products left the
-            // tensor core idle for a third of the time).  A barrier follows
-            // the last deferred store, so that later loads see the rows.
+            // The epilogue of a pass reads its accumulators (warp w: TMEM
+            // lanes 32 (w % 4).., column blocks cgrp, cgrp + ngrp, ... of each
+            // M tile; at most four blocks of 16 columns) and stores their rows,
+            // except the last block, which stays in registers and is stored
+            // during the next pass's first step, while the tensor core works
+            // (a pass's 128 KB of rows take ~4 K cycles of the SM's store
+            // bandwidth alone, measured on GB300; registers allow one block).
+            // A barrier follows the deferred store, so that later loads see
+            // the rows.
             const int ncb = ncols / 16;
             const int ncbw = cgrp < ncb ? (ncb - cgrp + ngrp - 1) / ngrp : 0; // this warp's column blocks
             const int ncbu = (ncb + ngrp - 1) / ngrp;                          // the most any warp has
