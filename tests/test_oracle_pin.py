@@ -71,6 +71,26 @@ def test_oracle_matches_reference_live(factory, dtype):
     assert CM.exact_mesh(mo, mr)
 
 
+@_live
+@pytest.mark.parametrize("dtype", ["float32", "float64"])
+def test_oracle_matches_reference_live_level_flip_extra_and_hidden_transform(dtype):
+    """The iso level, the inside-out flip, extra constraints (three planes of
+    a box corner) and a transform between hidden layers of uneven widths, all
+    in one run."""
+    m = wl.geometric([20, 50, 20, 80, 20], 13, skips=[[0], [1, 1, 0], [1, 1, 1], [0], [0]],
+                     tm_shapes=[[0, 0], [80, 20]])
+    we = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0]], float) + 1e-8
+    be = np.array([-0.2, -0.3, -0.1])
+    net = wl.net_arrays(m, we, be)
+    st, pt = wl.seeds_for(m, init_num=128, seed=12, iso=0.05, w_extra=we, b_extra=be)
+    kw = dict(iso=0.05, flip=True, dtype=dtype, combine=(1.5, [0.0, 0.1, -0.1]))
+    ro, mo = O.run_oracle(net, st, pt, **kw)
+    rr, mr = O.run_ref(net, st, pt, **kw)
+    assert ro.num > 0
+    assert CM.exact_records(ro, rr) == []
+    assert CM.exact_mesh(mo, mr)
+
+
 def test_oracle_seed_independence_and_deduplication():
     """A connected surface: one seed reaches every region; seeds given three
     times in shuffled order keep one of each state."""
